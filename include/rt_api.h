@@ -1,0 +1,258 @@
+/* rt_api.h -- C ABI of the GB300 path tracer (librtxplay_gb300.so).
+ *
+ * Drop-in boundary for the render path behind RTXplay's Scene / Thing /
+ * Optics / Camera / Launcher classes and the rtwo launcher (reference project
+ * otabuzzman/RTXplay, directory optx/).  Every function is extern "C", takes
+ * plain pointers and sizes, returns an rt_status and never throws.  Device
+ * buffers named in rt_frame are caller-owned device pointers; everything
+ * behind an opaque handle is library-owned.  A failing call leaves a message
+ * for rt_last_error_string() in the calling thread.
+ *
+ * Streams are passed as `void*` holding a cudaStream_t (NULL = legacy default
+ * stream).  All launches on a stream are asynchronous unless stated.
+ */
+#ifndef RT_API_H
+#define RT_API_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status */
+typedef enum {
+    RT_OK = 0,
+    RT_ERR_INVALID_ARG = 1,   /* bad handle, id, size or flag; Scene::set/get's `false` (optx/scene.cxx:198-225) */
+    RT_ERR_CUDA = 2,          /* a CUDA runtime call failed; CUDA_CHECK's throw (optx/util_cpu.h:18-28) */
+    RT_ERR_OUT_OF_MEMORY = 3,
+    RT_ERR_NOT_BUILT = 4,     /* render or update before rt_scene_build */
+    RT_ERR_LIMIT = 5,         /* an internal iteration limit was reached (device error word set) */
+    RT_ERR_INTERNAL = 6
+} rt_status;
+
+/* Message of the last failing call in this thread ("" if none). */
+const char* rt_last_error_string(void);
+/* Library version string, e.g. "rtxplay_gb300 0.1 sm_103a". */
+const char* rt_version(void);
+
+/* ------------------------------------------------------------- data types */
+typedef struct { float x, y, z; } rt_float3;
+typedef struct { unsigned int x, y, z; } rt_uint3;
+typedef struct { unsigned char x, y, z, w; } rt_uchar4;
+
+/* Optics: flattened form of the tagged union Optics{type; Diffuse{albedo} /
+ * Reflect{albedo,fuzz} / Refract{index}} of optx/thing.h:17-52. */
+typedef enum { RT_OPTICS_DIFFUSE = 0, RT_OPTICS_REFLECT = 1, RT_OPTICS_REFRACT = 2 } rt_optics_type;
+typedef struct {
+    int type;          /* rt_optics_type */
+    rt_float3 albedo;  /* Diffuse, Reflect */
+    float fuzz;        /* Reflect */
+    float index;       /* Refract */
+} rt_optics;
+
+/* Camera: host-side state of class Camera (optx/camera.h:28-94).  Filled by
+ * rt_camera_set; the derived basis and viewport vectors are what the device
+ * ray generator (optx/camera.h:67-77) reads. */
+typedef struct {
+    rt_float3 eye, pat, vup;
+    float fov, aspratio, aperture, fostance;
+    rt_float3 u, v, w, hvec, wvec, dvec;
+} rt_camera;
+
+/* Per-launch parameters: the render fields of LpGeneral (optx/rtwo.h:26-52)
+ * plus the counter-RNG seed and the sky colours of __miss__ambient
+ * (optx/camera_i.cu:130-139; ambient is the miss SBT record of
+ * optx/rtwo.cxx:110-111, white the constant of optx/camera_i.cu:137). */
+typedef struct {
+    unsigned int image_w, image_h;
+    unsigned int spp;        /* samples per pixel, >= 1 */
+    unsigned int depth;      /* rays per path, 1..255; a hit on the depth-th ray is black */
+    unsigned int seed;       /* counter-RNG key */
+    unsigned int flags;      /* RT_FLAG_* */
+    rt_float3 ambient;       /* default (0.5, 0.7, 1.0) */
+    rt_float3 white;         /* default (1, 1, 1) */
+} rt_launch_params;
+
+#define RT_FLAG_GUIDES        0x1u  /* write normals/albedos guide layers */
+#define RT_FLAG_STAGE_TIMING  0x2u  /* time the traversal and shading kernels with CUDA events */
+#define RT_FLAG_COUNT_VISITS  0x4u  /* count BVH nodes visited and primitives tested (slower) */
+
+/* Output buffers (device pointers, caller-owned): the image buffers of
+ * LpGeneral allocated by Launcher::resize (optx/launcher.cxx:36-47). */
+typedef struct {
+    rt_float3* rawRGB;      /* w*h, clamped mean colour (required) */
+    unsigned int* rpp;      /* w*h, rays per pixel (may be NULL) */
+    rt_float3* normals;     /* w*h, guide layer (NULL unless RT_FLAG_GUIDES) */
+    rt_float3* albedos;     /* w*h, guide layer (NULL unless RT_FLAG_GUIDES) */
+} rt_frame;
+
+/* Statistics of one rt_launch_ex call (host-side after it returns). */
+typedef struct {
+    unsigned long long rays;          /* sum of rpp over all pixels */
+    unsigned long long paths;
+    unsigned long long node_visits;   /* RT_FLAG_COUNT_VISITS only */
+    unsigned long long prim_tests;    /* RT_FLAG_COUNT_VISITS only */
+    unsigned int waves;               /* extend/shade iterations */
+    unsigned int kernel_launches;     /* kernels launched by this call */
+    float extend_ms;                  /* RT_FLAG_STAGE_TIMING only: sum over traversal launches */
+    float shade_ms;                   /* RT_FLAG_STAGE_TIMING only */
+    unsigned int extend_launches;
+    unsigned int wave_capacity;       /* rays per wave queue */
+} rt_launch_stats;
+
+/* --------------------------------------------------------------- camera */
+/* Camera::set (optx/camera.h:30-48): basis w = unit(eye-pat), u, v and the
+ * focus-plane vectors, computed on the host in binary32 (tanf only here). */
+rt_status rt_camera_set(rt_camera* cam, rt_float3 eye, rt_float3 pat, rt_float3 vup, float fov,
+                        float aspratio, float aperture, float fostance);
+
+/* ---------------------------------------------------------------- scene */
+typedef struct rt_scene_s* rt_scene;
+
+/* Scene::Scene / ~Scene (optx/scene.cxx:38-45; optx/scene.h:19-63). */
+rt_status rt_scene_create(rt_scene* out);
+rt_status rt_scene_destroy(rt_scene scene);
+
+/* Scene::add(Object&) (optx/scene.cxx:47-167): copies one indexed triangle
+ * mesh to the device and returns its mesh id ("GAS id"). */
+rt_status rt_scene_add_mesh(rt_scene scene, const rt_float3* vces, unsigned int nv,
+                            const rt_uint3* ices, unsigned int ni, unsigned int* mesh_id);
+
+/* Sphere(radius, ndiv) (optx/sphere.cxx:17-106) + Scene::add: tessellates a
+ * regular tetrahedron ndiv times on the GPU (4*4^ndiv triangles, vertices
+ * deduplicated in first-seen order) and adds the mesh.  ndiv <= 10. */
+rt_status rt_scene_add_sphere_mesh(rt_scene scene, float radius, unsigned int ndiv,
+                                   unsigned int* mesh_id);
+
+/* Copies a mesh back to the host (Sphere::mesh(), optx/sphere.cxx:21-26).
+ * Pass NULL buffers to query the counts only. */
+rt_status rt_scene_get_mesh(rt_scene scene, unsigned int mesh_id, rt_float3* vces,
+                            unsigned int* nv, rt_uint3* ices, unsigned int* ni);
+
+/* Scene::add(Thing&, gas) + Scene::set (optx/scene.cxx:169-215): an instance
+ * of mesh_id with its optics and 3x4 row-major object-to-world transform. */
+rt_status rt_scene_add_thing(rt_scene scene, const rt_optics* optics, unsigned int mesh_id,
+                             const float transform[12], unsigned int* thing_id);
+
+/* An analytic sphere thing (rtow's Sphere, sphere.h:9-48). */
+rt_status rt_scene_add_analytic_sphere(rt_scene scene, rt_float3 center, float radius,
+                                       const rt_optics* optics, unsigned int* thing_id);
+
+/* RTWO::load (optx/rtwo.cxx:137-244) / rtow's scene() (rtow.cxx:51-80): the
+ * final scene -- ground sphere (r 1000), a grid a,b in [-H,H) of r 0.2
+ * spheres with random centre and material, three r 1 spheres.  rng_kind
+ * RT_RECIPE_GLIBC reproduces the reference's scene for glibc rand() seeded
+ * `seed` (seed 1: 487 spheres); RT_RECIPE_COUNTER draws from a Philox stream.
+ * rt_rtow_spheres only lists the spheres (host code, no GPU needed; pass
+ * NULL arrays to query the count).  rt_scene_load_rtow adds them as analytic
+ * spheres (ndiv = -1) or as instances of one tessellated unit sphere mesh
+ * (ndiv >= 0) scaled by the radius and translated to the centre. */
+#define RT_RECIPE_GLIBC 0
+#define RT_RECIPE_COUNTER 1
+rt_status rt_rtow_spheres(int rng_kind, unsigned int seed, int half_extent, unsigned int cap,
+                          rt_float3* centers, float* radii, rt_optics* optics, unsigned int* count);
+rt_status rt_scene_load_rtow(rt_scene scene, int rng_kind, unsigned int seed, int half_extent,
+                             int ndiv, unsigned int* n_things);
+
+/* Scene::set / Scene::get (optx/scene.cxx:198-225); RT_ERR_INVALID_ARG for a
+ * bad thing id (the reference returns false).  set takes effect on the next
+ * rt_scene_update or rt_scene_build. */
+rt_status rt_scene_set_transform(rt_scene scene, unsigned int thing_id, const float transform[12]);
+rt_status rt_scene_get_transform(rt_scene scene, unsigned int thing_id, float transform[12]);
+rt_status rt_scene_set_optics(rt_scene scene, unsigned int thing_id, const rt_optics* optics);
+
+/* Scene::build (optx/scene.cxx:227-273, optixAccelBuild): flattens all
+ * things to world-space primitives and builds the LBVH (Morton codes, radix
+ * sort, Karras hierarchy, atomic bottom-up refit).  morton_bits 30 or 60
+ * (0 = 60).  Returns after the build has finished on `stream`. */
+rt_status rt_scene_build(rt_scene scene, unsigned int morton_bits, void* stream);
+
+/* Scene::update (optx/scene.cxx:275-294, IAS refit): re-flattens the things
+ * whose transform changed and refits the boxes, keeping the topology. */
+rt_status rt_scene_update(rt_scene scene, void* stream);
+
+typedef struct {
+    unsigned int n_meshes, n_things, n_prims, morton_bits;
+    unsigned long long device_bytes;
+    float build_ms;   /* last rt_scene_build, CUDA events */
+    float refit_ms;   /* last rt_scene_update */
+} rt_scene_info;
+rt_status rt_scene_info_get(rt_scene scene, rt_scene_info* info);
+
+/* LBVH snapshot for parity tests: sorted Morton codes (as 64-bit), sorted
+ * primitive ids, Karras children (child >= 0 internal node, < 0 leaf ~child)
+ * and per internal node the two child boxes (12 floats: lo0 hi0 lo1 hi1).
+ * Host buffers sized n, n, n-1, n-1, 12*(n-1); any may be NULL. */
+rt_status rt_scene_get_lbvh(rt_scene scene, unsigned long long* codes, unsigned int* ids,
+                            int* left, int* right, float* boxes);
+
+/* -------------------------------------------------------------- render */
+/* Launcher::ignite + __raygen__camera / __closesthit__* / __miss__ambient
+ * (optx/launcher.cxx:49-77, optx/camera_i.cu:24-141, optx/optics_i.cu:23-288):
+ * renders w*h pixels x spp samples with the wavefront path tracer into the
+ * caller's device buffers.  Asynchronous on `stream` except for its
+ * host-side wave loop. */
+rt_status rt_launch(rt_scene scene, const rt_camera* cam, const rt_launch_params* params,
+                    const rt_frame* frame, void* stream);
+/* Same, filling `stats` (synchronises `stream` before returning). */
+rt_status rt_launch_ex(rt_scene scene, const rt_camera* cam, const rt_launch_params* params,
+                       const rt_frame* frame, void* stream, rt_launch_stats* stats);
+
+/* Primary-ray closest hit of sample `sample` for every pixel (parity and
+ * picking): prim id (global, -1 on a miss), thing id, t, barycentrics u, v.
+ * Device buffers of w*h entries each; any but prim may be NULL. */
+rt_status rt_first_hit(rt_scene scene, const rt_camera* cam, const rt_launch_params* params,
+                       unsigned int sample, int* prim, int* thing, float* t, float* u, float* v,
+                       void* stream);
+
+/* Picker: the 1x1 launch of SimpleSM::eaEdtSed (optx/simplesm.cxx:1014-1034,
+ * optx/optics_i.cu:25-29): thing id under pixel (x, y), or 0xFFFFFFFF on a
+ * miss.  Synchronous. */
+rt_status rt_pick(rt_scene scene, const rt_camera* cam, const rt_launch_params* params,
+                  unsigned int x, unsigned int y, unsigned int* thing_id, void* stream);
+
+/* ---------------------------------------------------------- post-process */
+/* pp_sRGB / pp_none (optx/postproc.cu:49-61; declared at optx/rtwo.cxx:53-54):
+ * float3 -> uchar4 through the sRGB curve, or x255 truncation.  Same
+ * arguments as the reference plus a stream; device pointers. */
+rt_status rt_postproc_srgb(const rt_float3* src, rt_uchar4* dst, int w, int h, void* stream);
+rt_status rt_postproc_none(const rt_float3* src, rt_uchar4* dst, int w, int h, void* stream);
+/* rtow's gamma-2 writer (rtow.cxx:6-21): int(256*clamp(sqrt(x), 0, .999)). */
+rt_status rt_postproc_gamma2(const rt_float3* src, rt_uchar4* dst, int w, int h, void* stream);
+
+/* ------------------------------------------------------------- launcher */
+/* class Launcher (optx/launcher.h:17-31, optx/launcher.cxx:24-85): owns the
+ * device image buffers of LpGeneral (rawRGB, rpp, normals, albedos, image,
+ * pick id) and renders synchronously into them. */
+typedef struct rt_launcher_s* rt_launcher;
+rt_status rt_launcher_create(rt_launcher* out, unsigned int w, unsigned int h);
+rt_status rt_launcher_destroy(rt_launcher l);
+rt_status rt_launcher_resize(rt_launcher l, unsigned int w, unsigned int h);
+/* Launcher::ignite(stream, once): once != 0 is the 1x1 picker launch at
+ * (pick_x, pick_y); otherwise a full render followed by pp_sRGB into the
+ * launcher's uchar4 image.  Synchronous, like the reference. */
+rt_status rt_launcher_ignite(rt_launcher l, rt_scene scene, const rt_camera* cam,
+                             const rt_launch_params* params, void* stream, int once,
+                             unsigned int pick_x, unsigned int pick_y, rt_launch_stats* stats);
+/* Device pointers of the launcher's buffers (valid until resize/destroy). */
+rt_status rt_launcher_frame(rt_launcher l, rt_frame* frame, rt_uchar4** image,
+                            unsigned int** pick_id);
+/* Copies the launcher's buffers to host memory (any pointer may be NULL):
+ * the device-to-host reads of imgtopnm and -S (optx/rtwo.cxx:61-74,578-591). */
+rt_status rt_launcher_download(rt_launcher l, rt_float3* rawRGB, unsigned int* rpp,
+                               rt_float3* normals, rt_float3* albedos, rt_uchar4* image,
+                               unsigned int* pick_id);
+
+/* -------------------------------------------------- device-side helpers */
+/* Stable LSD radix sort of (key, value) pairs on the device, in place, with
+ * the LBVH builder's kernels (parity hook: bit-exact against a CPU stable
+ * sort).  key_bits <= 32 sorts 32-bit keys, otherwise 64-bit keys. */
+rt_status rt_radix_sort_pairs(void* keys, unsigned int* vals, unsigned int n,
+                              unsigned int key_bits, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RT_API_H */

@@ -1,0 +1,356 @@
+"""rtxplay_gb300 -- GB300-native path tracer behind RTXplay's render API.
+
+The product is the native library ``_build/librtxplay_gb300.so`` (CUDA
+kernels for sm_103a + the C ABI declared in ``include/rt_api.h``).  This module
+binds that ABI with ctypes; it never falls back to Python or CPU code.  If the
+library is missing, :func:`lib` raises -- build it with
+``python -c "import __graft_entry__ as g; g.build()"``.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import _build
+
+LIB_PATH = _build.LIB
+
+RT_OK = 0
+RT_ERR_INVALID_ARG = 1
+RT_ERR_CUDA = 2
+RT_ERR_OUT_OF_MEMORY = 3
+RT_ERR_NOT_BUILT = 4
+RT_ERR_LIMIT = 5
+RT_ERR_INTERNAL = 6
+
+RT_OPTICS_DIFFUSE, RT_OPTICS_REFLECT, RT_OPTICS_REFRACT = 0, 1, 2
+RT_FLAG_GUIDES, RT_FLAG_STAGE_TIMING, RT_FLAG_COUNT_VISITS = 0x1, 0x2, 0x4
+RT_RECIPE_GLIBC, RT_RECIPE_COUNTER = 0, 1
+
+
+class RTError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"rt status {status}: {msg}")
+        self.status = status
+
+
+class float3(ctypes.Structure):
+    _fields_ = [("x", ctypes.c_float), ("y", ctypes.c_float), ("z", ctypes.c_float)]
+
+
+class uint3(ctypes.Structure):
+    _fields_ = [("x", ctypes.c_uint), ("y", ctypes.c_uint), ("z", ctypes.c_uint)]
+
+
+class Optics(ctypes.Structure):
+    """rt_optics: flattened Optics union (optx/thing.h:17-52)."""
+    _fields_ = [("type", ctypes.c_int), ("albedo", float3), ("fuzz", ctypes.c_float),
+                ("index", ctypes.c_float)]
+
+
+class Camera(ctypes.Structure):
+    """rt_camera: class Camera state (optx/camera.h:28-94)."""
+    _fields_ = [("eye", float3), ("pat", float3), ("vup", float3), ("fov", ctypes.c_float),
+                ("aspratio", ctypes.c_float), ("aperture", ctypes.c_float),
+                ("fostance", ctypes.c_float), ("u", float3), ("v", float3), ("w", float3),
+                ("hvec", float3), ("wvec", float3), ("dvec", float3)]
+
+
+class LaunchParams(ctypes.Structure):
+    _fields_ = [("image_w", ctypes.c_uint), ("image_h", ctypes.c_uint), ("spp", ctypes.c_uint),
+                ("depth", ctypes.c_uint), ("seed", ctypes.c_uint), ("flags", ctypes.c_uint),
+                ("ambient", float3), ("white", float3)]
+
+
+class Frame(ctypes.Structure):
+    _fields_ = [("rawRGB", ctypes.c_void_p), ("rpp", ctypes.c_void_p),
+                ("normals", ctypes.c_void_p), ("albedos", ctypes.c_void_p)]
+
+
+class LaunchStats(ctypes.Structure):
+    _fields_ = [("rays", ctypes.c_ulonglong), ("paths", ctypes.c_ulonglong),
+                ("node_visits", ctypes.c_ulonglong), ("prim_tests", ctypes.c_ulonglong),
+                ("waves", ctypes.c_uint), ("kernel_launches", ctypes.c_uint),
+                ("extend_ms", ctypes.c_float), ("shade_ms", ctypes.c_float),
+                ("extend_launches", ctypes.c_uint), ("wave_capacity", ctypes.c_uint)]
+
+
+class SceneInfo(ctypes.Structure):
+    _fields_ = [("n_meshes", ctypes.c_uint), ("n_things", ctypes.c_uint), ("n_prims", ctypes.c_uint),
+                ("morton_bits", ctypes.c_uint), ("device_bytes", ctypes.c_ulonglong),
+                ("build_ms", ctypes.c_float), ("refit_ms", ctypes.c_float)]
+
+
+_P = ctypes.c_void_p
+_U = ctypes.c_uint
+_I = ctypes.c_int
+_F = ctypes.c_float
+_PU = ctypes.POINTER(ctypes.c_uint)
+
+# name -> argtypes (every function returns rt_status)
+SIGNATURES = {
+    "rt_camera_set": [ctypes.POINTER(Camera), float3, float3, float3, _F, _F, _F, _F],
+    "rt_scene_create": [ctypes.POINTER(_P)],
+    "rt_scene_destroy": [_P],
+    "rt_scene_add_mesh": [_P, _P, _U, _P, _U, _PU],
+    "rt_scene_add_sphere_mesh": [_P, _F, _U, _PU],
+    "rt_scene_get_mesh": [_P, _U, _P, _PU, _P, _PU],
+    "rt_scene_add_thing": [_P, ctypes.POINTER(Optics), _U, _P, _PU],
+    "rt_scene_add_analytic_sphere": [_P, float3, _F, ctypes.POINTER(Optics), _PU],
+    "rt_rtow_spheres": [_I, _U, _I, _U, _P, _P, _P, _PU],
+    "rt_scene_load_rtow": [_P, _I, _U, _I, _I, _PU],
+    "rt_scene_set_transform": [_P, _U, _P],
+    "rt_scene_get_transform": [_P, _U, _P],
+    "rt_scene_set_optics": [_P, _U, ctypes.POINTER(Optics)],
+    "rt_scene_build": [_P, _U, _P],
+    "rt_scene_update": [_P, _P],
+    "rt_scene_info_get": [_P, ctypes.POINTER(SceneInfo)],
+    "rt_scene_get_lbvh": [_P, _P, _P, _P, _P, _P],
+    "rt_launch": [_P, ctypes.POINTER(Camera), ctypes.POINTER(LaunchParams), ctypes.POINTER(Frame), _P],
+    "rt_launch_ex": [_P, ctypes.POINTER(Camera), ctypes.POINTER(LaunchParams), ctypes.POINTER(Frame), _P,
+                     ctypes.POINTER(LaunchStats)],
+    "rt_first_hit": [_P, ctypes.POINTER(Camera), ctypes.POINTER(LaunchParams), _U, _P, _P, _P, _P, _P, _P],
+    "rt_pick": [_P, ctypes.POINTER(Camera), ctypes.POINTER(LaunchParams), _U, _U, _PU, _P],
+    "rt_postproc_srgb": [_P, _P, _I, _I, _P],
+    "rt_postproc_none": [_P, _P, _I, _I, _P],
+    "rt_postproc_gamma2": [_P, _P, _I, _I, _P],
+    "rt_launcher_create": [ctypes.POINTER(_P), _U, _U],
+    "rt_launcher_destroy": [_P],
+    "rt_launcher_resize": [_P, _U, _U],
+    "rt_launcher_ignite": [_P, _P, ctypes.POINTER(Camera), ctypes.POINTER(LaunchParams), _P, _I, _U, _U,
+                           ctypes.POINTER(LaunchStats)],
+    "rt_launcher_frame": [_P, ctypes.POINTER(Frame), ctypes.POINTER(_P), ctypes.POINTER(_P)],
+    "rt_launcher_download": [_P, _P, _P, _P, _P, _P, _P],
+    "rt_radix_sort_pairs": [_P, _P, _U, _U, _P],
+}
+
+_lib = None
+
+
+def lib():
+    """Loads librtxplay_gb300.so; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: build it with __graft_entry__.build()")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, args in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = ctypes.c_int
+        L.rt_last_error_string.restype = ctypes.c_char_p
+        L.rt_last_error_string.argtypes = []
+        L.rt_version.restype = ctypes.c_char_p
+        L.rt_version.argtypes = []
+        _lib = L
+    return _lib
+
+
+def check(status):
+    if status != RT_OK:
+        raise RTError(status, lib().rt_last_error_string().decode())
+    return status
+
+
+def f3(v):
+    return float3(float(v[0]), float(v[1]), float(v[2]))
+
+
+def _ptr(a):
+    return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+def camera_set(eye, pat, vup, fov, aspratio, aperture, fostance):
+    cam = Camera()
+    check(lib().rt_camera_set(ctypes.byref(cam), f3(eye), f3(pat), f3(vup), fov, aspratio, aperture,
+                              fostance))
+    return cam
+
+
+def rtow_camera(w, h):
+    """The final-scene camera of optx/rtwo.cxx:100-108 (aspect = w/h in binary32)."""
+    return camera_set((13, 2, 3), (0, 0, 0), (0, 1, 0), 20.0,
+                      float(np.float32(w) / np.float32(h)), 0.1, 10.0)
+
+
+def launch_params(w, h, spp, depth=50, seed=4711, flags=0, ambient=(0.5, 0.7, 1.0),
+                  white=(1.0, 1.0, 1.0)):
+    return LaunchParams(w, h, spp, depth, seed, flags, f3(ambient), f3(white))
+
+
+def optics(otype, albedo=(0, 0, 0), fuzz=0.0, index=0.0):
+    return Optics(int(otype), f3(albedo), float(fuzz), float(index))
+
+
+def rtow_spheres(rng_kind=RT_RECIPE_GLIBC, seed=1, half_extent=11):
+    """The final-scene sphere list (host code, no GPU needed)."""
+    n = ctypes.c_uint()
+    check(lib().rt_rtow_spheres(rng_kind, seed, half_extent, 0, None, None, None, ctypes.byref(n)))
+    c = np.zeros((n.value, 3), np.float32)
+    r = np.zeros(n.value, np.float32)
+    o = (Optics * n.value)()
+    check(lib().rt_rtow_spheres(rng_kind, seed, half_extent, n.value, _ptr(c), _ptr(r),
+                                ctypes.cast(o, ctypes.c_void_p), ctypes.byref(n)))
+    types = np.array([x.type for x in o], np.int32)
+    alb = np.array([[x.albedo.x, x.albedo.y, x.albedo.z] for x in o], np.float32).reshape(-1, 3)
+    fuzz = np.array([x.fuzz for x in o], np.float32)
+    index = np.array([x.index for x in o], np.float32)
+    return dict(centers=c, radii=r, types=types, albedos=alb, fuzz=fuzz, index=index)
+
+
+class Scene:
+    """Owns an rt_scene handle (the reference's class Scene, optx/scene.h:19-63)."""
+
+    def __init__(self):
+        self.h = ctypes.c_void_p()
+        check(lib().rt_scene_create(ctypes.byref(self.h)))
+
+    def close(self):
+        if self.h:
+            lib().rt_scene_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_mesh(self, vces, ices):
+        v = np.ascontiguousarray(vces, np.float32)
+        i = np.ascontiguousarray(ices, np.uint32)
+        mid = ctypes.c_uint()
+        check(lib().rt_scene_add_mesh(self.h, _ptr(v), len(v), _ptr(i), len(i), ctypes.byref(mid)))
+        return mid.value
+
+    def add_sphere_mesh(self, radius, ndiv):
+        mid = ctypes.c_uint()
+        check(lib().rt_scene_add_sphere_mesh(self.h, radius, ndiv, ctypes.byref(mid)))
+        return mid.value
+
+    def get_mesh(self, mesh_id):
+        nv, ni = ctypes.c_uint(), ctypes.c_uint()
+        check(lib().rt_scene_get_mesh(self.h, mesh_id, None, ctypes.byref(nv), None, ctypes.byref(ni)))
+        v = np.zeros((nv.value, 3), np.float32)
+        i = np.zeros((ni.value, 3), np.uint32)
+        check(lib().rt_scene_get_mesh(self.h, mesh_id, _ptr(v), ctypes.byref(nv), _ptr(i), ctypes.byref(ni)))
+        return v, i
+
+    def add_thing(self, opt, mesh_id, transform):
+        t = np.ascontiguousarray(transform, np.float32)
+        tid = ctypes.c_uint()
+        check(lib().rt_scene_add_thing(self.h, ctypes.byref(opt), mesh_id, _ptr(t), ctypes.byref(tid)))
+        return tid.value
+
+    def add_analytic_sphere(self, center, radius, opt):
+        tid = ctypes.c_uint()
+        check(lib().rt_scene_add_analytic_sphere(self.h, f3(center), radius, ctypes.byref(opt),
+                                                 ctypes.byref(tid)))
+        return tid.value
+
+    def load_rtow(self, rng_kind=RT_RECIPE_GLIBC, seed=1, half_extent=11, ndiv=6):
+        n = ctypes.c_uint()
+        check(lib().rt_scene_load_rtow(self.h, rng_kind, seed, half_extent, ndiv, ctypes.byref(n)))
+        return n.value
+
+    def set_transform(self, thing, transform):
+        t = np.ascontiguousarray(transform, np.float32)
+        return lib().rt_scene_set_transform(self.h, thing, _ptr(t))
+
+    def get_transform(self, thing):
+        t = np.zeros(12, np.float32)
+        st = lib().rt_scene_get_transform(self.h, thing, _ptr(t))
+        return st, t
+
+    def set_optics(self, thing, opt):
+        return lib().rt_scene_set_optics(self.h, thing, ctypes.byref(opt))
+
+    def build(self, morton_bits=60, stream=None):
+        check(lib().rt_scene_build(self.h, morton_bits, stream))
+
+    def update(self, stream=None):
+        check(lib().rt_scene_update(self.h, stream))
+
+    def info(self):
+        inf = SceneInfo()
+        check(lib().rt_scene_info_get(self.h, ctypes.byref(inf)))
+        return inf
+
+    def lbvh(self):
+        n = self.info().n_prims
+        codes = np.zeros(n, np.uint64)
+        ids = np.zeros(n, np.uint32)
+        left = np.zeros(max(n - 1, 0), np.int32)
+        right = np.zeros(max(n - 1, 0), np.int32)
+        boxes = np.zeros((max(n - 1, 0), 12), np.float32)
+        check(lib().rt_scene_get_lbvh(self.h, _ptr(codes), _ptr(ids), _ptr(left), _ptr(right), _ptr(boxes)))
+        return dict(codes=codes, ids=ids, left=left, right=right, boxes=boxes)
+
+
+class Launcher:
+    """Owns an rt_launcher (class Launcher, optx/launcher.h:17-31): device image buffers."""
+
+    def __init__(self, w, h):
+        self.h = ctypes.c_void_p()
+        self.w, self.hgt = w, h
+        check(lib().rt_launcher_create(ctypes.byref(self.h), w, h))
+
+    def close(self):
+        if self.h:
+            lib().rt_launcher_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def ignite(self, scene, cam, params, once=False, pick=(0, 0), stream=None):
+        stats = LaunchStats()
+        check(lib().rt_launcher_ignite(self.h, scene.h, ctypes.byref(cam), ctypes.byref(params), stream,
+                                       1 if once else 0, pick[0], pick[1], ctypes.byref(stats)))
+        return stats
+
+    def download(self, guides=False):
+        n = self.w * self.hgt
+        raw = np.zeros((n, 3), np.float32)
+        rpp = np.zeros(n, np.uint32)
+        img = np.zeros((n, 4), np.uint8)
+        pick = np.zeros(1, np.uint32)
+        nrm = np.zeros((n, 3), np.float32) if guides else None
+        alb = np.zeros((n, 3), np.float32) if guides else None
+        check(lib().rt_launcher_download(self.h, _ptr(raw), _ptr(rpp), _ptr(nrm), _ptr(alb), _ptr(img),
+                                         _ptr(pick)))
+        return dict(rawRGB=raw, rpp=rpp, image=img, pick_id=int(pick[0]), normals=nrm, albedos=alb)
+
+    def frame(self):
+        f = Frame()
+        img = ctypes.c_void_p()
+        pick = ctypes.c_void_p()
+        check(lib().rt_launcher_frame(self.h, ctypes.byref(f), ctypes.byref(img), ctypes.byref(pick)))
+        return f, img, pick
+
+
+def render(scene, cam, params, guides=False):
+    """Synchronous render through a Launcher; returns host arrays and stats."""
+    L = Launcher(params.image_w, params.image_h)
+    try:
+        stats = L.ignite(scene, cam, params)
+        out = L.download(guides=guides)
+    finally:
+        L.close()
+    out["stats"] = stats
+    return out
+
+
+def rtow_scene(level=6, rng_kind=RT_RECIPE_GLIBC, seed=1, half_extent=11, morton_bits=60):
+    """The final scene, tessellated at `level` (None: analytic spheres), built."""
+    sc = Scene()
+    sc.load_rtow(rng_kind, seed, half_extent, -1 if level is None else level)
+    sc.build(morton_bits)
+    return sc
+
+
+def version():
+    return lib().rt_version().decode()

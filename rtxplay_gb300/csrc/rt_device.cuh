@@ -1,0 +1,294 @@
+// rt_device.cuh -- device-side core of the GB300 path tracer.
+//
+// Vector maths in the operation order of optx/v.h:26-78, the counter RNG,
+// the rejection samplers of optx/v.h:66-76, the primitive and node layouts in
+// HBM and the closest-hit traversal shared by the first-hit and wavefront
+// extend kernels.  Everything here is compiled with --fmad=false: products
+// and sums are never fused behind the source's back, so results are the same
+// bits as the binary32 CPU restatement of the same formulas.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace rt {
+
+// ------------------------------------------------------------------ vectors
+__host__ __device__ __forceinline__ float3 mk(float x, float y, float z) { return make_float3(x, y, z); }
+__host__ __device__ __forceinline__ float3 add(float3 a, float3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+__host__ __device__ __forceinline__ float3 sub(float3 a, float3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+__host__ __device__ __forceinline__ float3 neg(float3 a) { return mk(-a.x, -a.y, -a.z); }
+__host__ __device__ __forceinline__ float3 mul(float s, float3 a) { return mk(s * a.x, s * a.y, s * a.z); }
+__host__ __device__ __forceinline__ float3 mulv(float3 a, float3 b) { return mk(a.x * b.x, a.y * b.y, a.z * b.z); }
+__host__ __device__ __forceinline__ float dot(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__host__ __device__ __forceinline__ float3 cross(float3 a, float3 b) {
+    return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__host__ __device__ __forceinline__ float len(float3 v) { return sqrtf(dot(v, v)); }
+// optx/v.h:576: unitV(v) = 1/len(v) * v
+__host__ __device__ __forceinline__ float3 unitV(float3 v) { return mul(1.f / len(v), v); }
+// optx/v.h:578 (kNear0 = 1e-8)
+__host__ __device__ __forceinline__ bool near0(float3 v) {
+    return fabsf(v.x) < 1e-8f && fabsf(v.y) < 1e-8f && fabsf(v.z) < 1e-8f;
+}
+__host__ __device__ __forceinline__ bool isnull(float3 v) { return v.x == 0.f && v.y == 0.f && v.z == 0.f; }
+__host__ __device__ __forceinline__ float3 xyz(float4 a) { return mk(a.x, a.y, a.z); }
+
+// ------------------------------------------------------------------ Philox
+// Philox4x32-10 counter-based generator (Salmon, Moraes, Dror, Shaw, SC'11).
+struct U4 {
+    uint32_t x, y, z, w;
+};
+
+__device__ __forceinline__ U4 philox10(U4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+        const uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+        c = U4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return c;
+}
+
+// 24 high bits -> [0, 1), exact in binary32.
+__host__ __device__ __forceinline__ float u01(uint32_t x) { return float(x >> 8) * (1.0f / 16777216.0f); }
+
+// The draws of one bounce of one path: key = (seed, scene), counter =
+// (pixel, sample, bounce, draw / 4); draw k is lane k % 4 of block k / 4.
+// Bounce 0 is the camera (jitter and lens), bounce b >= 1 the scatter at the
+// hit of the b-th ray.  Any path segment can be replayed from its ids alone.
+struct Stream {
+    uint32_t k0, k1, pixel, sample, bounce;
+    uint32_t n;
+    U4 buf;
+    __device__ __forceinline__ Stream(uint32_t seed, uint32_t scene, uint32_t pix, uint32_t smp, uint32_t bnc)
+        : k0(seed), k1(scene), pixel(pix), sample(smp), bounce(bnc), n(0), buf{0, 0, 0, 0} {}
+    __device__ __forceinline__ float next() {
+        const uint32_t lane = n & 3u;
+        if (lane == 0) buf = philox10(U4{pixel, sample, bounce, n >> 2}, k0, k1);
+        ++n;
+        const uint32_t x = lane == 0 ? buf.x : lane == 1 ? buf.y : lane == 2 ? buf.z : buf.w;
+        return u01(x);
+    }
+    // optx/util_gpu.h:28: rnd(min, max) = min + rnd * (max - min)
+    __device__ __forceinline__ float next(float lo, float hi) { return lo + next() * (hi - lo); }
+};
+
+constexpr int kMaxRejections = 64;   // probability of reaching it < 1e-20
+
+// optx/v.h:72: rejection sample of the unit ball; draws x, y, z in order.
+__device__ __forceinline__ float3 rndVin1sphere(Stream& s) {
+    for (int i = 0; i < kMaxRejections; ++i) {
+        const float x = s.next(-1.f, 1.f);
+        const float y = s.next(-1.f, 1.f);
+        const float z = s.next(-1.f, 1.f);
+        const float3 v = mk(x, y, z);
+        if (1.f > dot(v, v)) return v;
+    }
+    return mk(0.f, 0.f, .5f);
+}
+// optx/v.h:73
+__device__ __forceinline__ float3 rndVon1sphere(Stream& s) { return unitV(rndVin1sphere(s)); }
+// optx/v.h:75: rejection sample of the unit disk; draws x then y.
+__device__ __forceinline__ float3 rndVin1disk(Stream& s) {
+    for (int i = 0; i < kMaxRejections; ++i) {
+        const float x = s.next(-1.f, 1.f);
+        const float y = s.next(-1.f, 1.f);
+        const float3 v = mk(x, y, 0.f);
+        if (1.f > dot(v, v)) return v;
+    }
+    return mk(0.f, 0.f, 0.f);
+}
+
+// ------------------------------------------------------------------ camera
+struct CamDev {
+    float3 eye, u, v, w, hvec, wvec, dvec;
+    float aperture;
+};
+
+// optx/camera.h:67-77 with the pixel jitter of optx/camera_i.cu:61-65.
+__device__ __forceinline__ void camera_ray(const CamDev& c, uint32_t x, uint32_t y, uint32_t W, uint32_t H,
+                                           Stream& s, float3& ori, float3& dir) {
+    const float jx = s.next();
+    const float jy = s.next();
+    const float sx = 2.f * (float(x) + jx) / float(W) - 1.f;
+    const float ty = 2.f * (float(y) + jy) / float(H) - 1.f;
+    const float3 r = mul(c.aperture / 2.f, rndVin1disk(s));
+    const float3 o = add(mul(r.x, c.u), mul(r.y, c.v));
+    ori = add(c.eye, o);
+    dir = sub(sub(add(mul(sx, c.wvec), mul(ty, c.hvec)), c.dvec), o);
+}
+
+// ------------------------------------------------------------------ layouts
+// Primitive record in LBVH leaf order, 48 bytes (three float4):
+//   triangle: a = (v0, thing id bits), b = (v1, prim id bits), c = (v2, 0)
+//   sphere:   a = (centre, thing id bits), b = (radius, 0, 0, prim id bits), c = (0, 0, 0, 1)
+// Leaf i of the hierarchy is record i; `prim id` is the global id in
+// thing-insertion order (the id parity tests and the picker report).
+constexpr uint32_t kPrimTriangle = 0u;
+constexpr uint32_t kPrimSphere = 1u;
+
+// Internal node, 64 bytes (four float4), both child boxes held by the parent:
+//   n0 = (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y)
+//   n1 = (c1.lo.x, c1.hi.x, c1.lo.y, c1.hi.y)
+//   n2 = (c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z)
+//   n3 = (child0 bits, child1 bits, 0, 0); child >= 0 internal node, < 0 leaf ~child
+struct ThingDev {       // 48 bytes
+    float4 albedo_type; // albedo.xyz, optics type (int bits)
+    float4 center_fuzz; // instance centre (transform translation), fuzz
+    float4 index_pad;   // refraction index, -, -, -
+};
+
+constexpr float kTmin = 1e-3f;   // optx/camera_i.cu:81
+constexpr float kTmax = 1e16f;   // optx/camera_i.cu:82
+// Conservative slab test: relative slack 2^-12 on the exit distance, so a
+// box that holds the closest primitive is never culled by rounding and the
+// closest hit equals brute force over all primitives.
+constexpr float kSlack = 1.f + 1.f / 4096.f;
+
+__device__ __forceinline__ float safe_inv(float d) {
+    const float dd = fabsf(d) < 1e-20f ? copysignf(1e-20f, d) : d;
+    return 1.f / dd;
+}
+
+// Moller-Trumbore (edges formed from the stored vertices), t >= tmin.
+__device__ __forceinline__ bool tri_test(float3 A, float3 B, float3 C, float3 o, float3 d, float& t, float& u,
+                                         float& v) {
+    const float3 e1 = sub(B, A);
+    const float3 e2 = sub(C, A);
+    const float3 pv = cross(d, e2);
+    const float det = dot(e1, pv);
+    if (det == 0.f) return false;
+    const float inv = 1.f / det;
+    const float3 tv = sub(o, A);
+    const float uu = dot(tv, pv) * inv;
+    if (uu < 0.f || uu > 1.f) return false;
+    const float3 qv = cross(tv, e1);
+    const float vv = dot(d, qv) * inv;
+    if (vv < 0.f || uu + vv > 1.f) return false;
+    const float tt = dot(e2, qv) * inv;
+    if (!(tt >= kTmin)) return false;
+    t = tt;
+    u = uu;
+    v = vv;
+    return true;
+}
+
+// rtow's Sphere::hit (sphere.h:20-38) in binary32: nearest root in range.
+__device__ __forceinline__ bool sph_test(float3 c, float r, float3 o, float3 d, float& t) {
+    const float3 oc = sub(o, c);
+    const float a = dot(d, d);
+    const float b = dot(d, oc);
+    const float cc = dot(oc, oc) - r * r;
+    const float disc = b * b - a * cc;
+    if (0.f > disc) return false;
+    const float x = sqrtf(disc);
+    float tt = (-b - x) / a;
+    if (kTmin > tt || !(tt <= kTmax)) {
+        tt = (-b + x) / a;
+        if (kTmin > tt || !(tt <= kTmax)) return false;
+    }
+    t = tt;
+    return true;
+}
+
+struct HitRec {
+    float t, u, v;
+    int leaf;       // LBVH leaf (record) index, -1 on a miss
+    uint32_t id;    // global primitive id of the hit
+    bool overflow;  // the traversal stack was full: a subtree was skipped
+};
+
+constexpr int kStackSize = 64;   // > the depth of an LBVH over 2^24 primitives in practice (50 at 8M)
+
+struct TraceCounters {
+    unsigned long long nodes, prims;
+};
+
+// Closest hit over the LBVH: smallest t, equal t -> larger primitive id.
+// Child boxes are tested together; leaves are tested as soon as their box is
+// hit, internal children are descended near-first with a per-thread stack.
+template <bool kCount>
+__device__ __forceinline__ HitRec closest_hit(const float4* __restrict__ nodes, const float4* __restrict__ prims,
+                                              uint32_t nprims, float3 o, float3 d, uint32_t& nvis,
+                                              uint32_t& ntest) {
+    HitRec h{0.f, 0.f, 0.f, -1, 0u, false};
+    if (nprims == 0) return h;
+    float best = kTmax;
+    const float3 inv = mk(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
+    int stack[kStackSize];
+    int sp = 0;
+    int node = 0;
+    auto leaf_test = [&](int li) {
+        if (kCount) ++ntest;
+        const float4 a = __ldg(prims + 3 * li);
+        const float4 b = __ldg(prims + 3 * li + 1);
+        const float4 c = __ldg(prims + 3 * li + 2);
+        float t, u, v;
+        bool hit;
+        if (__float_as_uint(c.w) == kPrimTriangle) {
+            hit = tri_test(xyz(a), xyz(b), xyz(c), o, d, t, u, v);
+        } else {
+            u = v = 0.f;
+            hit = sph_test(xyz(a), b.x, o, d, t);
+        }
+        if (!hit || t > best) return;
+        const uint32_t id = __float_as_uint(b.w);
+        if (h.leaf < 0 || t < h.t || (t == h.t && id > h.id)) {
+            h.t = t; h.u = u; h.v = v; h.leaf = li; h.id = id;
+            best = t;
+        }
+    };
+    while (true) {
+        if (kCount) ++nvis;
+        const float4 n0 = __ldg(nodes + 4 * node);
+        const float4 n1 = __ldg(nodes + 4 * node + 1);
+        const float4 n2 = __ldg(nodes + 4 * node + 2);
+        const float4 n3 = __ldg(nodes + 4 * node + 3);
+        // child 0
+        float a0 = (n0.x - o.x) * inv.x, b0 = (n0.y - o.x) * inv.x;
+        float a1 = (n0.z - o.y) * inv.y, b1 = (n0.w - o.y) * inv.y;
+        float a2 = (n2.x - o.z) * inv.z, b2 = (n2.y - o.z) * inv.z;
+        const float tn0 = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fmaxf(fminf(a2, b2), kTmin));
+        const float tf0 = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fminf(fmaxf(a2, b2), best));
+        // child 1
+        a0 = (n1.x - o.x) * inv.x; b0 = (n1.y - o.x) * inv.x;
+        a1 = (n1.z - o.y) * inv.y; b1 = (n1.w - o.y) * inv.y;
+        a2 = (n2.z - o.z) * inv.z; b2 = (n2.w - o.z) * inv.z;
+        const float tn1 = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fmaxf(fminf(a2, b2), kTmin));
+        const float tf1 = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fminf(fmaxf(a2, b2), best));
+        bool h0 = tn0 <= tf0 * kSlack;
+        bool h1 = tn1 <= tf1 * kSlack;
+        int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
+        if (h0 && h1 && tn1 < tn0) {
+            const int tc = c0; c0 = c1; c1 = tc;
+        }
+        if (h0 && h1) {
+            // (c0 is now the nearer child)
+        } else if (h1) {
+            c0 = c1;
+            h0 = true;
+            h1 = false;
+        }
+        // h0: c0 hit; h1: c1 hit too (c0 nearer)
+        if (h0 && c0 < 0) { leaf_test(~c0); h0 = false; }
+        if (h1 && c1 < 0) { leaf_test(~c1); h1 = false; }
+        if (h0 && h1) {
+            if (sp < kStackSize) stack[sp++] = c1;
+            else h.overflow = true;
+            node = c0;
+        } else if (h0) {
+            node = c0;
+        } else if (h1) {
+            node = c1;
+        } else {
+            if (sp == 0) break;
+            node = stack[--sp];
+        }
+    }
+    return h;
+}
+
+}  // namespace rt

@@ -1,0 +1,782 @@
+// rt_scene.cu -- scene construction: tessellation, flattening, LBVH build and refit.
+//
+// Replaces Sphere (optx/sphere.cxx:17-106), Scene::add / set / get / build /
+// update (optx/scene.cxx:38-294) and the closed optixAccelBuild with GPU
+// kernels.  HBM layout after a build: primitive records in leaf order (48 B
+// each, three float4), internal nodes holding both child boxes (64 B each),
+// a 48-byte optics record per thing.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <numeric>
+#include <vector>
+
+#include "rt_scene.h"
+
+namespace rt {
+namespace {
+
+constexpr int kThreads = 256;
+
+inline unsigned grid_for(uint64_t n, int threads = kThreads) { return unsigned((n + threads - 1) / threads); }
+
+// ------------------------------------------------------------ tessellation
+// One thread per leaf triangle of the 4-way subdivision, walking the path of
+// pumpup (optx/sphere.cxx:51-66) from its base face: the midpoints are the
+// same operations on the same operands as the recursion, hence the same bits.
+__global__ void k_tess_leaves(float radius, uint32_t ndiv, uint32_t ntri, float3* __restrict__ out) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntri) return;
+    // optx/sphere.cxx:34-46: regular tetrahedron, midsphere radius m
+    const float m = .57735026919f;
+    const float3 v00 = mk(m, m, m), v01 = mk(m, -m, -m), v02 = mk(-m, -m, m), v03 = mk(-m, m, -m);
+    const uint32_t face = t >> (2 * ndiv);
+    float3 a, b, c;
+    switch (face) {
+        case 0: a = v00; b = v01; c = v02; break;
+        case 1: a = v00; b = v02; c = v03; break;
+        case 2: a = v00; b = v03; c = v01; break;
+        default: a = v03; b = v02; c = v01; break;
+    }
+    for (int k = int(ndiv) - 1; k >= 0; --k) {
+        const uint32_t digit = (t >> (2 * k)) & 3u;
+        const float3 ab = unitV(mul(.5f, add(a, b)));
+        const float3 bc = unitV(mul(.5f, add(b, c)));
+        const float3 ca = unitV(mul(.5f, add(c, a)));
+        switch (digit) {
+            case 0: b = ab; c = ca; break;                 // (a, ab, ca)
+            case 1: a = ab; c = bc; break;                 // (ab, b, bc)
+            case 2: a = ca; b = bc; break;                 // (ca, bc, c)
+            default: a = ab; b = bc; c = ca; break;        // (ab, bc, ca)
+        }
+    }
+    out[3 * t] = mul(radius, a);
+    out[3 * t + 1] = mul(radius, b);
+    out[3 * t + 2] = mul(radius, c);
+}
+
+// IEEE order-preserving map float -> u32 (-0 folded onto +0 first, as the
+// reference's comparator treats them as equal).
+__device__ __forceinline__ uint32_t f2o(float f) {
+    const uint32_t b = __float_as_uint(f + 0.0f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+
+__global__ void k_iota(uint32_t* __restrict__ v, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) v[i] = i;
+}
+
+__global__ void k_axis_keys(const float3* __restrict__ pts, const uint32_t* __restrict__ idx, uint32_t n, int axis,
+                            uint32_t* __restrict__ keys) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float3 p = pts[idx[i]];
+    keys[i] = f2o(axis == 0 ? p.x : axis == 1 ? p.y : p.z);
+}
+
+__global__ void k_run_heads(const float3* __restrict__ pts, const uint32_t* __restrict__ idx, uint32_t n,
+                            uint32_t* __restrict__ head) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t h = 1;
+    if (i > 0) {
+        const float3 a = pts[idx[i]], b = pts[idx[i - 1]];
+        h = (a.x != b.x || a.y != b.y || a.z != b.z) ? 1u : 0u;
+    }
+    head[i] = h;
+}
+
+// run[i] = (exclusive scan of heads)[i] + head[i] - 1; the head of a run is
+// its first occurrence in generation order (stable sort keeps that order).
+__global__ void k_mark_heads(const uint32_t* __restrict__ idx, const uint32_t* __restrict__ head,
+                             const uint32_t* __restrict__ head_scan, uint32_t n, uint32_t* __restrict__ head_orig,
+                             uint32_t* __restrict__ run_of_orig, uint32_t* __restrict__ mark) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t run = head_scan[i] + head[i] - 1u;
+    const uint32_t orig = idx[i];
+    run_of_orig[orig] = run;
+    if (head[i]) {
+        head_orig[run] = orig;
+        mark[orig] = 1u;
+    }
+}
+
+__global__ void k_emit_mesh(const float3* __restrict__ pts, const uint32_t* __restrict__ head_orig,
+                            const uint32_t* __restrict__ run_of_orig, const uint32_t* __restrict__ mark,
+                            const uint32_t* __restrict__ vid, uint32_t n, float3* __restrict__ vces,
+                            uint32_t* __restrict__ ices) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const uint32_t h = head_orig[run_of_orig[p]];
+    const uint32_t id = vid[h];
+    ices[p] = id;
+    if (mark[p]) vces[id] = pts[p];
+}
+
+// ------------------------------------------------------------- flattening
+__global__ void k_flatten(const FlatDesc* __restrict__ desc, uint32_t nthings, uint32_t nprims,
+                          float4* __restrict__ out) {
+    const uint32_t pid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pid >= nprims) return;
+    // last thing whose prim_offset <= pid
+    uint32_t lo = 0, hi = nthings;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (desc[mid].prim_offset <= pid) lo = mid; else hi = mid;
+    }
+    const FlatDesc& d = desc[lo];
+    const uint32_t thing = lo;
+    float4* o = out + 3 * size_t(pid);
+    if (d.analytic) {
+        o[0] = make_float4(d.sphere.x, d.sphere.y, d.sphere.z, __uint_as_float(thing));
+        o[1] = make_float4(d.sphere.w, 0.f, 0.f, __uint_as_float(pid));
+        o[2] = make_float4(0.f, 0.f, 0.f, __uint_as_float(kPrimSphere));
+        return;
+    }
+    const uint3 tri = d.idx[pid - d.prim_offset];
+    const float* t = d.T;
+    auto xf = [&](uint32_t vi) {
+        const float3 a = d.v[vi];
+        // optx/optics_i.cu:46-62: object-to-world transform, left to right
+        return mk(a.x * t[0] + a.y * t[1] + a.z * t[2] + t[3], a.x * t[4] + a.y * t[5] + a.z * t[6] + t[7],
+                  a.x * t[8] + a.y * t[9] + a.z * t[10] + t[11]);
+    };
+    const float3 A = xf(tri.x), B = xf(tri.y), C = xf(tri.z);
+    o[0] = make_float4(A.x, A.y, A.z, __uint_as_float(thing));
+    o[1] = make_float4(B.x, B.y, B.z, __uint_as_float(pid));
+    o[2] = make_float4(C.x, C.y, C.z, __uint_as_float(kPrimTriangle));
+}
+
+// ------------------------------------------------------------------- LBVH
+struct Box3 {
+    float3 lo, hi;
+};
+
+__device__ __forceinline__ Box3 prim_box(const float4* __restrict__ rec) {
+    const float4 a = rec[0], b = rec[1], c = rec[2];
+    if (__float_as_uint(c.w) == kPrimTriangle) {
+        return Box3{mk(fminf(fminf(a.x, b.x), c.x), fminf(fminf(a.y, b.y), c.y), fminf(fminf(a.z, b.z), c.z)),
+                    mk(fmaxf(fmaxf(a.x, b.x), c.x), fmaxf(fmaxf(a.y, b.y), c.y), fmaxf(fmaxf(a.z, b.z), c.z))};
+    }
+    const float r = b.x;
+    return Box3{mk(a.x - r, a.y - r, a.z - r), mk(a.x + r, a.y + r, a.z + r)};
+}
+
+__device__ __forceinline__ float3 centroid(const Box3& b) { return mul(0.5f, add(b.lo, b.hi)); }
+
+__device__ __forceinline__ uint32_t ford(float f) {   // float -> orderable u32 (no -0 folding needed for min/max)
+    const uint32_t b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float fdeord(uint32_t o) {
+    return __uint_as_float((o & 0x80000000u) ? (o & 0x7FFFFFFFu) : ~o);
+}
+
+__global__ void k_init_bounds(uint32_t* b) {
+    if (threadIdx.x < 3) b[threadIdx.x] = 0xFFFFFFFFu;       // min
+    else if (threadIdx.x < 6) b[threadIdx.x] = 0u;          // max
+}
+
+__global__ void k_centroid_bounds(const float4* __restrict__ prims, uint32_t n, uint32_t* __restrict__ bounds) {
+    __shared__ uint32_t s[6];
+    if (threadIdx.x < 3) s[threadIdx.x] = 0xFFFFFFFFu;
+    else if (threadIdx.x < 6) s[threadIdx.x] = 0u;
+    __syncthreads();
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const float3 c = centroid(prim_box(prims + 3 * size_t(i)));
+        atomicMin(&s[0], ford(c.x)); atomicMin(&s[1], ford(c.y)); atomicMin(&s[2], ford(c.z));
+        atomicMax(&s[3], ford(c.x)); atomicMax(&s[4], ford(c.y)); atomicMax(&s[5], ford(c.z));
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) atomicMin(&bounds[threadIdx.x], s[threadIdx.x]);
+    else if (threadIdx.x < 6) atomicMax(&bounds[threadIdx.x], s[threadIdx.x]);
+}
+
+__device__ __forceinline__ uint32_t expand10(uint32_t x) {
+    x = (x * 0x00010001u) & 0xFF0000FFu;
+    x = (x * 0x00000101u) & 0x0F00F00Fu;
+    x = (x * 0x00000011u) & 0xC30C30C3u;
+    x = (x * 0x00000005u) & 0x49249249u;
+    return x;
+}
+__device__ __forceinline__ unsigned long long expand20(unsigned long long x) {
+    x &= 0xFFFFFull;
+    x = (x | x << 32) & 0x001F00000000FFFFull;
+    x = (x | x << 16) & 0x001F0000FF0000FFull;
+    x = (x | x << 8) & 0x100F00F00F00F00Full;
+    x = (x | x << 4) & 0x10C30C30C30C30C3ull;
+    x = (x | x << 2) & 0x1249249249249249ull;
+    return x;
+}
+__device__ __forceinline__ float quantf(float c, float lo, float ext, float cells) {
+    const float f = ext > 0.f ? (c - lo) / ext : 0.f;
+    const float q = f * cells;
+    const float top = cells - 1.f;
+    return q < 0.f ? 0.f : (q > top ? top : q);
+}
+
+template <class K>
+__global__ void k_morton(const float4* __restrict__ prims, uint32_t n, const uint32_t* __restrict__ bounds,
+                         K* __restrict__ codes, uint32_t* __restrict__ ids) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float3 lo = mk(fdeord(bounds[0]), fdeord(bounds[1]), fdeord(bounds[2]));
+    const float3 hi = mk(fdeord(bounds[3]), fdeord(bounds[4]), fdeord(bounds[5]));
+    const float3 ext = sub(hi, lo);
+    const float3 c = centroid(prim_box(prims + 3 * size_t(i)));
+    if (sizeof(K) == 4) {
+        const uint32_t qx = uint32_t(quantf(c.x, lo.x, ext.x, 1024.f));
+        const uint32_t qy = uint32_t(quantf(c.y, lo.y, ext.y, 1024.f));
+        const uint32_t qz = uint32_t(quantf(c.z, lo.z, ext.z, 1024.f));
+        codes[i] = K((expand10(qx) << 2) | (expand10(qy) << 1) | expand10(qz));
+    } else {
+        const unsigned long long qx = (unsigned long long)(quantf(c.x, lo.x, ext.x, 1048576.f));
+        const unsigned long long qy = (unsigned long long)(quantf(c.y, lo.y, ext.y, 1048576.f));
+        const unsigned long long qz = (unsigned long long)(quantf(c.z, lo.z, ext.z, 1048576.f));
+        codes[i] = K((expand20(qx) << 2) | (expand20(qy) << 1) | expand20(qz));
+    }
+    ids[i] = i;
+}
+
+// Karras 2012 (equal keys fall back to the index bits, 64 + clz(i ^ j)).
+template <class K>
+__device__ __forceinline__ int kdelta(const K* __restrict__ k, int n, int i, int j) {
+    if (j < 0 || j >= n) return -1;
+    const unsigned long long a = (unsigned long long)k[i], b = (unsigned long long)k[j];
+    if (a != b) return __clzll((long long)(a ^ b));
+    return 64 + __clz(i ^ j);
+}
+
+template <class K>
+__global__ void k_karras(const K* __restrict__ k, int n, float4* __restrict__ nodes, int* __restrict__ parent_leaf,
+                         int* __restrict__ parent_int) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    const int d = (kdelta(k, n, i, i + 1) - kdelta(k, n, i, i - 1)) >= 0 ? 1 : -1;
+    const int dmin = kdelta(k, n, i, i - d);
+    int lmax = 2;
+    while (kdelta(k, n, i, i + lmax * d) > dmin) lmax <<= 1;
+    int l = 0;
+    for (int t = lmax >> 1; t >= 1; t >>= 1)
+        if (kdelta(k, n, i, i + (l + t) * d) > dmin) l += t;
+    const int j = i + l * d;
+    const int dnode = kdelta(k, n, i, j);
+    int s = 0;
+    int t = l;
+    do {
+        t = (t + 1) >> 1;
+        if (kdelta(k, n, i, i + (s + t) * d) > dnode) s += t;
+    } while (t > 1);
+    const int gamma = i + s * d + (d < 0 ? -1 : 0);
+    const int lo = min(i, j), hi = max(i, j);
+    const int left = (lo == gamma) ? ~gamma : gamma;
+    const int right = (hi == gamma + 1) ? ~(gamma + 1) : gamma + 1;
+    nodes[4 * size_t(i) + 3] = make_float4(__int_as_float(left), __int_as_float(right), 0.f, 0.f);
+    if (left < 0) parent_leaf[~left] = i; else parent_int[left] = i;
+    if (right < 0) parent_leaf[~right] = i; else parent_int[right] = i;
+    if (i == 0) parent_int[0] = -1;
+}
+
+__global__ void k_gather_prims(const float4* __restrict__ flat, const uint32_t* __restrict__ ids, uint32_t n,
+                               float4* __restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4* s = flat + 3 * size_t(ids[i]);
+    float4* o = out + 3 * size_t(i);
+    o[0] = s[0];
+    o[1] = s[1];
+    o[2] = s[2];
+}
+
+__device__ __forceinline__ void write_child_box(float4* node, int slot, const Box3& b) {
+    float* f = reinterpret_cast<float*>(node);
+    if (slot == 0) {
+        f[0] = b.lo.x; f[1] = b.hi.x; f[2] = b.lo.y; f[3] = b.hi.y;   // n0
+        f[8] = b.lo.z; f[9] = b.hi.z;                                   // n2.xy
+    } else {
+        f[4] = b.lo.x; f[5] = b.hi.x; f[6] = b.lo.y; f[7] = b.hi.y;   // n1
+        f[10] = b.lo.z; f[11] = b.hi.z;                                 // n2.zw
+    }
+}
+
+// Bottom-up refit: every leaf writes its box into its parent's slot; the
+// second thread to arrive at a node (atomic counter) unites both child boxes
+// and climbs on.  No thread ever waits, so the kernel cannot stall.
+__global__ void k_refit(const float4* __restrict__ prims, uint32_t n, float4* nodes, const int* __restrict__ parent_leaf,
+                        const int* __restrict__ parent_int, uint32_t* flags) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Box3 b = prim_box(prims + 3 * size_t(i));
+    int child = ~int(i);
+    int p = parent_leaf[i];
+    while (p >= 0) {
+        const float4 n3 = __ldcg(nodes + 4 * size_t(p) + 3);
+        const int slot = (__float_as_int(n3.x) == child) ? 0 : 1;
+        write_child_box(nodes + 4 * size_t(p), slot, b);
+        __threadfence();
+        const uint32_t old = atomicAdd(&flags[p], 1u);
+        if (old == 0u) return;   // first arrival: the sibling finishes the node
+        __threadfence();
+        const float4 n0 = __ldcg(nodes + 4 * size_t(p));
+        const float4 n1 = __ldcg(nodes + 4 * size_t(p) + 1);
+        const float4 n2 = __ldcg(nodes + 4 * size_t(p) + 2);
+        b.lo = mk(fminf(n0.x, n1.x), fminf(n0.z, n1.z), fminf(n2.x, n2.z));
+        b.hi = mk(fmaxf(n0.y, n1.y), fmaxf(n0.w, n1.w), fmaxf(n2.y, n2.w));
+        child = p;
+        p = parent_int[p];
+    }
+}
+
+// Single-primitive scene: node 0 holds the one leaf in both slots.
+__global__ void k_single_leaf(const float4* __restrict__ prims, float4* __restrict__ nodes) {
+    const Box3 b = prim_box(prims);
+    write_child_box(nodes, 0, b);
+    write_child_box(nodes, 1, b);
+    nodes[3] = make_float4(__int_as_float(~0), __int_as_float(~0), 0.f, 0.f);
+}
+
+__global__ void k_lbvh_snapshot_codes32(const uint32_t* __restrict__ c, uint32_t n, unsigned long long* __restrict__ o) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) o[i] = c[i];
+}
+
+// ------------------------------------------------------------- host side
+inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+void check_optics(const rt_optics* o) {
+    RT_REQUIRE(o != nullptr, "optics is NULL");
+    RT_REQUIRE(o->type >= RT_OPTICS_DIFFUSE && o->type <= RT_OPTICS_REFRACT, "unknown optics type");
+}
+
+void check_transform(const float* t) {
+    RT_REQUIRE(t != nullptr, "transform is NULL");
+    for (int k = 0; k < 12; ++k) RT_REQUIRE(std::isfinite(t[k]), "transform has a non-finite entry");
+}
+
+inline float int_bits_as_float(int i) {
+    float f;
+    std::memcpy(&f, &i, 4);
+    return f;
+}
+
+ThingDev thing_dev(const ThingHost& th) {
+    ThingDev d;
+    const float3 c = th.mesh < 0 ? th.center : make_float3(th.T[3], th.T[7], th.T[11]);
+    d.albedo_type = make_float4(th.optics.albedo.x, th.optics.albedo.y, th.optics.albedo.z,
+                                int_bits_as_float(th.optics.type));
+    d.center_fuzz = make_float4(c.x, c.y, c.z, th.optics.fuzz);
+    d.index_pad = make_float4(th.optics.index, 0.f, 0.f, 0.f);
+    return d;
+}
+
+// Uploads things + flattening descriptors and flattens into prims_flat.
+void flatten(Scene& sc, cudaStream_t s) {
+    const uint32_t nt = uint32_t(sc.things.size());
+    std::vector<FlatDesc> desc(nt);
+    std::vector<ThingDev> td(nt);
+    uint64_t off = 0;
+    for (uint32_t k = 0; k < nt; ++k) {
+        const ThingHost& th = sc.things[k];
+        FlatDesc& d = desc[k];
+        std::memset(&d, 0, sizeof(d));
+        d.prim_offset = uint32_t(off);
+        if (th.mesh < 0) {
+            d.analytic = 1;
+            d.nprims = 1;
+            d.sphere = make_float4(th.center.x, th.center.y, th.center.z, th.radius);
+        } else {
+            const MeshDev& m = sc.meshes[th.mesh];
+            d.v = m.v.as<float3>();
+            d.idx = m.i.as<uint3>();
+            d.nprims = m.ni;
+            std::memcpy(d.T, th.T, sizeof(d.T));
+        }
+        off += d.nprims;
+        td[k] = thing_dev(th);
+    }
+    RT_REQUIRE(off < (uint64_t(1) << 31), "scene has too many primitives (>= 2^31)");
+    sc.nprims = uint32_t(off);
+    sc.desc.reserve(std::max<size_t>(1, nt) * sizeof(FlatDesc));
+    sc.things_dev.reserve(std::max<size_t>(1, nt) * sizeof(ThingDev));
+    if (nt) {
+        RT_CUDA(cudaMemcpyAsync(sc.desc.p, desc.data(), nt * sizeof(FlatDesc), cudaMemcpyHostToDevice, s));
+        RT_CUDA(cudaMemcpyAsync(sc.things_dev.p, td.data(), nt * sizeof(ThingDev), cudaMemcpyHostToDevice, s));
+    }
+    sc.prims_flat.reserve(std::max<size_t>(1, sc.nprims) * 48);
+    if (sc.nprims) {
+        k_flatten<<<grid_for(sc.nprims), kThreads, 0, s>>>(sc.desc.as<FlatDesc>(), nt, sc.nprims,
+                                                            sc.prims_flat.as<float4>());
+        RT_CHECK_LAUNCH();
+    }
+    // host copies of desc/td must outlive the async copies
+    RT_CUDA(cudaStreamSynchronize(s));
+}
+
+void refit(Scene& sc, cudaStream_t s) {
+    const uint32_t n = sc.nprims;
+    if (n == 0) return;
+    k_gather_prims<<<grid_for(n), kThreads, 0, s>>>(sc.prims_flat.as<float4>(), sc.ids.as<uint32_t>(), n,
+                                                     sc.prims.as<float4>());
+    RT_CHECK_LAUNCH();
+    if (n == 1) {
+        k_single_leaf<<<1, 1, 0, s>>>(sc.prims.as<float4>(), sc.nodes.as<float4>());
+        RT_CHECK_LAUNCH();
+        return;
+    }
+    int* parents = sc.parents.as<int>();
+    RT_CUDA(cudaMemsetAsync(sc.flags.p, 0, size_t(n - 1) * sizeof(uint32_t), s));
+    k_refit<<<grid_for(n), kThreads, 0, s>>>(sc.prims.as<float4>(), n, sc.nodes.as<float4>(), parents,
+                                              parents + n, sc.flags.as<uint32_t>());
+    RT_CHECK_LAUNCH();
+}
+
+template <class K>
+void build_topology(Scene& sc, cudaStream_t s) {
+    const uint32_t n = sc.nprims;
+    sc.codes.reserve(size_t(n) * sizeof(K));
+    sc.ids.reserve(size_t(n) * sizeof(uint32_t));
+    K* codes = sc.codes.as<K>();
+    uint32_t* ids = sc.ids.as<uint32_t>();
+    k_morton<K><<<grid_for(n), kThreads, 0, s>>>(sc.prims_flat.as<float4>(), n, sc.bounds.as<uint32_t>(), codes, ids);
+    RT_CHECK_LAUNCH();
+    if (sizeof(K) == 4)
+        radix_sort_pairs_u32(reinterpret_cast<uint32_t*>(codes), ids, n, sc.morton_bits, sc.sort_tmp, s);
+    else
+        radix_sort_pairs_u64(reinterpret_cast<unsigned long long*>(codes), ids, n, sc.morton_bits, sc.sort_tmp, s);
+    if (n > 1) {
+        int* parents = sc.parents.as<int>();
+        k_karras<K><<<grid_for(n - 1), kThreads, 0, s>>>(codes, int(n), sc.nodes.as<float4>(), parents, parents + n);
+        RT_CHECK_LAUNCH();
+    }
+}
+
+void build(Scene& sc, int morton_bits, cudaStream_t s) {
+    RT_REQUIRE(morton_bits == 0 || morton_bits == 30 || morton_bits == 60, "morton_bits must be 0, 30 or 60");
+    sc.morton_bits = morton_bits == 0 ? 60 : morton_bits;
+    cudaEvent_t e0, e1;
+    RT_CUDA(cudaEventCreate(&e0));
+    RT_CUDA(cudaEventCreate(&e1));
+    RT_CUDA(cudaEventRecord(e0, s));
+    flatten(sc, s);
+    const uint32_t n = sc.nprims;
+    sc.prims.reserve(std::max<size_t>(1, n) * 48);
+    sc.nodes.reserve(std::max<size_t>(1, n > 1 ? n - 1 : 1) * 64);
+    sc.parents.reserve((size_t(n) * 2 + 1) * sizeof(int));
+    sc.flags.reserve(std::max<size_t>(1, n) * sizeof(uint32_t));
+    sc.bounds.reserve(6 * sizeof(uint32_t));
+    sc.misc.reserve(256);
+    if (n > 0) {
+        k_init_bounds<<<1, 32, 0, s>>>(sc.bounds.as<uint32_t>());
+        RT_CHECK_LAUNCH();
+        k_centroid_bounds<<<grid_for(n), kThreads, 0, s>>>(sc.prims_flat.as<float4>(), n, sc.bounds.as<uint32_t>());
+        RT_CHECK_LAUNCH();
+        if (sc.morton_bits == 30) build_topology<uint32_t>(sc, s);
+        else build_topology<unsigned long long>(sc, s);
+        refit(sc, s);
+    }
+    RT_CUDA(cudaEventRecord(e1, s));
+    RT_CUDA(cudaEventSynchronize(e1));
+    RT_CUDA(cudaEventElapsedTime(&sc.build_ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    sc.built = true;
+    sc.topology_dirty = false;
+    sc.xf_dirty = false;
+}
+
+void update(Scene& sc, cudaStream_t s) {
+    if (!sc.built) throw Error(RT_ERR_NOT_BUILT, "rt_scene_update before rt_scene_build");
+    if (sc.topology_dirty) throw Error(RT_ERR_NOT_BUILT, "things were added since the last build; rebuild");
+    cudaEvent_t e0, e1;
+    RT_CUDA(cudaEventCreate(&e0));
+    RT_CUDA(cudaEventCreate(&e1));
+    RT_CUDA(cudaEventRecord(e0, s));
+    flatten(sc, s);
+    refit(sc, s);
+    RT_CUDA(cudaEventRecord(e1, s));
+    RT_CUDA(cudaEventSynchronize(e1));
+    RT_CUDA(cudaEventElapsedTime(&sc.refit_ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    sc.xf_dirty = false;
+}
+
+void tessellate(Scene& sc, float radius, uint32_t ndiv, cudaStream_t s, uint32_t* mesh_id) {
+    RT_REQUIRE(ndiv <= 10, "ndiv must be <= 10");
+    RT_REQUIRE(std::isfinite(radius), "radius must be finite");
+    const uint32_t ntri = 4u << (2 * ndiv);
+    const uint32_t m = 3 * ntri;   // vertex instances in generation order
+    DevBuf pts, idx, keys, head, head_scan, head_orig, run_of_orig, mark, vid, scan_tmp, sort_tmp;
+    pts.reserve(size_t(m) * sizeof(float3));
+    idx.reserve(size_t(m) * 4);
+    keys.reserve(size_t(m) * 4);
+    head.reserve(size_t(m) * 4);
+    head_scan.reserve(size_t(m) * 4);
+    head_orig.reserve(size_t(m) * 4);
+    run_of_orig.reserve(size_t(m) * 4);
+    mark.reserve(size_t(m) * 4);
+    vid.reserve(size_t(m) * 4);
+    k_tess_leaves<<<grid_for(ntri), kThreads, 0, s>>>(radius, ndiv, ntri, pts.as<float3>());
+    RT_CHECK_LAUNCH();
+    k_iota<<<grid_for(m), kThreads, 0, s>>>(idx.as<uint32_t>(), m);
+    RT_CHECK_LAUNCH();
+    // lexicographic (x, y, z) stable sort as three stable passes z, y, x
+    for (int axis = 2; axis >= 0; --axis) {
+        k_axis_keys<<<grid_for(m), kThreads, 0, s>>>(pts.as<float3>(), idx.as<uint32_t>(), m, axis, keys.as<uint32_t>());
+        RT_CHECK_LAUNCH();
+        radix_sort_pairs_u32(keys.as<uint32_t>(), idx.as<uint32_t>(), m, 32, sort_tmp, s);
+    }
+    k_run_heads<<<grid_for(m), kThreads, 0, s>>>(pts.as<float3>(), idx.as<uint32_t>(), m, head.as<uint32_t>());
+    RT_CHECK_LAUNCH();
+    scan_exclusive_u32(head.as<uint32_t>(), head_scan.as<uint32_t>(), m, scan_tmp, s);
+    RT_CUDA(cudaMemsetAsync(mark.p, 0, size_t(m) * 4, s));
+    k_mark_heads<<<grid_for(m), kThreads, 0, s>>>(idx.as<uint32_t>(), head.as<uint32_t>(), head_scan.as<uint32_t>(), m,
+                                                  head_orig.as<uint32_t>(), run_of_orig.as<uint32_t>(),
+                                                  mark.as<uint32_t>());
+    RT_CHECK_LAUNCH();
+    scan_exclusive_u32(mark.as<uint32_t>(), vid.as<uint32_t>(), m, scan_tmp, s);
+    uint32_t last_vid = 0, last_mark = 0;
+    RT_CUDA(cudaMemcpyAsync(&last_vid, vid.as<uint32_t>() + (m - 1), 4, cudaMemcpyDeviceToHost, s));
+    RT_CUDA(cudaMemcpyAsync(&last_mark, mark.as<uint32_t>() + (m - 1), 4, cudaMemcpyDeviceToHost, s));
+    RT_CUDA(cudaStreamSynchronize(s));
+    const uint32_t nv = last_vid + last_mark;
+    MeshDev mesh;
+    mesh.v.reserve(size_t(nv) * sizeof(float3));
+    mesh.i.reserve(size_t(ntri) * sizeof(uint3));
+    mesh.nv = nv;
+    mesh.ni = ntri;
+    k_emit_mesh<<<grid_for(m), kThreads, 0, s>>>(pts.as<float3>(), head_orig.as<uint32_t>(),
+                                                 run_of_orig.as<uint32_t>(), mark.as<uint32_t>(), vid.as<uint32_t>(), m,
+                                                 mesh.v.as<float3>(), mesh.i.as<uint32_t>());
+    RT_CHECK_LAUNCH();
+    RT_CUDA(cudaStreamSynchronize(s));
+    sc.meshes.push_back(std::move(mesh));
+    *mesh_id = uint32_t(sc.meshes.size() - 1);
+}
+
+}  // namespace
+
+size_t Scene::device_bytes() const {
+    size_t b = things_dev.bytes + desc.bytes + prims_flat.bytes + prims.bytes + nodes.bytes + codes.bytes + ids.bytes +
+               parents.bytes + flags.bytes + bounds.bytes + sort_tmp.bytes + misc.bytes;
+    for (const auto& m : meshes) b += m.v.bytes + m.i.bytes;
+    return b;
+}
+
+Scene* scene_from(rt_scene h) {
+    RT_REQUIRE(h != nullptr, "scene handle is NULL");
+    return reinterpret_cast<Scene*>(h);
+}
+
+}  // namespace rt
+
+using namespace rt;
+
+extern "C" {
+
+rt_status rt_scene_create(rt_scene* out) {
+    return guarded([&] {
+        RT_REQUIRE(out != nullptr, "out is NULL");
+        *out = reinterpret_cast<rt_scene>(new Scene());
+    });
+}
+
+rt_status rt_scene_destroy(rt_scene scene) {
+    return guarded([&] {
+        if (scene) delete reinterpret_cast<Scene*>(scene);
+    });
+}
+
+rt_status rt_scene_add_mesh(rt_scene scene, const rt_float3* vces, unsigned int nv, const rt_uint3* ices,
+                            unsigned int ni, unsigned int* mesh_id) {
+    return guarded([&] {
+        Scene* sc = scene_from(scene);
+        RT_REQUIRE(mesh_id != nullptr, "mesh_id is NULL");
+        RT_REQUIRE(nv > 0 && ni > 0 && vces && ices, "mesh needs vertices and triangles");
+        for (unsigned int k = 0; k < ni; ++k)
+            RT_REQUIRE(ices[k].x < nv && ices[k].y < nv && ices[k].z < nv, "triangle index out of range");
+        MeshDev m;
+        m.v.reserve(size_t(nv) * sizeof(float3));
+        m.i.reserve(size_t(ni) * sizeof(uint3));
+        RT_CUDA(cudaMemcpy(m.v.p, vces, size_t(nv) * sizeof(float3), cudaMemcpyHostToDevice));
+        RT_CUDA(cudaMemcpy(m.i.p, ices, size_t(ni) * sizeof(uint3), cudaMemcpyHostToDevice));
+        m.nv = nv;
+        m.ni = ni;
+        sc->meshes.push_back(std::move(m));
+        *mesh_id = unsigned(sc->meshes.size() - 1);
+    });
+}
+
+rt_status rt_scene_add_sphere_mesh(rt_scene scene, float radius, unsigned int ndiv, unsigned int* mesh_id) {
+    return guarded([&] {
+        Scene* sc = scene_from(scene);
+        RT_REQUIRE(mesh_id != nullptr, "mesh_id is NULL");
+        tessellate(*sc, radius, ndiv, nullptr, mesh_id);
+    });
+}
+
+rt_status rt_scene_get_mesh(rt_scene scene, unsigned int mesh_id, rt_float3* vces, unsigned int* nv, rt_uint3* ices,
+                            unsigned int* ni) {
+    return guarded([&] {
+        Scene* sc = scene_from(scene);
+        RT_REQUIRE(mesh_id < sc->meshes.size(), "bad mesh id");
+        const MeshDev& m = sc->meshes[mesh_id];
+        if (nv) *nv = m.nv;
+        if (ni) *ni = m.ni;
+        if (vces) RT_CUDA(cudaMemcpy(vces, m.v.p, size_t(m.nv) * sizeof(float3), cudaMemcpyDeviceToHost));
+        if (ices) RT_CUDA(cudaMemcpy(ices, m.i.p, size_t(m.ni) * sizeof(uint3), cudaMemcpyDeviceToHost));
+    });
+}
+
+rt_status rt_scene_add_thing(rt_scene scene, const rt_optics* optics, unsigned int mesh_id, const float transform[12],
+                             unsigned int* thing_id) {
+    return guarded([&] {
+        Scene* sc = scene_from(scene);
+        check_optics(optics);
+        check_transform(transform);
+        RT_REQUIRE(thing_id != nullptr, "thing_id is NULL");
+        RT_REQUIRE(mesh_id < sc->meshes.size(), "bad mesh id");
+        ThingHost th;
+        th.optics = *optics;
+        th.mesh = int(mesh_id);
+        std::memcpy(th.T, transform, sizeof(th.T));
+        sc->things.push_back(th);
+        sc->topology_dirty = true;
+        *thing_id = unsigned(sc->things.size() - 1);
+    });
+}
+
+rt_status rt_scene_add_analytic_sphere(rt_scene scene, rt_float3 center, float radius, const rt_optics* optics,
+                                       unsigned int* thing_id) {
+    return guarded([&] {
+        Scene* sc = scene_from(scene);
+        check_optics(optics);
+        RT_REQUIRE(thing_id != nullptr, "thing_id is NULL");
+        RT_REQUIRE(std::isfinite(radius) && radius > 0.f, "radius must be positive");
+        ThingHost th;
+        th.optics = *optics;
+        th.mesh = -1;
+        th.center = make_float3(center.x, center.y, center.z);
+        th.radius = radius;
+        const float T[12] = {radius, 0, 0, center.x, 0, radius, 0, center.y, 0, 0, radius, center.z};
+        std::memcpy(th.T, T, sizeof(T));
+        sc->things.push_back(th);
+        sc->topology_dirty = true;
+        *thing_id = unsigned(sc->things.size() - 1);
+    });
+}
+
+rt_status rt_scene_set_transform(rt_scene scene, unsigned int thing_id, const float transform[12]) {
+    return guarded([&] {
+        Scene* sc = scene_from(scene);
+        RT_REQUIRE(thing_id < sc->things.size(), "bad thing id");
+        check_transform(transform);
+        ThingHost& th = sc->things[thing_id];
+        std::memcpy(th.T, transform, sizeof(th.T));
+        if (th.mesh < 0) {   // analytic sphere: translation and the x scale
+            th.center = make_float3(transform[3], transform[7], transform[11]);
+            th.radius = transform[0];
+        }
+        sc->xf_dirty = true;
+    });
+}
+
+rt_status rt_scene_get_transform(rt_scene scene, unsigned int thing_id, float transform[12]) {
+    return guarded([&] {
+        Scene* sc = scene_from(scene);
+        RT_REQUIRE(thing_id < sc->things.size(), "bad thing id");
+        RT_REQUIRE(transform != nullptr, "transform is NULL");
+        std::memcpy(transform, sc->things[thing_id].T, 12 * sizeof(float));
+    });
+}
+
+rt_status rt_scene_set_optics(rt_scene scene, unsigned int thing_id, const rt_optics* optics) {
+    return guarded([&] {
+        Scene* sc = scene_from(scene);
+        RT_REQUIRE(thing_id < sc->things.size(), "bad thing id");
+        check_optics(optics);
+        sc->things[thing_id].optics = *optics;
+        sc->xf_dirty = true;
+    });
+}
+
+rt_status rt_scene_build(rt_scene scene, unsigned int morton_bits, void* stream) {
+    return guarded([&] { build(*scene_from(scene), int(morton_bits), as_stream(stream)); });
+}
+
+rt_status rt_scene_update(rt_scene scene, void* stream) {
+    return guarded([&] { update(*scene_from(scene), as_stream(stream)); });
+}
+
+rt_status rt_scene_info_get(rt_scene scene, rt_scene_info* info) {
+    return guarded([&] {
+        Scene* sc = scene_from(scene);
+        RT_REQUIRE(info != nullptr, "info is NULL");
+        info->n_meshes = unsigned(sc->meshes.size());
+        info->n_things = unsigned(sc->things.size());
+        info->n_prims = sc->nprims;
+        info->morton_bits = unsigned(sc->morton_bits);
+        info->device_bytes = sc->device_bytes();
+        info->build_ms = sc->build_ms;
+        info->refit_ms = sc->refit_ms;
+    });
+}
+
+rt_status rt_scene_get_lbvh(rt_scene scene, unsigned long long* codes, unsigned int* ids, int* left, int* right,
+                            float* boxes) {
+    return guarded([&] {
+        Scene* sc = scene_from(scene);
+        if (!sc->built) throw Error(RT_ERR_NOT_BUILT, "scene not built");
+        const uint32_t n = sc->nprims;
+        if (n == 0) return;
+        if (codes) {
+            if (sc->morton_bits == 30) {
+                DevBuf tmp;
+                tmp.reserve(size_t(n) * 8);
+                k_lbvh_snapshot_codes32<<<grid_for(n), kThreads>>>(sc->codes.as<uint32_t>(), n,
+                                                                    tmp.as<unsigned long long>());
+                RT_CHECK_LAUNCH();
+                RT_CUDA(cudaMemcpy(codes, tmp.p, size_t(n) * 8, cudaMemcpyDeviceToHost));
+            } else {
+                RT_CUDA(cudaMemcpy(codes, sc->codes.p, size_t(n) * 8, cudaMemcpyDeviceToHost));
+            }
+        }
+        if (ids) RT_CUDA(cudaMemcpy(ids, sc->ids.p, size_t(n) * 4, cudaMemcpyDeviceToHost));
+        if (n < 2) return;
+        std::vector<float4> nodes(size_t(n - 1) * 4);
+        RT_CUDA(cudaMemcpy(nodes.data(), sc->nodes.p, nodes.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+        for (uint32_t i = 0; i + 1 < n; ++i) {
+            const float4 n0 = nodes[4 * i], n1 = nodes[4 * i + 1], n2 = nodes[4 * i + 2], n3 = nodes[4 * i + 3];
+            int l, r;
+            std::memcpy(&l, &n3.x, 4);
+            std::memcpy(&r, &n3.y, 4);
+            if (left) left[i] = l;
+            if (right) right[i] = r;
+            if (boxes) {
+                float* o = boxes + 12 * size_t(i);
+                o[0] = n0.x; o[1] = n0.z; o[2] = n2.x;   // lo0
+                o[3] = n0.y; o[4] = n0.w; o[5] = n2.y;   // hi0
+                o[6] = n1.x; o[7] = n1.z; o[8] = n2.z;   // lo1
+                o[9] = n1.y; o[10] = n1.w; o[11] = n2.w; // hi1
+            }
+        }
+    });
+}
+
+rt_status rt_radix_sort_pairs(void* keys, unsigned int* vals, unsigned int n, unsigned int key_bits, void* stream) {
+    return guarded([&] {
+        RT_REQUIRE(keys != nullptr && vals != nullptr, "keys/vals are NULL");
+        RT_REQUIRE(key_bits >= 1 && key_bits <= 64, "key_bits must be 1..64");
+        DevBuf tmp;
+        cudaStream_t s = as_stream(stream);
+        if (key_bits <= 32) radix_sort_pairs_u32(static_cast<uint32_t*>(keys), vals, n, int(key_bits), tmp, s);
+        else radix_sort_pairs_u64(static_cast<unsigned long long*>(keys), vals, n, int(key_bits), tmp, s);
+        RT_CUDA(cudaStreamSynchronize(s));
+    });
+}
+
+}  // extern "C"
