@@ -201,11 +201,13 @@ rt_status rt_launch_ex(rt_scene scene, const rt_camera* cam, const rt_launch_par
                        const rt_frame* frame, void* stream, rt_launch_stats* stats);
 
 /* Primary-ray closest hit of sample `sample` for every pixel (parity and
- * picking): prim id (global, -1 on a miss), thing id, t, barycentrics u, v.
+ * picking): prim id (global, -1 on a miss), thing id, binary32 distance t
+ * and barycentrics u, v of the selection, and t64, the distance to the
+ * selected primitive re-evaluated in double precision (NaN on a miss).
  * Device buffers of w*h entries each; any but prim may be NULL. */
 rt_status rt_first_hit(rt_scene scene, const rt_camera* cam, const rt_launch_params* params,
                        unsigned int sample, int* prim, int* thing, float* t, float* u, float* v,
-                       void* stream);
+                       double* t64, void* stream);
 
 /* Picker: the 1x1 launch of SimpleSM::eaEdtSed (optx/simplesm.cxx:1014-1034,
  * optx/optics_i.cu:25-29): thing id under pixel (x, y), or 0xFFFFFFFF on a

@@ -109,7 +109,7 @@ SIGNATURES = {
     "rt_launch": [_P, ctypes.POINTER(Camera), ctypes.POINTER(LaunchParams), ctypes.POINTER(Frame), _P],
     "rt_launch_ex": [_P, ctypes.POINTER(Camera), ctypes.POINTER(LaunchParams), ctypes.POINTER(Frame), _P,
                      ctypes.POINTER(LaunchStats)],
-    "rt_first_hit": [_P, ctypes.POINTER(Camera), ctypes.POINTER(LaunchParams), _U, _P, _P, _P, _P, _P, _P],
+    "rt_first_hit": [_P, ctypes.POINTER(Camera), ctypes.POINTER(LaunchParams), _U, _P, _P, _P, _P, _P, _P, _P],
     "rt_pick": [_P, ctypes.POINTER(Camera), ctypes.POINTER(LaunchParams), _U, _U, _PU, _P],
     "rt_postproc_srgb": [_P, _P, _I, _I, _P],
     "rt_postproc_none": [_P, _P, _I, _I, _P],

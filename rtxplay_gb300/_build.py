@@ -80,7 +80,7 @@ def build_library(extra=(), verbose=False, jobs=None):
 def build_rtwo():
     """Builds the rtwo launcher (C++ host code over the C ABI)."""
     src = os.path.join(HERE, "host", "rtwo.cpp")
-    hdrs = [os.path.join(HERE, "host", "rtwo.hpp"), os.path.join(ROOT, "include", "rt_api.h")]
+    hdrs = [os.path.join(ROOT, "include", "rtwo.hpp"), os.path.join(ROOT, "include", "rt_api.h")]
     if not os.path.exists(src):
         return None
     if _stale(RTWO, [src, LIB] + hdrs):

@@ -339,11 +339,43 @@ __global__ void __launch_bounds__(kThreads) k_finalize(const float4* __restrict_
     if (lane_id() == 0 && r) atomicAdd(&st->rays, r);
 }
 
+// FP64 distance from the (binary32) ray to the selected primitive: the
+// binary32 Moller-Trumbore t loses digits on grazing hits (its error grows
+// like 1/sin of the grazing angle), so the reported distance re-evaluates the
+// winner in double precision; the selection itself stays binary32.
+__device__ double dist64(const float4* __restrict__ rec, float3 of, float3 df) {
+    const float4 a = __ldg(rec), b = __ldg(rec + 1), c = __ldg(rec + 2);
+    const double o[3] = {of.x, of.y, of.z}, d[3] = {df.x, df.y, df.z};
+    if (__float_as_uint(c.w) == kPrimTriangle) {
+        const double A[3] = {a.x, a.y, a.z}, B[3] = {b.x, b.y, b.z}, C[3] = {c.x, c.y, c.z};
+        const double e1[3] = {B[0] - A[0], B[1] - A[1], B[2] - A[2]};
+        const double e2[3] = {C[0] - A[0], C[1] - A[1], C[2] - A[2]};
+        const double pv[3] = {d[1] * e2[2] - d[2] * e2[1], d[2] * e2[0] - d[0] * e2[2], d[0] * e2[1] - d[1] * e2[0]};
+        const double det = e1[0] * pv[0] + e1[1] * pv[1] + e1[2] * pv[2];
+        if (det == 0.0) return __longlong_as_double(0x7FF8000000000000ll);
+        const double tv[3] = {o[0] - A[0], o[1] - A[1], o[2] - A[2]};
+        const double qv[3] = {tv[1] * e1[2] - tv[2] * e1[1], tv[2] * e1[0] - tv[0] * e1[2],
+                              tv[0] * e1[1] - tv[1] * e1[0]};
+        return (e2[0] * qv[0] + e2[1] * qv[1] + e2[2] * qv[2]) / det;
+    }
+    const double oc[3] = {o[0] - a.x, o[1] - a.y, o[2] - a.z};
+    const double qa = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    const double qb = d[0] * oc[0] + d[1] * oc[1] + d[2] * oc[2];
+    const double qc = (oc[0] * oc[0] + oc[1] * oc[1] + oc[2] * oc[2]) - double(b.x) * b.x;
+    const double disc = qb * qb - qa * qc;
+    if (disc < 0.0) return __longlong_as_double(0x7FF8000000000000ll);
+    const double x = sqrt(disc);
+    double t = (-qb - x) / qa;
+    if (t < double(kTmin)) t = (-qb + x) / qa;
+    return t;
+}
+
 // Primary-ray closest hit of one sample for a pixel rectangle.
 __global__ void __launch_bounds__(kThreads) k_first_hit(RenderArgs a, uint32_t sample, uint32_t x0, uint32_t y0,
                                                         uint32_t nx, uint32_t ny, const float4* __restrict__ nodes,
                                                         const float4* __restrict__ prims, uint32_t nprims, int* prim,
-                                                        int* thing, float* t, float* u, float* v, uint32_t* err) {
+                                                        int* thing, float* t, float* u, float* v, double* t64,
+                                                        uint32_t* err) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nx * ny) return;
     const uint32_t x = x0 + k % nx, y = y0 + k / nx;
@@ -360,6 +392,7 @@ __global__ void __launch_bounds__(kThreads) k_first_hit(RenderArgs a, uint32_t s
         if (t) t[k] = 0.f;
         if (u) u[k] = 0.f;
         if (v) v[k] = 0.f;
+        if (t64) t64[k] = __longlong_as_double(0x7FF8000000000000ll);
         return;
     }
     prim[k] = int(h.id);
@@ -367,6 +400,7 @@ __global__ void __launch_bounds__(kThreads) k_first_hit(RenderArgs a, uint32_t s
     if (t) t[k] = h.t;
     if (u) u[k] = h.u;
     if (v) v[k] = h.v;
+    if (t64) t64[k] = dist64(prims + 3 * h.leaf, o, d);
 }
 
 // ------------------------------------------------------------ post-process
@@ -619,7 +653,7 @@ void render(Scene& sc, const rt_camera& cam, const rt_launch_params& p, const rt
 
 void first_hit_rect(Scene& sc, const rt_camera& cam, const rt_launch_params& p, uint32_t sample, uint32_t x0,
                     uint32_t y0, uint32_t nx, uint32_t ny, int* prim, int* thing, float* t, float* u, float* v,
-                    cudaStream_t s) {
+                    double* t64, cudaStream_t s) {
     check_params(&p);
     if (!sc.built || sc.topology_dirty || sc.xf_dirty) throw Error(RT_ERR_NOT_BUILT, "scene not built or not updated");
     RT_REQUIRE(prim != nullptr, "prim is NULL");
@@ -628,7 +662,7 @@ void first_hit_rect(Scene& sc, const rt_camera& cam, const rt_launch_params& p, 
     RT_CUDA(cudaMemsetAsync(err, 0, 4, s));
     k_first_hit<<<grid_for(uint64_t(nx) * ny), kThreads, 0, s>>>(a, sample, x0, y0, nx, ny, sc.nodes.as<float4>(),
                                                                   sc.prims.as<float4>(), sc.nprims, prim, thing, t, u, v,
-                                                                  err);
+                                                                  t64, err);
     RT_CHECK_LAUNCH();
     uint32_t herr = 0;
     RT_CUDA(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, s));
@@ -690,11 +724,11 @@ rt_status rt_launch_ex(rt_scene scene, const rt_camera* cam, const rt_launch_par
 }
 
 rt_status rt_first_hit(rt_scene scene, const rt_camera* cam, const rt_launch_params* params, unsigned int sample,
-                       int* prim, int* thing, float* t, float* u, float* v, void* stream) {
+                       int* prim, int* thing, float* t, float* u, float* v, double* t64, void* stream) {
     return guarded([&] {
         RT_REQUIRE(cam && params, "cam/params is NULL");
         first_hit_rect(*scene_from(scene), *cam, *params, sample, 0, 0, params->image_w, params->image_h, prim, thing,
-                       t, u, v, as_stream(stream));
+                       t, u, v, t64, as_stream(stream));
     });
 }
 
@@ -707,7 +741,7 @@ rt_status rt_pick(rt_scene scene, const rt_camera* cam, const rt_launch_params* 
         buf.reserve(8);
         cudaStream_t s = as_stream(stream);
         first_hit_rect(*scene_from(scene), *cam, *params, 0, x, y, 1, 1, buf.as<int>(), buf.as<int>() + 1, nullptr,
-                       nullptr, nullptr, s);
+                       nullptr, nullptr, nullptr, s);
         int host[2];
         RT_CUDA(cudaMemcpyAsync(host, buf.p, 8, cudaMemcpyDeviceToHost, s));
         RT_CUDA(cudaStreamSynchronize(s));
@@ -762,7 +796,7 @@ rt_status rt_launcher_ignite(rt_launcher l, rt_scene scene, const rt_camera* cam
             DevBuf buf;
             buf.reserve(8);
             first_hit_rect(sc, *cam, *params, 0, pick_x, pick_y, 1, 1, buf.as<int>(), buf.as<int>() + 1, nullptr,
-                           nullptr, nullptr, s);
+                           nullptr, nullptr, nullptr, s);
             int host[2];
             RT_CUDA(cudaMemcpyAsync(host, buf.p, 8, cudaMemcpyDeviceToHost, s));
             RT_CUDA(cudaStreamSynchronize(s));

@@ -50,11 +50,12 @@ def device_first_hit(R, torch, sc, cam, params, sample=0):
     t = torch.empty(n, dtype=torch.float32, device="cuda")
     u = torch.empty(n, dtype=torch.float32, device="cuda")
     v = torch.empty(n, dtype=torch.float32, device="cuda")
+    t64 = torch.empty(n, dtype=torch.float64, device="cuda")
     R.check(R.lib().rt_first_hit(sc.h, ctypes.byref(cam), ctypes.byref(params), sample, dptr(prim),
-                                 dptr(thing), dptr(t), dptr(u), dptr(v), None))
+                                 dptr(thing), dptr(t), dptr(u), dptr(v), dptr(t64), None))
     torch.cuda.synchronize()
     return dict(prim=prim.cpu().numpy(), thing=thing.cpu().numpy(), t=t.cpu().numpy(),
-                u=u.cpu().numpy(), v=v.cpu().numpy())
+                u=u.cpu().numpy(), v=v.cpu().numpy(), t64=t64.cpu().numpy())
 
 
 def oracle_camera(O, cam):
