@@ -254,6 +254,19 @@ rt_status rt_launcher_download(rt_launcher l, rt_float3* rawRGB, unsigned int* r
 rt_status rt_radix_sort_pairs(void* keys, unsigned int* vals, unsigned int n,
                               unsigned int key_bits, void* stream);
 
+/* No counterpart in the reference.  The same stable pair sort for callers
+ * that may not allocate device memory while they run (an engine that hands
+ * out all device memory from its own pool, or a per-frame loop where a
+ * cudaMalloc would synchronise the device): it allocates nothing and sorts
+ * out of a fixed 3.1 MiB scratch array that every GPU loading the library
+ * holds until the process exits.  n is limited to 262,144 pairs; larger n
+ * returns RT_ERR_INVALID_ARG.  Stream-ordered, does not synchronise.  The
+ * first call on a device looks up the scratch's device address; make it
+ * before any stream capture.  All calls share the scratch, so calls that can
+ * overlap on the GPU (other streams, other host threads) race. */
+rt_status rt_radix_sort_pairs_noalloc(void* keys, unsigned int* vals, unsigned int n,
+                                      unsigned int key_bits, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

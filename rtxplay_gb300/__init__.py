@@ -122,6 +122,7 @@ SIGNATURES = {
     "rt_launcher_frame": [_P, ctypes.POINTER(Frame), ctypes.POINTER(_P), ctypes.POINTER(_P)],
     "rt_launcher_download": [_P, _P, _P, _P, _P, _P, _P],
     "rt_radix_sort_pairs": [_P, _P, _U, _U, _P],
+    "rt_radix_sort_pairs_noalloc": [_P, _P, _U, _U, _P],
 }
 
 _lib = None

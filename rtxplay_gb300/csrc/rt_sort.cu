@@ -9,6 +9,8 @@
 // can spin.  Stability makes the result bit-exact against std::stable_sort.
 #include <algorithm>
 #include <cstdint>
+#include <mutex>
+#include <string>
 #include <vector>
 
 #include "rt_internal.h"
@@ -231,3 +233,132 @@ void radix_sort_pairs_u64(unsigned long long* keys, uint32_t* vals, uint32_t n, 
 }
 
 }  // namespace rt
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of the pair sort.
+//
+// Some callers cannot allocate device memory while they run: a host engine
+// that reserves all device memory for its own pool up front, or a per-frame
+// loop where a cudaMalloc/cudaFree would synchronise the whole device and
+// stall the frame.  For them rt_radix_sort_pairs_noalloc sorts out of a fixed
+// scratch array that lives in this library's device image instead of a
+// cudaMalloc'd buffer.  The array is reserved on every GPU that loads the
+// library and stays reserved until the process exits.
+namespace rt {
+namespace {
+
+constexpr uint32_t kNoAllocMaxPairs = 1u << 18;   // 262,144 (key, value) pairs
+
+struct NoAllocLayout {
+    size_t keys, vals, hist, scan, total;
+};
+
+// Offsets of the sort's scratch inside the fixed array, for n pairs of
+// key_bytes-wide keys (alternate keys and values, digit histograms, scan tree).
+constexpr size_t noalloc_align(size_t b) { return (b + 255) & ~size_t(255); }
+constexpr size_t noalloc_scan_words(uint32_t n) {
+    size_t words = 0;
+    while (n > uint32_t(kScanTile)) {
+        n = (n + kScanTile - 1) / kScanTile;
+        words += n;
+    }
+    return words + 1;
+}
+constexpr NoAllocLayout noalloc_layout(uint32_t n, size_t key_bytes) {
+    const uint32_t nblocks = (n + kSortTile - 1) / kSortTile;
+    const uint32_t nhist = kRadix * nblocks;
+    const size_t keys = 0;
+    const size_t vals = keys + noalloc_align(size_t(n) * key_bytes);
+    const size_t hist = vals + noalloc_align(size_t(n) * sizeof(uint32_t));
+    const size_t scan = hist + noalloc_align(size_t(nhist) * sizeof(uint32_t));
+    const size_t total = scan + noalloc_align(noalloc_scan_words(nhist) * sizeof(uint32_t));
+    return NoAllocLayout{keys, vals, hist, scan, total};
+}
+
+constexpr size_t kNoAllocScratchBytes = noalloc_layout(kNoAllocMaxPairs, 8).total;   // about 3.1 MiB
+
+// The fixed scratch.  Host code must not take its address directly (on the
+// host the name is only a stand-in); the device address comes from
+// cudaGetSymbolAddress, once per device.
+static __device__ __align__(256) unsigned char g_noalloc_sort_scratch[kNoAllocScratchBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+// Device address of the scratch on the current device (set up on first use).
+unsigned char* noalloc_scratch() {
+    int dev = 0;
+    RT_CUDA(cudaGetDevice(&dev));
+    RT_REQUIRE(dev >= 0 && dev < kNoAllocMaxDevices, "device ordinal out of range for the fixed scratch");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        RT_CUDA(cudaGetSymbolAddress(&p, g_noalloc_sort_scratch));
+        g_noalloc_ptr[dev] = p;
+    }
+    return static_cast<unsigned char*>(g_noalloc_ptr[dev]);
+}
+
+template <class K>
+void radix_sort_pairs_fixed(K* keys, uint32_t* vals, uint32_t n, int bits, unsigned char* scratch, cudaStream_t s) {
+    if (n <= 1 || bits <= 0) return;
+    const NoAllocLayout L = noalloc_layout(n, sizeof(K));
+    RT_REQUIRE(L.total <= kNoAllocScratchBytes, "no-allocation sort scratch too small");
+    const uint32_t nblocks = (n + kSortTile - 1) / kSortTile;
+    const uint32_t nhist = kRadix * nblocks;
+    K* alt_keys = reinterpret_cast<K*>(scratch + L.keys);
+    uint32_t* alt_vals = reinterpret_cast<uint32_t*>(scratch + L.vals);
+    uint32_t* hist = reinterpret_cast<uint32_t*>(scratch + L.hist);
+    uint32_t* scan_tmp = reinterpret_cast<uint32_t*>(scratch + L.scan);
+    // Every pass writes all of hist and the scan tree before reading them, so
+    // nothing in the shared scratch has to be cleared between calls.
+    K* src_k = keys;
+    uint32_t* src_v = vals;
+    K* dst_k = alt_keys;
+    uint32_t* dst_v = alt_vals;
+    const int passes = (bits + 7) / 8;
+    for (int p = 0; p < passes; ++p) {
+        const int shift = 8 * p;
+        k_radix_hist<K><<<nblocks, kSortThreads, 0, s>>>(src_k, n, shift, hist, nblocks);
+        RT_CHECK_LAUNCH();
+        scan_rec(hist, hist, nhist, scan_tmp, s);
+        k_radix_scatter<K><<<nblocks, kSortThreads, 0, s>>>(src_k, src_v, n, shift, hist, nblocks, dst_k, dst_v);
+        RT_CHECK_LAUNCH();
+        std::swap(src_k, dst_k);
+        std::swap(src_v, dst_v);
+    }
+    if (src_k != keys) {
+        RT_CUDA(cudaMemcpyAsync(keys, src_k, size_t(n) * sizeof(K), cudaMemcpyDeviceToDevice, s));
+        RT_CUDA(cudaMemcpyAsync(vals, src_v, size_t(n) * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+    }
+}
+
+}  // namespace
+}  // namespace rt
+
+// Same result as rt_radix_sort_pairs, but no device allocation: the scratch is
+// the fixed array above, so n is limited to 262,144 pairs.  Stream-ordered,
+// returns without synchronising.  The first call on a device looks up the
+// array's device address; make that first call before any stream capture.
+// All calls share the one array: calls whose work can overlap on the GPU (on
+// different streams, or from several host threads) race on it.
+extern "C" rt_status rt_radix_sort_pairs_noalloc(void* keys, unsigned int* vals, unsigned int n,
+                                                 unsigned int key_bits, void* stream) {
+    using namespace rt;
+    return guarded([&] {
+        RT_REQUIRE(keys != nullptr && vals != nullptr, "keys/vals are NULL");
+        RT_REQUIRE(key_bits >= 1 && key_bits <= 64, "key_bits must be 1..64");
+        if (n > kNoAllocMaxPairs)
+            throw Error(RT_ERR_INVALID_ARG, "rt_radix_sort_pairs_noalloc: n = " + std::to_string(n) +
+                                                " exceeds the fixed scratch limit of " +
+                                                std::to_string(kNoAllocMaxPairs) + " pairs");
+        unsigned char* scratch = noalloc_scratch();
+        cudaStream_t s = as_stream(stream);
+        if (key_bits <= 32)
+            radix_sort_pairs_fixed<uint32_t>(static_cast<uint32_t*>(keys), vals, n, int(key_bits), scratch, s);
+        else
+            radix_sort_pairs_fixed<unsigned long long>(static_cast<unsigned long long*>(keys), vals, n,
+                                                       int(key_bits), scratch, s);
+    });
+}
