@@ -74,13 +74,14 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic():
-    """Per-launch DRAM bytes of k_extend from the committed ncu summary, if any."""
+def profile_dram_bytes_per_ray():
+    """DRAM bytes per ray of k_extend from the committed ncu summary (one
+    capture of full-wave launches), or None."""
     path = os.path.join(ROOT, "profiles", "k_extend_c1.txt")
     if not os.path.exists(path):
         return None
     with open(path) as f:
-        m = re.search(r"traffic_bytes_per_launch_full:\s*([0-9.eE+]+)", f.read())
+        m = re.search(r"^dram_bytes_per_ray:\s*([0-9.eE+]+)", f.read(), re.M)
     return float(m.group(1)) if m else None
 
 
@@ -309,10 +310,13 @@ def main():
     per_launch_ms = ext_ms / max(1, ext_launches)
     rays_per_launch = rays / max(1, ext_launches)
     achieved = bytes_per_ray * rays_per_launch / (per_launch_ms * 1e-3) / 1e9 if per_launch_ms > 0 else None
-    traffic_full = profile_traffic()
+    dram_per_ray = profile_dram_bytes_per_ray()
+    traffic = dram_per_ray * rays_per_launch if dram_per_ray else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": (achieved / peak) if achieved else None,
-                "traffic": traffic_full,
+                "traffic": traffic,
+                "traffic_note": "ncu dram bytes of full-wave launches (profiles/k_extend_c1.txt), "
+                                "per ray, times the rays of a mean launch",
                 "kernel": "k_extend (LBVH traversal + ray/triangle tests)",
                 "peak_source": f"{peak_src} hbm_gbs",
                 "bytes_per_ray": bytes_per_ray, "nodes_per_ray": nodes_per_ray, "prims_per_ray": prims_per_ray,
