@@ -55,6 +55,7 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample time")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     p.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
+    p.add_argument("--batch-scenes", type=int, default=256, help="scenes of the batched leg (0: skip it)")
     return p.parse_args()
 
 
@@ -177,6 +178,98 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def batch_specs(n, seed):
+    """The batched workload: n random final-scene variants (counter-RNG
+    recipe), half-extent U{2..11}, tessellation level U{2..6}, width
+    U{128..1024} at 16:9 or 1:1, spp U{1..64}, depth 16."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for i in range(n):
+        half = int(rng.integers(2, 12))
+        level = int(rng.integers(2, 7))
+        w = int(rng.integers(128, 1025))
+        h = w if rng.random() < 0.5 else max(1, (w * 9 + 8) // 16)
+        spp = int(rng.integers(1, 65))
+        specs.append(dict(half=half, level=level, w=w, h=h, spp=spp, depth=16, scene_seed=1000 + i,
+                          seed=7000 + i))
+    return specs
+
+
+def batched_leg(R, torch, sptr, stream, nscenes, steps):
+    """Many scenes in one launch against one launch per scene (same scenes,
+    same outputs); returns timings, rays and an equality check."""
+    lib = R.lib()
+    specs = batch_specs(nscenes, 2024)
+    scenes, frames, bufs = [], [], []
+    for sp in specs:
+        sc = R.Scene()
+        sc.load_rtow(R.RT_RECIPE_COUNTER, sp["scene_seed"], sp["half"], sp["level"])
+        scenes.append(sc)
+        n = sp["w"] * sp["h"]
+        raw = torch.empty(n * 3, dtype=torch.float32, device="cuda")
+        rpp = torch.empty(n, dtype=torch.int32, device="cuda")
+        bufs.append((raw, rpp))
+        frames.append(R.Frame(ctypes.c_void_p(raw.data_ptr()), ctypes.c_void_p(rpp.data_ptr()), None, None))
+    cams = [R.rtow_camera(sp["w"], sp["h"]) for sp in specs]
+    params = [R.launch_params(sp["w"], sp["h"], sp["spp"], sp["depth"], sp["seed"], 0) for sp in specs]
+    batch = R.Batch()
+    for sc, cam, pa, fr in zip(scenes, cams, params, frames):
+        batch.add(sc, cam, pa, fr)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    batch.build(60, stream=sptr)
+    batch_build_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for sc in scenes:
+        sc.build(60, stream=sptr)
+    serial_build_s = time.perf_counter() - t0
+    binfo = batch.info()
+
+    def time_it(fn):
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        r = fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1), r
+
+    batch.launch(stream=sptr)   # warm-up
+    b_ms, b_rays = [], 0
+    for _ in range(steps):
+        ms, st = time_it(lambda: batch.launch(stream=sptr))
+        b_ms.append(ms)
+        b_rays = int(st.rays)
+    keep = [(raw.clone(), rpp.clone()) for raw, rpp in bufs[:8]]
+
+    def serial():
+        rays = 0
+        for sc, cam, pa, fr in zip(scenes, cams, params, frames):
+            st = R.LaunchStats()
+            R.check(lib.rt_launch_ex(sc.h, ctypes.byref(cam), ctypes.byref(pa), ctypes.byref(fr), sptr,
+                                     ctypes.byref(st)))
+            rays += int(st.rays)
+        return rays
+
+    serial()   # warm-up
+    s_ms, s_rays = [], 0
+    for _ in range(steps):
+        ms, s_rays = time_it(serial)
+        s_ms.append(ms)
+    equal = all(torch.equal(a, raw) and torch.equal(b, rpp) for (a, b), (raw, rpp) in zip(keep, bufs[:8]))
+    bm, sm = float(np.median(b_ms)), float(np.median(s_ms))
+    return {"scenes": nscenes, "triangles": binfo["n_prims"],
+            "paths": int(sum(sp["w"] * sp["h"] * sp["spp"] for sp in specs)),
+            "rays": b_rays, "batched_ms": bm, "serial_ms": sm, "speedup": sm / bm,
+            "batched_mrays_s": b_rays / (bm * 1e-3) / 1e6, "serial_mrays_s": s_rays / (sm * 1e-3) / 1e6,
+            "images_equal_first8": bool(equal and b_rays == s_rays),
+            "build_batched_s": batch_build_s, "build_serial_s": serial_build_s,
+            "device_gib": binfo["device_bytes"] / 2**30,
+            "workload": "256 random final-scene variants: half-extent U{2..11}, level U{2..6}, "
+                        "width U{128..1024} at 16:9 or 1:1, spp U{1..64}, depth 16"}
+
+
 def main():
     args = parse()
     world, rank, local = dist_setup()
@@ -208,18 +301,15 @@ def main():
     rpp = torch.empty(npix, dtype=torch.int32, device="cuda")
     frame = R.Frame(ctypes.c_void_p(raw.data_ptr()), ctypes.c_void_p(rpp.data_ptr()), None, None)
 
-    def step(seed, flags):
-        params = R.launch_params(W, H, args.spp, args.depth, seed, flags)
+    def step(seed, flags, spp=None):
+        params = R.launch_params(W, H, spp or args.spp, args.depth, seed, flags)
         st = R.LaunchStats()
         R.check(lib.rt_launch_ex(sc.h, ctypes.byref(cam), ctypes.byref(params), ctypes.byref(frame), sptr,
                                  ctypes.byref(st)))
         return st
 
     # algorithmic bytes per ray from a counting pass (untimed, reduced spp)
-    cnt_params = R.launch_params(W, H, max(1, min(args.spp, 16)), args.depth, 99, R.RT_FLAG_COUNT_VISITS)
-    cst = R.LaunchStats()
-    R.check(lib.rt_launch_ex(sc.h, ctypes.byref(cam), ctypes.byref(cnt_params), ctypes.byref(frame), sptr,
-                             ctypes.byref(cst)))
+    cst = step(99, R.RT_FLAG_COUNT_VISITS, spp=max(1, min(args.spp, 16)))
     nodes_per_ray = cst.node_visits / max(1, cst.rays)
     prims_per_ray = cst.prim_tests / max(1, cst.rays)
     bytes_per_ray = 64.0 * nodes_per_ray + 48.0 * prims_per_ray + 48.0
@@ -236,18 +326,18 @@ def main():
     ev1 = torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
     rays = 0
-    ext_ms = 0.0
-    ext_launches = 0
     launches = 0
     for k in range(args.steps):
-        st = step(4711 + k, R.RT_FLAG_STAGE_TIMING)
+        st = step(4711 + k, 0)
         rays += st.rays
-        ext_ms += st.extend_ms
-        ext_launches += st.extend_launches
         launches += st.kernel_launches
     ev1.record(stream)
     torch.cuda.synchronize()
     elapsed_ms = ev0.elapsed_time(ev1)
+    # traversal kernel times: one more frame with a CUDA event pair around
+    # every k_extend / k_shade launch (host-driven wave loop)
+    rst = step(4711 + args.steps, R.RT_FLAG_STAGE_TIMING)
+    torch.cuda.synchronize()
     clk = clocks.stop()
     if dist:
         t = torch.tensor([elapsed_ms], device="cuda")
@@ -263,8 +353,6 @@ def main():
     # ---- end to end through the C ABI with host buffers
     e2e = None
     if not args.no_e2e:
-        from rtxplay_gb300 import _build  # noqa: F401
-        mesh_host = None
         m = R.Scene()
         mid = m.add_sphere_mesh(1.0, args.level)
         mesh_host = m.get_mesh(mid)
@@ -287,7 +375,7 @@ def main():
                 s2.add_thing(R.optics(int(t_), a_, float(f_), float(i_)), mid, T)
             s2.build(args.morton_bits)
             params = R.launch_params(W, H, args.spp, args.depth, 4711 + k, 0)
-            st = L.ignite(s2, cam, params)
+            L.ignite(s2, cam, params)
             R.check(lib.rt_launcher_download(L.h, None, ctypes.c_void_p(rpp_host.ctypes.data), None, None,
                                              ctypes.c_void_p(img_host.ctypes.data), None))
             e2e_rays += int(rpp_host.sum(dtype=np.uint64))
@@ -302,40 +390,51 @@ def main():
             dist.all_reduce(t[1:2])
             e2e["value"] = float(t[1].item()) / float(t[0].item()) / 1e6
 
+    batched = None
+    if rank == 0 and world == 1 and args.batch_scenes > 0:
+        batched = batched_leg(R, torch, sptr, stream, args.batch_scenes, max(1, min(args.steps, 3)))
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_oracle_run(args, args.cpu_seconds)
 
     peak, peak_src = load_peaks()
-    per_launch_ms = ext_ms / max(1, ext_launches)
-    rays_per_launch = rays / max(1, ext_launches)
+    ext_launches = max(1, rst.extend_launches)
+    per_launch_ms = rst.extend_ms / ext_launches
+    rays_per_launch = rst.rays / ext_launches
     achieved = bytes_per_ray * rays_per_launch / (per_launch_ms * 1e-3) / 1e9 if per_launch_ms > 0 else None
     dram_per_ray = profile_dram_bytes_per_ray()
     traffic = dram_per_ray * rays_per_launch if dram_per_ray else None
+    frame_ms = elapsed_ms / args.steps
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": (achieved / peak) if achieved else None,
                 "traffic": traffic,
                 "traffic_note": "ncu dram bytes of full-wave launches (profiles/k_extend_c1.txt), "
                                 "per ray, times the rays of a mean launch",
                 "kernel": "k_extend (LBVH traversal + ray/triangle tests)",
+                "timing": "CUDA events around every k_extend launch of one frame of the same workload "
+                          "rendered right after the timed steps",
                 "peak_source": f"{peak_src} hbm_gbs",
                 "bytes_per_ray": bytes_per_ray, "nodes_per_ray": nodes_per_ray, "prims_per_ray": prims_per_ray,
-                "extend_ms_per_launch": per_launch_ms, "extend_share": ext_ms / max(elapsed_ms, 1e-9),
-                "rays_per_launch": rays_per_launch}
+                "extend_ms_per_launch": per_launch_ms, "extend_launches": int(rst.extend_launches),
+                "shade_ms_per_frame": rst.shade_ms, "extend_ms_per_frame": rst.extend_ms,
+                "extend_share": rst.extend_ms / max(frame_ms, 1e-9), "rays_per_launch": rays_per_launch}
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
+                "warmup": args.warmup, "ms_per_step": frame_ms, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (reference scene recipe, glibc rand seed 1)",
                 "config": {"workload": f"rtow final scene, level-{args.level} tessellation "
                                        f"({info.n_prims} triangles), {W}x{H}, {args.spp} spp, depth {args.depth}",
                            "parallelism": f"replicas x{world}", "morton_bits": info.morton_bits,
+                           "wave_loop": "CUDA graph (conditional WHILE node)" if os.environ.get("RTX_GRAPH", "1") != "0"
+                           else "host-driven",
                            "l2": "inputs larger than L2 (LBVH + triangles "
                                  f"{info.device_bytes / 2**30:.2f} GiB on device)",
                            "build_ms": info.build_ms},
                 "rays_per_step": total_rays / args.steps / world,
                 "gpu_launches": launches,
-                "clocks": clk, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e}
+                "clocks": clk, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "batched": batched}
         print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()

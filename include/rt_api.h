@@ -215,6 +215,25 @@ rt_status rt_first_hit(rt_scene scene, const rt_camera* cam, const rt_launch_par
 rt_status rt_pick(rt_scene scene, const rt_camera* cam, const rt_launch_params* params,
                   unsigned int x, unsigned int y, unsigned int* thing_id, void* stream);
 
+/* ----------------------------------------------------------------- batch */
+/* Many independent scenes in one launch (no counterpart in the reference,
+ * whose Launcher renders one scene per optixLaunch): every scene keeps its
+ * own camera, size, spp, depth, seed and output frame; rt_batch_build builds
+ * all their LBVHs in one segmented pass (one Morton sort by (scene, code), a
+ * Karras hierarchy per segment, one refit); rt_batch_launch renders all of
+ * them with one wavefront whose wave loop runs as a CUDA graph.  Each scene's
+ * image equals the one rt_launch renders for it alone.  The scenes must stay
+ * alive and unchanged until the batch is destroyed or rebuilt. */
+typedef struct rt_batch_s* rt_batch;
+rt_status rt_batch_create(rt_batch* out);
+rt_status rt_batch_destroy(rt_batch b);
+rt_status rt_batch_add(rt_batch b, rt_scene scene, const rt_camera* cam,
+                       const rt_launch_params* params, const rt_frame* frame, unsigned int* index);
+rt_status rt_batch_build(rt_batch b, unsigned int morton_bits, void* stream);
+rt_status rt_batch_launch(rt_batch b, void* stream, rt_launch_stats* stats);
+rt_status rt_batch_info(rt_batch b, unsigned int* n_scenes, unsigned int* n_prims, float* build_ms,
+                        unsigned long long* device_bytes);
+
 /* ---------------------------------------------------------- post-process */
 /* pp_sRGB / pp_none (optx/postproc.cu:49-61; declared at optx/rtwo.cxx:53-54):
  * float3 -> uchar4 through the sRGB curve, or x255 truncation.  Same

@@ -90,6 +90,18 @@ def lib():
                                  _f32p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                  ctypes.c_int]
         L.orc_render.restype = ctypes.c_uint64
+        L.orc_world_nthings.argtypes = [ctypes.c_void_p]
+        L.orc_world_nthings.restype = ctypes.c_uint
+        L.orc_world_set_optics.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _f32p, ctypes.c_float,
+                                           ctypes.c_float]
+        L.orc_world_set_optics.restype = ctypes.c_int
+        L.orc_world_get_optics.argtypes = [ctypes.c_void_p, _i32p, _f32p, _f32p, _f32p]
+        L.orc_adjoint.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Camera), ctypes.c_uint, ctypes.c_uint,
+                                  ctypes.c_uint, ctypes.c_uint, ctypes.c_uint32, ctypes.c_uint32, _f32p, _f32p,
+                                  _f32p, _f32p, _f64p, _f64p, _f64p, ctypes.c_int]
+        L.orc_fuzz_path_check.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Camera), ctypes.c_uint, ctypes.c_uint,
+                                          ctypes.c_uint, ctypes.c_uint, ctypes.c_uint32, ctypes.c_int,
+                                          ctypes.c_float, _f32p, _f32p, _f64p]
         for name in ("orc_pp_srgb", "orc_pp_none", "orc_pp_gamma2"):
             getattr(L, name).argtypes = [_f32p, _u8p, ctypes.c_int, ctypes.c_int]
         _lib = L
@@ -256,6 +268,43 @@ class World:
         if fp64:
             out["t64"] = t64
         return out
+
+    @property
+    def nthings(self):
+        return lib().orc_world_nthings(self._w)
+
+    def optics(self):
+        n = self.nthings
+        t = np.zeros(n, np.int32)
+        a = np.zeros((n, 3), np.float32)
+        f = np.zeros(n, np.float32)
+        ix = np.zeros(n, np.float32)
+        lib().orc_world_get_optics(self._w, t, a, f, ix)
+        return dict(types=t, albedos=a, fuzz=f, index=ix)
+
+    def fuzz_path_check(self, cam, w, h, spp, depth, seed, thing, step=1e-3, ambient=(0.5, 0.7, 1.0),
+                        white=(1.0, 1.0, 1.0)):
+        out = np.zeros(7, np.float64)
+        lib().orc_fuzz_path_check(self._w, ctypes.byref(cam), w, h, spp, depth, seed, thing, step,
+                                  np.asarray(ambient, np.float32), np.asarray(white, np.float32), out)
+        return dict(compared=int(out[0]), skipped=int(out[1]), max_rel=out[2], sum_abs_fd=out[3],
+                    outliers=int(out[4]), sum_adj=out[5], sum_fd=out[6])
+
+    def set_optics(self, thing, otype, albedo, fuzz, index):
+        assert lib().orc_world_set_optics(self._w, thing, otype, np.asarray(albedo, np.float32), fuzz,
+                                          index) == 0
+
+    def adjoint(self, cam, w, h, spp, depth, seed, image, grad_image, scene=0, ambient=(0.5, 0.7, 1.0),
+                white=(1.0, 1.0, 1.0), nthreads=0):
+        n = self.nthings
+        ga = np.zeros((n, 3), np.float64)
+        gf = np.zeros(n, np.float64)
+        gs = np.zeros(6, np.float64)
+        lib().orc_adjoint(self._w, ctypes.byref(cam), w, h, spp, depth, seed, scene,
+                          np.asarray(ambient, np.float32), np.asarray(white, np.float32),
+                          np.ascontiguousarray(image, np.float32).reshape(-1),
+                          np.ascontiguousarray(grad_image, np.float32).reshape(-1), ga, gf, gs, nthreads)
+        return dict(albedo=ga, fuzz=gf, sky=gs)
 
     def render(self, cam, w, h, spp, depth, seed, scene=0, ambient=(0.5, 0.7, 1.0),
                white=(1.0, 1.0, 1.0), pixels=None, guides=True, nthreads=0):

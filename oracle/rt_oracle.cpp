@@ -11,7 +11,8 @@
 // run here, so closest-hit and image parity are defined by this restatement.
 //
 // Arithmetic: IEEE binary32, no FMA contraction (-ffp-contract=off), the same
-// operation order as the CUDA kernels.  Pow-5 in Schlick's term is written as
+// operation order as the CUDA kernels; per-pixel sample sums in 64-bit fixed
+// point (see fx_add).  Pow-5 in Schlick's term is written as
 // products (((x*x)*(x*x))*x) on both sides so CPU and GPU agree bit for bit.
 
 #include "rt_oracle.h"
@@ -620,6 +621,25 @@ struct PathOut {
     uint32_t rays;
 };
 
+// One scattering vertex of a recorded path (for the adjoint): the incoming
+// ray, the hit and the random choices that fix the outgoing direction.
+struct Vtx {
+    int prim, thing, type;
+    F3 o, d;        // incoming ray
+    float t;        // hit distance along d
+    F3 p, N;        // hit point, normal facing the incoming ray
+    bool front;
+    F3 v;           // diffuse: unit random vector; metal: in-sphere vector
+    int branch;     // diffuse: 1 = near-zero fallback; glass: 0 reflect, 1 refract
+    float ratio;    // glass: index ratio
+};
+
+struct PathRec {
+    std::vector<Vtx> vtx;
+    bool miss = false;   // ended by a miss (sky), not absorbed / depth limit
+    F3 d_last{0, 0, 0};  // direction of the missing ray
+};
+
 inline F3 sky(F3 d, F3 ambient, F3 white) {
     // optx/camera_i.cu:133-139
     const F3 unit = unitV(d);
@@ -629,7 +649,7 @@ inline F3 sky(F3 d, F3 ambient, F3 white) {
 
 PathOut trace_path(const orc_world& w, const Cam& cam, unsigned x, unsigned y, unsigned W,
                    unsigned H, unsigned depth, uint32_t seed, uint32_t scene, uint32_t sample,
-                   F3 ambient, F3 white) {
+                   F3 ambient, F3 white, PathRec* rec = nullptr) {
     const uint32_t pix = W * y + x;
     PathOut out{mk(1.f, 1.f, 1.f), mk(0, 0, 0), mk(0, 0, 0), 0};
     F3 o, d;
@@ -637,11 +657,13 @@ PathOut trace_path(const orc_world& w, const Cam& cam, unsigned x, unsigned y, u
         Stream s(seed, scene, pix, sample, 0);
         camera_ray(cam, x, y, W, H, s, o, d);
     }
+    if (rec) { rec->vtx.clear(); rec->miss = false; }
     for (uint32_t k = 0;; ++k) {
         out.rays++;
         const Hit h = closest_bvh(w, o, d);
         if (h.prim < 0) {
             out.color = mulv(out.color, sky(d, ambient, white));
+            if (rec) { rec->miss = true; rec->d_last = d; }
             break;
         }
         if (k + 1 >= depth) {  // black at the depth limit (optx/optics_r.cu:34-42)
@@ -651,10 +673,13 @@ PathOut trace_path(const orc_world& w, const Cam& cam, unsigned x, unsigned y, u
         const ShadeIn g = hit_geometry(w, h, o, d);
         const Thing& th = w.things[w.prims[h.prim].thing];
         Stream s(seed, scene, pix, sample, k + 1);
+        Vtx vx{h.prim, w.prims[h.prim].thing, th.type, o, d, h.t, g.p, g.N, g.front, mk(0, 0, 0), 0, 1.f};
         if (th.type == OPT_DIFFUSE) {
             // optx/optics_i.cu:87-96 with the near-zero fallback of optics.h:17-18
-            F3 dir = add(g.N, rndVon1sphere(s));
-            if (near0(dir)) dir = g.N;
+            const F3 u = rndVon1sphere(s);
+            F3 dir = add(g.N, u);
+            vx.v = u;
+            if (near0(dir)) { dir = g.N; vx.branch = 1; }
             out.color = mulv(out.color, th.albedo);
             if (isnull(out.normal)) out.normal = g.N;
             if (isnull(out.albedo)) out.albedo = th.albedo;
@@ -663,7 +688,9 @@ PathOut trace_path(const orc_world& w, const Cam& cam, unsigned x, unsigned y, u
             // optx/optics_i.cu:168-190
             const F3 d1V = unitV(d);
             const F3 refl = sub(d1V, mul(2.f * dot(d1V, g.N), g.N));
-            const F3 dir = add(refl, mul(th.fuzz, rndVin1sphere(s)));
+            const F3 v = rndVin1sphere(s);
+            const F3 dir = add(refl, mul(th.fuzz, v));
+            vx.v = v;
             if (isnull(out.normal)) out.normal = g.N;
             if (isnull(out.albedo)) out.albedo = th.albedo;
             if (dot(dir, g.N) > 0.f) {
@@ -671,6 +698,7 @@ PathOut trace_path(const orc_world& w, const Cam& cam, unsigned x, unsigned y, u
                 o = g.p; d = dir;
             } else {
                 out.color = mk(0.f, 0.f, 0.f);
+                if (rec) rec->vtx.push_back(vx);
                 break;
             }
         } else {
@@ -686,19 +714,110 @@ PathOut trace_path(const orc_world& w, const Cam& cam, unsigned x, unsigned y, u
             const float pow5 = ((om * om) * (om * om)) * om;
             const float schlick = r0 + (1.f - r0) * pow5;
             F3 dir;
+            vx.ratio = ratio;
             if (cannot || schlick > s.next()) {
                 dir = sub(d1V, mul(2.f * dot(d1V, g.N), g.N));
+                vx.branch = 0;
             } else {
                 const float theta = fminf(dot(neg(d1V), g.N), 1.f);
                 const F3 perpen = mul(ratio, add(d1V, mul(theta, g.N)));
                 const F3 parall = mul(-sqrtf(fabsf(1.f - dot(perpen, perpen))), g.N);
                 dir = add(perpen, parall);
+                vx.branch = 1;
             }
             o = g.p; d = dir;
         }
+        if (rec) rec->vtx.push_back(vx);
     }
     return out;
 }
+
+// ------------------------------------------------------------- adjoint --
+// Double-precision tangent of the path below a perturbation (do, dd) of the
+// ray leaving vertex k0: the same hits and branches as the primal path
+// (visibility is held fixed), differentiated vertex by vertex.
+struct D3 {
+    double x, y, z;
+};
+inline D3 dd3(F3 a) { return D3{a.x, a.y, a.z}; }
+inline D3 operator+(D3 a, D3 b) { return D3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline D3 operator-(D3 a, D3 b) { return D3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline D3 operator*(double s, D3 a) { return D3{s * a.x, s * a.y, s * a.z}; }
+inline double ddot(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline double dlen(D3 a) { return std::sqrt(ddot(a, a)); }
+
+// derivative of unit(d) along dd
+inline D3 dunit(D3 d, D3 dd) {
+    const double l = dlen(d);
+    const D3 u = (1.0 / l) * d;
+    return (1.0 / l) * (dd - ddot(u, dd) * u);
+}
+
+// Propagates (dO, dD) of the ray entering vertex m through vertices m..end;
+// returns d(sky colour)/d(perturbation) of the final miss, per channel.
+D3 tangent_to_sky(const orc_world& w, const PathRec& rec, size_t m, D3 dO, D3 dD, F3 ambient, F3 white) {
+    for (size_t k = m; k < rec.vtx.size(); ++k) {
+        const Vtx& v = rec.vtx[k];
+        const Prim& pr = w.prims[v.prim];
+        const D3 d = dd3(v.d), N = dd3(v.N);
+        const double t = v.t;
+        // hit point on the (fixed) surface: dp = q - d (n.q)/(n.d), q = dO + t dD
+        const D3 q = dO + t * dD;
+        D3 n;
+        if (pr.kind == 0) n = N; else n = dd3(v.p) - dd3(pr.a);
+        const double nd = ddot(n, d);
+        const D3 dp = nd != 0.0 ? q - (ddot(n, q) / nd) * d : q;
+        D3 dN{0, 0, 0};
+        if (pr.kind == 1) {   // sphere: N = +-(p - c)/r
+            const double sgn = v.front ? 1.0 : -1.0;
+            dN = (sgn / double(pr.r)) * dp;
+        }
+        D3 dOut;
+        if (v.type == OPT_DIFFUSE) {
+            dOut = dN;   // d' = N + u (or N)
+        } else {
+            const D3 d1 = (1.0 / dlen(d)) * d;
+            const D3 dd1 = dunit(d, dD);
+            const bool refl = v.type == OPT_REFLECT || v.branch == 0;
+            if (refl) {
+                const double c = ddot(d1, N);
+                const double dc = ddot(dd1, N) + ddot(d1, dN);
+                dOut = dd1 - 2.0 * ((dc * N) + c * dN);
+            } else {
+                const double ratio = v.ratio;
+                const double raw = -ddot(d1, N);
+                const double cth = raw < 1.0 ? raw : 1.0;
+                const double dcth = raw < 1.0 ? -(ddot(dd1, N) + ddot(d1, dN)) : 0.0;
+                const D3 perp = ratio * (d1 + cth * N);
+                const D3 dperp = ratio * (dd1 + (dcth * N) + cth * dN);
+                const double qq = ddot(perp, perp);
+                const double sroot = std::sqrt(std::fabs(1.0 - qq));
+                const double dq = 2.0 * ddot(perp, dperp);
+                const double ds = sroot > 0.0 ? ((1.0 - qq) >= 0.0 ? -dq : dq) / (2.0 * sroot) : 0.0;
+                dOut = dperp - ((ds * N) + sroot * dN);
+            }
+        }
+        dO = dp;
+        dD = dOut;
+    }
+    // miss: sky = (1 - s) white + s ambient, s = .5 (unit(d).y + 1)
+    const D3 du = dunit(dd3(rec.d_last), dD);
+    const double ds = 0.5 * du.y;
+    return D3{ds * (double(ambient.x) - white.x), ds * (double(ambient.y) - white.y),
+              ds * (double(ambient.z) - white.z)};
+}
+
+// 64-bit fixed-point sample sums: q(x) = round-half-even(x * 2^32) (exact in
+// binary32 up to the final rounding); mean = (double)sum * 2^-32 / spp rounded
+// to binary32.
+inline int64_t fx_q(float x) { return int64_t(llrintf(x * 4294967296.0f)); }
+inline void fx_add(int64_t s[3], F3 v) {
+    s[0] += fx_q(v.x);
+    s[1] += fx_q(v.y);
+    s[2] += fx_q(v.z);
+}
+inline float fx_div(int64_t s, unsigned spp) { return float(double(s) * 0x1p-32 / double(spp)); }
+inline F3 fx_mean(const int64_t s[3], unsigned spp) { return mk(fx_div(s[0], spp), fx_div(s[1], spp), fx_div(s[2], spp)); }
 
 Cam to_cam(const orc_camera* c) {
     Cam k;
@@ -1083,29 +1202,196 @@ uint64_t orc_render(const orc_world* wd, const orc_camera* cam, unsigned w, unsi
         for (long q = 0; q < count; ++q) {
             const uint32_t pix = pixels ? pixels[q] : uint32_t(q);
             const unsigned x = pix % w, y = pix / w;
-            F3 color = mk(0, 0, 0), normal = mk(0, 0, 0), albedo = mk(0, 0, 0);
+            // Per-pixel sums in 64-bit fixed point (2^-32 units): every sample
+            // adds round(x * 2^32), an integer sum that is exact and does not
+            // depend on the order in which samples finish.
+            int64_t sc[3] = {0, 0, 0}, sn[3] = {0, 0, 0}, sa[3] = {0, 0, 0};
             uint32_t rays = 0;
             for (unsigned s = 0; s < spp; ++s) {
                 const PathOut po = trace_path(*wd, c, x, y, w, h, depth, seed, scene, s, amb, wht);
-                color = add(color, po.color);   // optx/camera_i.cu:95
-                normal = add(normal, po.normal);
-                albedo = add(albedo, po.albedo);
+                fx_add(sc, po.color);   // optx/camera_i.cu:95
+                fx_add(sn, po.normal);
+                fx_add(sa, po.albedo);
                 rays += po.rays;
             }
-            // optx/camera_i.cu:105-113: mean = 1/spp * sum, clamped to [0,1]
-            const float inv = 1.f / float(spp);
-            F3 mean = mul(inv, color);
+            // optx/camera_i.cu:105-113: mean over spp, clamped to [0,1]
             auto cl = [](float x) { return 0.f > x ? 0.f : (x > 1.f ? 1.f : x); };
-            mean = mk(cl(mean.x), cl(mean.y), cl(mean.z));
-            st3(rawRGB + 3 * q, mean);
+            const F3 mean = fx_mean(sc, spp);
+            st3(rawRGB + 3 * q, mk(cl(mean.x), cl(mean.y), cl(mean.z)));
             if (rpp) rpp[q] = rays;
-            if (normals) st3(normals + 3 * q, mul(inv, normal));
-            if (albedos) st3(albedos + 3 * q, mul(inv, albedo));
+            if (normals) st3(normals + 3 * q, fx_mean(sn, spp));
+            if (albedos) st3(albedos + 3 * q, fx_mean(sa, spp));
             mine += rays;
         }
         total += mine;
     }
     return total.load();
+}
+
+unsigned orc_world_nthings(const orc_world* w) { return unsigned(w->things.size()); }
+
+// Per-path check of the fuzz tangent: for every path of the image that
+// reflects off `thing`, d(colour)/d(fuzz) from tangent_to_sky against a
+// central difference of the same path (same random numbers) -- counted only
+// where both perturbed paths keep the hit sequence and branches (no
+// visibility change).  out[0] = paths compared, out[1] = paths skipped,
+// out[2] = max |adj - fd| / max(|fd|, floor), out[3] = sum |fd|, out[4] =
+// paths with a relative error above 5%, out[5] / out[6] = sum of adj / fd
+// over the compared paths (all channels).
+void orc_fuzz_path_check(orc_world* wd, const orc_camera* cam, unsigned w, unsigned h, unsigned spp,
+                         unsigned depth, uint32_t seed, int thing, float step, const float ambient[3],
+                         const float white[3], double* out) {
+    const Cam c = to_cam(cam);
+    const F3 amb = ld3(ambient), wht = ld3(white);
+    Thing& th = wd->things[thing];
+    const float f0 = th.fuzz;
+    double compared = 0, skipped = 0, maxrel = 0, sumfd = 0, outliers = 0, sadj = 0, sfd = 0;
+    PathRec r0, rp, rm;
+    auto same = [](const PathRec& a, const PathRec& b) {
+        if (a.miss != b.miss || a.vtx.size() != b.vtx.size()) return false;
+        for (size_t k = 0; k < a.vtx.size(); ++k)
+            if (a.vtx[k].prim != b.vtx[k].prim || a.vtx[k].branch != b.vtx[k].branch) return false;
+        return true;
+    };
+    for (unsigned pix = 0; pix < w * h; ++pix) {
+        for (unsigned smp = 0; smp < spp; ++smp) {
+            th.fuzz = f0;
+            const PathOut p0 = trace_path(*wd, c, pix % w, pix / w, w, h, depth, seed, 0, smp, amb, wht, &r0);
+            if (!r0.miss) continue;
+            bool touches = false;
+            for (const Vtx& v : r0.vtx) touches |= (v.thing == thing && v.type == OPT_REFLECT);
+            if (!touches) continue;
+            th.fuzz = f0 + step;
+            const PathOut pp = trace_path(*wd, c, pix % w, pix / w, w, h, depth, seed, 0, smp, amb, wht, &rp);
+            th.fuzz = f0 - step;
+            const PathOut pm = trace_path(*wd, c, pix % w, pix / w, w, h, depth, seed, 0, smp, amb, wht, &rm);
+            th.fuzz = f0;
+            if (!same(r0, rp) || !same(r0, rm)) { skipped += 1; continue; }
+            // tangent: sum over the events on `thing`
+            D3 thr{1, 1, 1};
+            for (const Vtx& v : r0.vtx)
+                if (v.type != OPT_REFRACT) {
+                    const F3 a = wd->things[v.thing].albedo;
+                    thr = D3{thr.x * a.x, thr.y * a.y, thr.z * a.z};
+                }
+            D3 adj{0, 0, 0};
+            for (size_t k = 0; k < r0.vtx.size(); ++k) {
+                const Vtx& v = r0.vtx[k];
+                if (v.thing != thing || v.type != OPT_REFLECT) continue;
+                const D3 ds = tangent_to_sky(*wd, r0, k + 1, D3{0, 0, 0}, dd3(v.v), amb, wht);
+                adj = adj + D3{thr.x * ds.x, thr.y * ds.y, thr.z * ds.z};
+            }
+            const D3 fd = (1.0 / (2.0 * step)) * (dd3(pp.color) - dd3(pm.color));
+            const double den = std::max(1e-3, std::max(std::fabs(fd.x), std::max(std::fabs(fd.y), std::fabs(fd.z))));
+            const double err = std::max(std::fabs(adj.x - fd.x), std::max(std::fabs(adj.y - fd.y), std::fabs(adj.z - fd.z)));
+            maxrel = std::max(maxrel, err / den);
+            if (err / den > 0.05) outliers += 1;
+            sumfd += std::fabs(fd.x) + std::fabs(fd.y) + std::fabs(fd.z);
+            sadj += adj.x + adj.y + adj.z;
+            sfd += fd.x + fd.y + fd.z;
+            compared += 1;
+            (void)p0;
+        }
+    }
+    out[0] = compared; out[1] = skipped; out[2] = maxrel; out[3] = sumfd;
+    out[4] = outliers; out[5] = sadj; out[6] = sfd;
+}
+
+int orc_world_set_optics(orc_world* w, int thing, int type, const float albedo[3], float fuzz, float index) {
+    if (thing < 0 || thing >= int(w->things.size())) return -1;
+    Thing& t = w->things[thing];
+    t.type = type; t.albedo = ld3(albedo); t.fuzz = fuzz; t.index = index;
+    return 0;   // optics do not change the geometry: no rebuild needed
+}
+
+void orc_world_get_optics(const orc_world* w, int* types, float* albedos, float* fuzz, float* index) {
+    for (size_t k = 0; k < w->things.size(); ++k) {
+        const Thing& t = w->things[k];
+        types[k] = t.type;
+        st3(albedos + 3 * k, t.albedo);
+        fuzz[k] = t.fuzz;
+        index[k] = t.index;
+    }
+}
+
+// Gradients of a scalar image loss L(I) given dL/dI (grad_image, w*h*3):
+// per thing d/d albedo (3), d/d fuzz, and d/d ambient (3), d/d white (3).
+// Each path is replayed exactly as rendered; visibility is held fixed.
+void orc_adjoint(const orc_world* wd, const orc_camera* cam, unsigned w, unsigned h, unsigned spp,
+                 unsigned depth, uint32_t seed, uint32_t scene, const float ambient[3],
+                 const float white[3], const float* image, const float* grad_image,
+                 double* grad_albedo, double* grad_fuzz, double* grad_sky, int nthreads) {
+    const Cam c = to_cam(cam);
+    const F3 amb = ld3(ambient), wht = ld3(white);
+    const size_t nt = wd->things.size();
+    std::fill(grad_albedo, grad_albedo + 3 * nt, 0.0);
+    std::fill(grad_fuzz, grad_fuzz + nt, 0.0);
+    std::fill(grad_sky, grad_sky + 6, 0.0);
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+#pragma omp parallel
+    {
+        std::vector<double> ga(3 * nt, 0.0), gf(nt, 0.0), gs(6, 0.0);
+        PathRec rec;
+#pragma omp for schedule(dynamic, 16)
+        for (long pix = 0; pix < long(w) * long(h); ++pix) {
+            const unsigned x = unsigned(pix % w), y = unsigned(pix / w);
+            double g[3];
+            for (int ch = 0; ch < 3; ++ch) {
+                const float I = image[3 * pix + ch];
+                const double mask = (I > 0.f && I < 1.f) ? 1.0 : 0.0;   // clamp to [0,1]
+                g[ch] = double(grad_image[3 * pix + ch]) * mask / double(spp);
+            }
+            if (g[0] == 0.0 && g[1] == 0.0 && g[2] == 0.0) continue;
+            for (unsigned smp = 0; smp < spp; ++smp) {
+                trace_path(*wd, c, x, y, w, h, depth, seed, scene, smp, amb, wht, &rec);
+                if (!rec.miss) continue;   // absorbed or depth-limited: black, no gradient
+                const size_t ne = rec.vtx.size();
+                // albedo factors per event (glass: 1)
+                std::vector<D3> a(ne);
+                for (size_t k = 0; k < ne; ++k) {
+                    const Vtx& v = rec.vtx[k];
+                    a[k] = v.type == OPT_REFRACT ? D3{1, 1, 1} : dd3(wd->things[v.thing].albedo);
+                }
+                const D3 u = (1.0 / dlen(dd3(rec.d_last))) * dd3(rec.d_last);
+                const double sv = 0.5 * (u.y + 1.0);
+                const double skyc[3] = {(1.0 - sv) * wht.x + sv * amb.x, (1.0 - sv) * wht.y + sv * amb.y,
+                                        (1.0 - sv) * wht.z + sv * amb.z};
+                // prefix / suffix products of the albedos
+                std::vector<D3> pre(ne + 1, D3{1, 1, 1}), suf(ne + 1, D3{1, 1, 1});
+                for (size_t k = 0; k < ne; ++k)
+                    pre[k + 1] = D3{pre[k].x * a[k].x, pre[k].y * a[k].y, pre[k].z * a[k].z};
+                for (size_t k = ne; k-- > 0;)
+                    suf[k] = D3{suf[k + 1].x * a[k].x, suf[k + 1].y * a[k].y, suf[k + 1].z * a[k].z};
+                const D3 thr = pre[ne];
+                const double th3[3] = {thr.x, thr.y, thr.z};
+                for (int ch = 0; ch < 3; ++ch) {
+                    gs[ch] += g[ch] * th3[ch] * sv;            // ambient
+                    gs[3 + ch] += g[ch] * th3[ch] * (1.0 - sv); // white
+                }
+                for (size_t k = 0; k < ne; ++k) {
+                    const Vtx& v = rec.vtx[k];
+                    if (v.type == OPT_REFRACT) continue;
+                    const double o3[3] = {pre[k].x * suf[k + 1].x, pre[k].y * suf[k + 1].y,
+                                          pre[k].z * suf[k + 1].z};
+                    for (int ch = 0; ch < 3; ++ch) ga[3 * size_t(v.thing) + ch] += g[ch] * o3[ch] * skyc[ch];
+                    if (v.type == OPT_REFLECT) {
+                        const D3 ds = tangent_to_sky(*wd, rec, k + 1, D3{0, 0, 0}, dd3(v.v), amb, wht);
+                        gf[size_t(v.thing)] += g[0] * th3[0] * ds.x + g[1] * th3[1] * ds.y + g[2] * th3[2] * ds.z;
+                    }
+                }
+            }
+        }
+#pragma omp critical
+        {
+            for (size_t i = 0; i < 3 * nt; ++i) grad_albedo[i] += ga[i];
+            for (size_t i = 0; i < nt; ++i) grad_fuzz[i] += gf[i];
+            for (int i = 0; i < 6; ++i) grad_sky[i] += gs[i];
+        }
+    }
 }
 
 // optx/postproc.cu:2-16: sRGB transfer curve, then x255 truncated.

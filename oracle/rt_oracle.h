@@ -106,6 +106,26 @@ uint64_t orc_render(const orc_world* wd, const orc_camera* cam, unsigned w, unsi
                     unsigned npixels, float* rawRGB, uint32_t* rpp, float* normals,
                     float* albedos, int nthreads);
 
+/* ---- adjoint ------------------------------------------------------------ */
+unsigned orc_world_nthings(const orc_world* w);
+int orc_world_set_optics(orc_world* w, int thing, int type, const float albedo[3], float fuzz, float index);
+void orc_world_get_optics(const orc_world* w, int* types, float* albedos, float* fuzz, float* index);
+/* Per-path check of the fuzz derivative (tangent vs central difference of the
+ * same path, paths whose hit sequence changes are skipped): out[4] =
+ * compared, skipped, max relative error, sum |fd|, paths off by more than 5%,
+ * sum of the tangent derivatives, sum of the differences. */
+void orc_fuzz_path_check(orc_world* wd, const orc_camera* cam, unsigned w, unsigned h, unsigned spp,
+                         unsigned depth, uint32_t seed, int thing, float step, const float ambient[3],
+                         const float white[3], double* out);  /* out[7] */
+/* FP64 gradients of a scalar loss of the rendered image, given dL/dI
+ * (grad_image, w*h*3, with image = the clamped render): per thing
+ * grad_albedo[3*n], grad_fuzz[n]; grad_sky[6] = d/d ambient xyz, d/d white xyz.
+ * Every path is replayed as rendered, visibility held fixed. */
+void orc_adjoint(const orc_world* wd, const orc_camera* cam, unsigned w, unsigned h, unsigned spp,
+                 unsigned depth, uint32_t seed, uint32_t scene, const float ambient[3],
+                 const float white[3], const float* image, const float* grad_image,
+                 double* grad_albedo, double* grad_fuzz, double* grad_sky, int nthreads);
+
 /* ---- post-processing (optx/postproc.cu:2-47, rtow.cxx:6-21) ------------- */
 void orc_pp_srgb(const float* src, uint8_t* dst, int w, int h);
 void orc_pp_none(const float* src, uint8_t* dst, int w, int h);

@@ -123,6 +123,12 @@ SIGNATURES = {
     "rt_launcher_download": [_P, _P, _P, _P, _P, _P, _P],
     "rt_radix_sort_pairs": [_P, _P, _U, _U, _P],
     "rt_radix_sort_pairs_noalloc": [_P, _P, _U, _U, _P],
+    "rt_batch_create": [ctypes.POINTER(_P)],
+    "rt_batch_destroy": [_P],
+    "rt_batch_add": [_P, _P, ctypes.POINTER(Camera), ctypes.POINTER(LaunchParams), ctypes.POINTER(Frame), _PU],
+    "rt_batch_build": [_P, _U, _P],
+    "rt_batch_launch": [_P, _P, ctypes.POINTER(LaunchStats)],
+    "rt_batch_info": [_P, _PU, _PU, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_ulonglong)],
 }
 
 _lib = None
@@ -331,6 +337,50 @@ class Launcher:
         pick = ctypes.c_void_p()
         check(lib().rt_launcher_frame(self.h, ctypes.byref(f), ctypes.byref(img), ctypes.byref(pick)))
         return f, img, pick
+
+
+class Batch:
+    """Owns an rt_batch: many scenes built and rendered together.  Device
+    output buffers are allocated here (cudaMalloc through the library is not
+    exposed, so torch tensors hold them) and kept alive with the batch."""
+
+    def __init__(self):
+        self.h = ctypes.c_void_p()
+        check(lib().rt_batch_create(ctypes.byref(self.h)))
+        self._keep = []
+
+    def close(self):
+        if self.h:
+            lib().rt_batch_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add(self, scene, cam, params, frame):
+        idx = ctypes.c_uint()
+        check(lib().rt_batch_add(self.h, scene.h, ctypes.byref(cam), ctypes.byref(params), ctypes.byref(frame),
+                                 ctypes.byref(idx)))
+        self._keep.append((scene, cam, params, frame))
+        return idx.value
+
+    def build(self, morton_bits=60, stream=None):
+        check(lib().rt_batch_build(self.h, morton_bits, stream))
+
+    def launch(self, stream=None):
+        st = LaunchStats()
+        check(lib().rt_batch_launch(self.h, stream, ctypes.byref(st)))
+        return st
+
+    def info(self):
+        n, p = ctypes.c_uint(), ctypes.c_uint()
+        ms = ctypes.c_float()
+        b = ctypes.c_ulonglong()
+        check(lib().rt_batch_info(self.h, ctypes.byref(n), ctypes.byref(p), ctypes.byref(ms), ctypes.byref(b)))
+        return dict(n_scenes=n.value, n_prims=p.value, build_ms=ms.value, device_bytes=b.value)
 
 
 def render(scene, cam, params, guides=False):

@@ -218,13 +218,13 @@ struct Trav {
     int sp;
 };
 
-__device__ __forceinline__ void trav_init(Trav& s, float3 o, float3 d) {
+__device__ __forceinline__ void trav_init(Trav& s, float3 o, float3 d, int root) {
     s.o = o;
     s.d = d;
     s.inv = mk(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
     s.best = kTmax;
     s.h = HitRec{0.f, 0.f, 0.f, -1, 0u, false};
-    s.node = 0;
+    s.node = root;
     s.sp = 0;
 }
 
@@ -309,15 +309,15 @@ __device__ __forceinline__ bool trav_step(Trav& s, int* stack, const float4* __r
     return true;
 }
 
-// Closest hit over the LBVH for one ray (loop over trav_step).
+// Closest hit over the LBVH below `root` for one ray (loop over trav_step);
+// root < 0 is an empty scene.
 template <bool kCount>
 __device__ __forceinline__ HitRec closest_hit(const float4* __restrict__ nodes, const float4* __restrict__ prims,
-                                              uint32_t nprims, float3 o, float3 d, uint32_t& nvis,
-                                              uint32_t& ntest) {
+                                              int root, float3 o, float3 d, uint32_t& nvis, uint32_t& ntest) {
     Trav s;
     int stack[kStackSize];
-    trav_init(s, o, d);
-    if (nprims == 0) return s.h;
+    trav_init(s, o, d, root);
+    if (root < 0) return s.h;
     while (trav_step<kCount>(s, stack, nodes, prims, nvis, ntest)) {
     }
     return s.h;

@@ -1,20 +1,24 @@
-// rt_render.cu -- wavefront path tracer, first-hit/picker kernels, post-processing.
+// rt_render.cu -- wavefront path tracer over one or many scenes, first-hit /
+// picker kernels, post-processing, launcher and batch ABI.
 //
 // Replaces Launcher::ignite + optixLaunch (optx/launcher.cxx:49-77) and the
 // OptiX programs __raygen__camera / __miss__ambient (optx/camera_i.cu:24-141)
 // and __closesthit__diffuse/reflect/refract (optx/optics_i.cu:23-288), plus
 // pp_sRGB / pp_none (optx/postproc.cu).
 //
-// Design: paths are numbered pid = sample_in_chunk * npix + pixel.  A wave
-// queue of W rays (SoA float4 arrays) is traversed by `extend` (one thread per
-// ray, closest hit over the LBVH) and resolved by `shade` (miss/sky, depth
-// limit, Lambertian / metal / dielectric scatter).  A path that ends writes
-// its colour and ray count to its own slot of a per-chunk result buffer and is
-// replaced in the same thread by the next camera path (one atomic per warp);
-// continuing and new rays are appended to the next queue with a warp ballot
-// and one atomic per warp.  After a chunk of samples drains, `accumulate` adds
-// each pixel's samples in sample order, so the image does not depend on the
-// order in which paths finished and equals the sequential CPU sum bit for bit.
+// Design: a render is a list of jobs (a scene segment of a geometry, its
+// camera, parameters and output frame); a single-scene launch is a list of
+// one.  Paths are numbered globally (job after job, sample-major inside a
+// job).  A wave queue of W rays (SoA float4 arrays) is traversed by `extend`
+// (closest hit over the job's LBVH) and resolved by `shade` (miss/sky, depth
+// limit, Lambertian / metal / dielectric scatter).  A path that ends adds its
+// colour and ray count to its pixel in 64-bit fixed point (integer atomics,
+// so the sums do not depend on the order in which paths finish) and its
+// thread starts the next camera path (one atomic per warp); continuing and new
+// rays are appended to the next queue with a warp ballot and one atomic per
+// warp.  A one-thread `ctrl` kernel flips the queues and decides whether
+// another wave runs; the wave loop runs either from the host (a status read
+// every 8 waves) or inside a CUDA graph as a conditional WHILE node.
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
@@ -29,68 +33,111 @@ namespace {
 constexpr int kThreads = 256;
 inline unsigned grid_for(uint64_t n, int threads = kThreads) { return unsigned((n + threads - 1) / threads); }
 
+struct JobDev {              // one render job on the device
+    CamDev cam;
+    float3 ambient, white;
+    uint32_t W, H, npix, spp, depth, seed, key1;
+    int root;                // root node of the job's scene, -1: empty scene
+    uint32_t pix_offset;     // first pixel of the job in the accumulators
+    int guides;
+    unsigned long long path_offset;   // first global path of the job
+    rt_float3* rawRGB;
+    uint32_t* rpp;
+    rt_float3* normals;
+    rt_float3* albedos;
+};
+
 struct WaveState {
     uint32_t count[2];       // rays in queue 0 / 1
-    uint32_t next_path;      // next path id to start (chunk-relative)
-    uint32_t err;            // nonzero: a traversal stack overflowed
-    uint32_t fetch[2];       // next ray of queue 0 / 1 to hand to a persistent traversal lane
+    uint32_t fetch[2];       // next ray of queue 0 / 1 handed to a persistent traversal lane
+    uint32_t cur;            // queue of the current wave
+    uint32_t iter;           // waves run
+    uint32_t max_iter;       // exact upper bound of the waves
+    uint32_t err;            // 1: traversal stack overflow, 2: wave bound exceeded
+    unsigned long long next_path, total_paths;
     unsigned long long nodes, prims, rays;
 };
 
-struct RenderArgs {
-    CamDev cam;
-    uint32_t W, H, npix;
-    uint32_t spp, depth, seed, scene_id;
-    uint32_t sample_base;    // first sample of this chunk
-    uint32_t npaths;         // paths in this chunk
-    float3 ambient, white;
-    int guides;
-};
-
 struct Queue {
-    float4* ori;   // origin.xyz, path id
-    float4* dir;   // direction.xyz, bounce
+    float4* ori;   // origin.xyz, job-local path id
+    float4* dir;   // direction.xyz, (job << 8) | bounce
     float4* thr;   // throughput.rgb
     float4* gn;    // guide normal (guides only)
     float4* ga;    // guide albedo (guides only)
 };
+struct Queues {
+    Queue q[2];
+};
 
-struct Results {
-    float4* col;   // colour.rgb, rays (as float)
-    float4* gn;
-    float4* ga;
+// Per-pixel sums, structure of arrays over the launch's pixels: colour
+// channels in 64-bit fixed point (2^-32 units), rays as u32, guide layers
+// (normal xyz, albedo xyz) in fixed point.
+struct Acc {
+    unsigned long long* col[3];
+    uint32_t* rays;
+    unsigned long long* gd[6];
 };
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
 
-// Camera path pid of the chunk: primary ray + queue entry.
-__device__ __forceinline__ void make_camera_ray(const RenderArgs& a, uint32_t pid, float3& o, float3& d) {
-    const uint32_t pixel = pid % a.npix;
-    const uint32_t sample = a.sample_base + pid / a.npix;
-    Stream s(a.seed, a.scene_id, pixel, sample, 0);
-    camera_ray(a.cam, pixel % a.W, pixel / a.W, a.W, a.H, s, o, d);
+__device__ __forceinline__ Queue pick(const Queues& qs, uint32_t k) { return k ? qs.q[1] : qs.q[0]; }
+
+// Job of a global path / global pixel (jobs are ordered by both offsets).
+__device__ __forceinline__ uint32_t job_of_path(const JobDev* __restrict__ jobs, uint32_t nj, unsigned long long g) {
+    uint32_t lo = 0, hi = nj;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (jobs[mid].path_offset <= g) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+__device__ __forceinline__ uint32_t job_of_pixel(const JobDev* __restrict__ jobs, uint32_t nj, uint32_t p) {
+    uint32_t lo = 0, hi = nj;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (jobs[mid].pix_offset <= p) lo = mid; else hi = mid;
+    }
+    return lo;
 }
 
-__global__ void __launch_bounds__(kThreads) k_generate(RenderArgs a, Queue q, uint32_t n) {
+// Camera ray of job-local path pid (sample-major: pid = sample * npix + pixel).
+__device__ __forceinline__ void make_camera_ray(const JobDev& j, uint32_t pid, float3& o, float3& d) {
+    const uint32_t pixel = pid % j.npix;
+    const uint32_t sample = pid / j.npix;
+    Stream s(j.seed, j.key1, pixel, sample, 0);
+    camera_ray(j.cam, pixel % j.W, pixel / j.W, j.W, j.H, s, o, d);
+}
+
+__global__ void k_init_state(WaveState* st, uint32_t n0, unsigned long long total, uint32_t max_iter) {
+    st->count[0] = n0;
+    st->count[1] = 0;
+    st->fetch[0] = 0;
+    st->fetch[1] = 0;
+    st->cur = 0;
+    st->iter = 0;
+    st->max_iter = max_iter;
+    st->err = 0;
+    st->next_path = n0;
+    st->total_paths = total;
+    st->nodes = st->prims = st->rays = 0;
+}
+
+__global__ void __launch_bounds__(kThreads) k_generate(const JobDev* __restrict__ jobs, uint32_t nj, Queue q,
+                                                       uint32_t n, int any_guides) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const uint32_t jx = job_of_path(jobs, nj, i);
+    const JobDev& j = jobs[jx];
+    const uint32_t pid = uint32_t(i - j.path_offset);
     float3 o, d;
-    make_camera_ray(a, i, o, d);
-    q.ori[i] = make_float4(o.x, o.y, o.z, __uint_as_float(i));
-    q.dir[i] = make_float4(d.x, d.y, d.z, __uint_as_float(0u));
+    make_camera_ray(j, pid, o, d);
+    q.ori[i] = make_float4(o.x, o.y, o.z, __uint_as_float(pid));
+    q.dir[i] = make_float4(d.x, d.y, d.z, __uint_as_float(jx << 8));
     q.thr[i] = make_float4(1.f, 1.f, 1.f, 0.f);
-    if (a.guides) {
+    if (any_guides) {
         q.gn[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         q.ga[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
-}
-
-__global__ void k_set_state(WaveState* st, uint32_t n0) {
-    st->count[0] = n0;
-    st->count[1] = 0;
-    st->next_path = n0;
-    st->fetch[0] = 0;
-    st->fetch[1] = 0;
 }
 
 // Persistent traversal: a grid sized to the resident blocks; every lane that
@@ -100,13 +147,14 @@ __global__ void k_set_state(WaveState* st, uint32_t n0) {
 // (one atomic per warp per refill).
 template <bool kCount, int kInner, int kRefill>
 __global__ void __launch_bounds__(kThreads)
-    k_extend_p(const float4* __restrict__ q_ori, const float4* __restrict__ q_dir, float4* __restrict__ hits,
-               WaveState* st, int cur, const float4* __restrict__ nodes, const float4* __restrict__ prims,
-               uint32_t nprims) {
+    k_extend_p(Queues qs, float4* __restrict__ hits, WaveState* st, const JobDev* __restrict__ jobs,
+               const float4* __restrict__ nodes, const float4* __restrict__ prims) {
+    const uint32_t cur = *((volatile uint32_t*)&st->cur);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         st->count[cur ^ 1] = 0;   // the next queue starts empty
         st->fetch[cur ^ 1] = 0;
     }
+    const Queue Q = pick(qs, cur);
     const uint32_t n = *((volatile uint32_t*)&st->count[cur]);
     const uint32_t lane = lane_id();
     const uint32_t lanemask_lt = (1u << lane) - 1u;
@@ -127,15 +175,15 @@ __global__ void __launch_bounds__(kThreads)
                 const uint32_t idx = base + __popc(idle & lanemask_lt);
                 if (idx < n) {
                     ray = int(idx);
-                    const float4 o4 = q_ori[idx], d4 = q_dir[idx];
-                    trav_init(s, xyz(o4), xyz(d4));
+                    const float4 o4 = Q.ori[idx], d4 = Q.dir[idx];
+                    trav_init(s, xyz(o4), xyz(d4), jobs[__float_as_uint(d4.w) >> 8].root);
                 }
             }
         }
         if (__ballot_sync(0xFFFFFFFFu, ray >= 0) == 0) break;
         if (ray >= 0) {
             for (int k = 0; k < kInner; ++k) {
-                if (nprims == 0 || !trav_step<kCount>(s, stack, nodes, prims, nvis, ntest)) {
+                if (s.node < 0 || !trav_step<kCount>(s, stack, nodes, prims, nvis, ntest)) {
                     hits[ray] = make_float4(s.h.t, s.h.u, s.h.v, __int_as_float(s.h.leaf));
                     if (s.h.overflow) atomicOr(&st->err, 1u);
                     ray = -1;
@@ -159,16 +207,18 @@ __global__ void __launch_bounds__(kThreads)
 // One thread per queued ray.
 template <bool kCount>
 __global__ void __launch_bounds__(kThreads)
-    k_extend(const float4* __restrict__ q_ori, const float4* __restrict__ q_dir, float4* __restrict__ hits,
-             WaveState* st, int cur, const float4* __restrict__ nodes, const float4* __restrict__ prims,
-             uint32_t nprims) {
+    k_extend(Queues qs, float4* __restrict__ hits, WaveState* st, const JobDev* __restrict__ jobs,
+             const float4* __restrict__ nodes, const float4* __restrict__ prims) {
+    const uint32_t cur = *((volatile uint32_t*)&st->cur);
     if (blockIdx.x == 0 && threadIdx.x == 0) st->count[cur ^ 1] = 0;   // the next queue starts empty
     const uint32_t n = *((volatile uint32_t*)&st->count[cur]);
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t nvis = 0, ntest = 0;
     if (i < n) {
-        const float4 o4 = q_ori[i], d4 = q_dir[i];
-        const HitRec h = closest_hit<kCount>(nodes, prims, nprims, xyz(o4), xyz(d4), nvis, ntest);
+        const Queue Q = pick(qs, cur);
+        const float4 o4 = Q.ori[i], d4 = Q.dir[i];
+        const int root = jobs[__float_as_uint(d4.w) >> 8].root;
+        const HitRec h = closest_hit<kCount>(nodes, prims, root, xyz(o4), xyz(d4), nvis, ntest);
         hits[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.leaf));
         if (h.overflow) atomicOr(&st->err, 1u);
     }
@@ -184,18 +234,17 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
-// Traversal kernel variants, chosen per launch by name (RTX_EXTEND) or the
-// default; each has a plain and a counting instantiation.
-using ExtendFn = void (*)(const float4*, const float4*, float4*, WaveState*, int, const float4*, const float4*,
-                          uint32_t);
+// Traversal kernel variants, chosen by name (RTX_EXTEND) or the default; each
+// has a plain and a counting instantiation.  Measured on C1 (1200x800, 64
+// spp): one thread per ray 1194-1241 Mrays/s; persistent lanes raise the
+// active lanes per instruction from 12.0 to 16.6 of 32 but add 35% more
+// instructions to an issue-bound kernel (1172 Mrays/s).
+using ExtendFn = void (*)(Queues, float4*, WaveState*, const JobDev*, const float4*, const float4*);
 struct ExtendVariant {
     const char* name;
     ExtendFn fn[2];     // [counting]
     bool persistent;
 };
-// Measured on C1 (1200x800, 64 spp): plain 1194-1241 Mrays/s; persistent
-// lanes raise the active lanes per instruction from 12.0 to 16.6 of 32 but add
-// 35% instructions to an issue-bound kernel (1172 Mrays/s, refill 8, 1 step).
 const ExtendVariant kExtendVariants[] = {
     {"plain", {k_extend<false>, k_extend<true>}, false},
     {"persistent", {k_extend_p<false, 4, 16>, k_extend_p<true, 4, 16>}, true},
@@ -210,35 +259,46 @@ __device__ __forceinline__ float3 sky(float3 d, float3 ambient, float3 white) {
     return add(mul(1.f - t, white), mul(t, ambient));
 }
 
-__global__ void __launch_bounds__(kThreads) k_shade(RenderArgs a, Queue cur, Queue nxt, const float4* __restrict__ hits,
-                                                    WaveState* st, int ci, const float4* __restrict__ prims,
-                                                    const ThingDev* __restrict__ things, Results res) {
-    const uint32_t n = *((volatile uint32_t*)&st->count[ci]);
+// 64-bit fixed-point sample sums: round-half-even(x * 2^32) as two's
+// complement, added with integer atomics (exact, order-free).
+__device__ __forceinline__ unsigned long long fx_q(float x) {
+    return (unsigned long long)__float2ll_rn(x * 4294967296.0f);
+}
+
+__global__ void __launch_bounds__(kThreads)
+    k_shade(Queues qs, const float4* __restrict__ hits, WaveState* st, const JobDev* __restrict__ jobs, uint32_t nj,
+            const float4* __restrict__ prims, const ThingDev* __restrict__ things, Acc acc, int any_guides) {
+    const uint32_t cur = *((volatile uint32_t*)&st->cur);
+    const uint32_t n = *((volatile uint32_t*)&st->count[cur]);
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t lane = lane_id();
     if (i - lane >= n) return;   // whole warp past the queue end
     const bool active = i < n;
+    const Queue Q = pick(qs, cur), N = pick(qs, cur ^ 1);
 
     bool cont = false, ended = false;
     float3 no{}, nd{}, nthr{};
     float3 gN{}, gA{};
-    uint32_t pid = 0, bounce = 0;
+    uint32_t pid = 0, bounce = 0, jx = 0;
     if (active) {
-        const float4 o4 = cur.ori[i], d4 = cur.dir[i], t4 = cur.thr[i], h4 = hits[i];
+        const float4 o4 = Q.ori[i], d4 = Q.dir[i], t4 = Q.thr[i], h4 = hits[i];
         pid = __float_as_uint(o4.w);
-        bounce = __float_as_uint(d4.w);
+        const uint32_t tag = __float_as_uint(d4.w);
+        jx = tag >> 8;
+        bounce = tag & 0xFFu;
+        const JobDev& j = jobs[jx];
         const float3 o = xyz(o4), d = xyz(d4);
         float3 thr = xyz(t4);
-        if (a.guides) {
-            gN = xyz(cur.gn[i]);
-            gA = xyz(cur.ga[i]);
+        if (any_guides) {
+            gN = xyz(Q.gn[i]);
+            gA = xyz(Q.ga[i]);
         }
         const int leaf = __float_as_int(h4.w);
         float3 color = mk(0.f, 0.f, 0.f);
         if (leaf < 0) {
-            color = mulv(thr, sky(d, a.ambient, a.white));
+            color = mulv(thr, sky(d, j.ambient, j.white));
             ended = true;
-        } else if (bounce + 1 >= a.depth) {
+        } else if (bounce + 1 >= j.depth) {
             ended = true;   // black at the depth limit (optx/optics_r.cu:34-42)
         } else {
             const float4 pa = __ldg(prims + 3 * leaf), pb = __ldg(prims + 3 * leaf + 1), pc = __ldg(prims + 3 * leaf + 2);
@@ -247,41 +307,39 @@ __global__ void __launch_bounds__(kThreads) k_shade(RenderArgs a, Queue cur, Que
             const int type = __float_as_int(th.albedo_type.w);
             const float3 albedo = xyz(th.albedo_type);
             // hit geometry: optx/optics_i.cu:40-82 (triangles), sphere.h:40-46 (spheres)
-            float3 p, N;
+            float3 p, Nn;
             bool front;
             if (__float_as_uint(pc.w) == kPrimTriangle) {
                 const float3 A = xyz(pa), B = xyz(pb), C = xyz(pc);
                 const float u = h4.y, v = h4.z;
                 const float w = 1.f - u - v;
                 p = add(add(mul(w, A), mul(u, B)), mul(v, C));
-                N = unitV(cross(sub(B, A), sub(C, A)));
-                if (dot(d, N) > 0.f) N = neg(N);
+                Nn = unitV(cross(sub(B, A), sub(C, A)));
+                if (dot(d, Nn) > 0.f) Nn = neg(Nn);
                 front = 0.f > dot(d, sub(p, xyz(th.center_fuzz)));   // optx/optics_i.cu:259-267
             } else {
                 p = add(o, mul(h4.x, d));
                 const float3 outward = mul(1.f / pb.x, sub(p, xyz(pa)));
                 front = 0.f > dot(d, outward);
-                N = front ? outward : neg(outward);
+                Nn = front ? outward : neg(outward);
             }
-            const uint32_t pixel = pid % a.npix;
-            const uint32_t sample = a.sample_base + pid / a.npix;
-            Stream s(a.seed, a.scene_id, pixel, sample, bounce + 1);
+            Stream s(j.seed, j.key1, pid % j.npix, pid / j.npix, bounce + 1);
             if (type == RT_OPTICS_DIFFUSE) {
                 // optx/optics_i.cu:87-96, near-zero fallback of optics.h:17-18
-                float3 dir = add(N, rndVon1sphere(s));
-                if (near0(dir)) dir = N;
+                float3 dir = add(Nn, rndVon1sphere(s));
+                if (near0(dir)) dir = Nn;
                 thr = mulv(thr, albedo);
-                if (isnull(gN)) gN = N;
+                if (isnull(gN)) gN = Nn;
                 if (isnull(gA)) gA = albedo;
                 no = p; nd = dir; nthr = thr; cont = true;
             } else if (type == RT_OPTICS_REFLECT) {
                 // optx/optics_i.cu:168-190
                 const float3 d1V = unitV(d);
-                const float3 refl = sub(d1V, mul(2.f * dot(d1V, N), N));
+                const float3 refl = sub(d1V, mul(2.f * dot(d1V, Nn), Nn));
                 const float3 dir = add(refl, mul(th.center_fuzz.w, rndVin1sphere(s)));
-                if (isnull(gN)) gN = N;
+                if (isnull(gN)) gN = Nn;
                 if (isnull(gA)) gA = albedo;
-                if (dot(dir, N) > 0.f) {
+                if (dot(dir, Nn) > 0.f) {
                     thr = mulv(thr, albedo);
                     no = p; nd = dir; nthr = thr; cont = true;
                 } else {
@@ -290,7 +348,7 @@ __global__ void __launch_bounds__(kThreads) k_shade(RenderArgs a, Queue cur, Que
             } else {
                 // optx/optics_i.cu:254-283, Schlick's pow 5 as products
                 const float3 d1V = unitV(d);
-                const float cos_theta = fminf(dot(neg(d1V), N), 1.f);
+                const float cos_theta = fminf(dot(neg(d1V), Nn), 1.f);
                 const float sin_theta = sqrtf(1.f - cos_theta * cos_theta);
                 const float index = th.index_pad.x;
                 const float ratio = front ? 1.f / index : index;
@@ -302,123 +360,116 @@ __global__ void __launch_bounds__(kThreads) k_shade(RenderArgs a, Queue cur, Que
                 const float schlick = r0 + (1.f - r0) * pow5;
                 float3 dir;
                 if (cannot || schlick > s.next()) {
-                    dir = sub(d1V, mul(2.f * dot(d1V, N), N));
+                    dir = sub(d1V, mul(2.f * dot(d1V, Nn), Nn));
                 } else {
-                    const float theta = fminf(dot(neg(d1V), N), 1.f);
-                    const float3 perpen = mul(ratio, add(d1V, mul(theta, N)));
-                    const float3 parall = mul(-sqrtf(fabsf(1.f - dot(perpen, perpen))), N);
+                    const float theta = fminf(dot(neg(d1V), Nn), 1.f);
+                    const float3 perpen = mul(ratio, add(d1V, mul(theta, Nn)));
+                    const float3 parall = mul(-sqrtf(fabsf(1.f - dot(perpen, perpen))), Nn);
                     dir = add(perpen, parall);
                 }
                 no = p; nd = dir; nthr = thr; cont = true;
             }
         }
         if (ended) {
-            const uint32_t slot = pid;   // chunk-relative path id
-            res.col[slot] = make_float4(color.x, color.y, color.z, float(bounce + 1));
-            if (a.guides) {
-                res.gn[slot] = make_float4(gN.x, gN.y, gN.z, 0.f);
-                res.ga[slot] = make_float4(gA.x, gA.y, gA.z, 0.f);
+            const size_t px = size_t(j.pix_offset) + pid % j.npix;
+            const unsigned long long qr = fx_q(color.x), qg = fx_q(color.y), qb = fx_q(color.z);
+            if (qr) atomicAdd(acc.col[0] + px, qr);   // zero terms (black paths) cost nothing
+            if (qg) atomicAdd(acc.col[1] + px, qg);
+            if (qb) atomicAdd(acc.col[2] + px, qb);
+            atomicAdd(acc.rays + px, bounce + 1);
+            if (j.guides) {
+                const float gv[6] = {gN.x, gN.y, gN.z, gA.x, gA.y, gA.z};
+#pragma unroll
+                for (int k = 0; k < 6; ++k) {
+                    const unsigned long long q = fx_q(gv[k]);
+                    if (q) atomicAdd(acc.gd[k] + px, q);
+                }
             }
         }
     }
 
     // regenerate: every ended path is replaced by the next camera path
     const uint32_t want = __ballot_sync(0xFFFFFFFFu, ended);
-    uint32_t new_pid = 0xFFFFFFFFu;
+    bool fresh = false;
     if (want) {
-        uint32_t base = 0;
-        if (lane == uint32_t(__ffs(want) - 1)) base = atomicAdd(&st->next_path, uint32_t(__popc(want)));
-        base = __shfl_sync(0xFFFFFFFFu, base, __ffs(want) - 1);
+        unsigned long long base = 0;
+        const int leader = __ffs(want) - 1;
+        if (int(lane) == leader) base = atomicAdd(&st->next_path, (unsigned long long)__popc(want));
+        base = __shfl_sync(0xFFFFFFFFu, base, leader);
         if (ended) {
-            const uint32_t cand = base + __popc(want & ((1u << lane) - 1u));
-            if (cand < a.npaths) new_pid = cand;
+            const unsigned long long g = base + __popc(want & ((1u << lane) - 1u));
+            if (g < st->total_paths) {
+                jx = job_of_path(jobs, nj, g);
+                const JobDev& j = jobs[jx];
+                pid = uint32_t(g - j.path_offset);
+                make_camera_ray(j, pid, no, nd);
+                nthr = mk(1.f, 1.f, 1.f);
+                gN = mk(0.f, 0.f, 0.f);
+                gA = mk(0.f, 0.f, 0.f);
+                bounce = 0;
+                fresh = true;
+            }
         }
     }
-    bool fresh = false;
-    if (new_pid != 0xFFFFFFFFu) {
-        make_camera_ray(a, new_pid, no, nd);
-        nthr = mk(1.f, 1.f, 1.f);
-        gN = mk(0.f, 0.f, 0.f);
-        gA = mk(0.f, 0.f, 0.f);
-        pid = new_pid;
-        bounce = 0;
-        fresh = true;
-    } else if (cont) {
-        bounce += 1;
-    }
+    if (cont) bounce += 1;
     const bool push = cont || fresh;
     const uint32_t pm = __ballot_sync(0xFFFFFFFFu, push);
     if (pm) {
         uint32_t base = 0;
-        if (lane == uint32_t(__ffs(pm) - 1)) base = atomicAdd(&st->count[ci ^ 1], uint32_t(__popc(pm)));
-        base = __shfl_sync(0xFFFFFFFFu, base, __ffs(pm) - 1);
+        const int leader = __ffs(pm) - 1;
+        if (int(lane) == leader) base = atomicAdd(&st->count[cur ^ 1], uint32_t(__popc(pm)));
+        base = __shfl_sync(0xFFFFFFFFu, base, leader);
         if (push) {
             const uint32_t slot = base + __popc(pm & ((1u << lane) - 1u));
-            nxt.ori[slot] = make_float4(no.x, no.y, no.z, __uint_as_float(pid));
-            nxt.dir[slot] = make_float4(nd.x, nd.y, nd.z, __uint_as_float(bounce));
-            nxt.thr[slot] = make_float4(nthr.x, nthr.y, nthr.z, 0.f);
-            if (a.guides) {
-                nxt.gn[slot] = make_float4(gN.x, gN.y, gN.z, 0.f);
-                nxt.ga[slot] = make_float4(gA.x, gA.y, gA.z, 0.f);
+            N.ori[slot] = make_float4(no.x, no.y, no.z, __uint_as_float(pid));
+            N.dir[slot] = make_float4(nd.x, nd.y, nd.z, __uint_as_float((jx << 8) | bounce));
+            N.thr[slot] = make_float4(nthr.x, nthr.y, nthr.z, 0.f);
+            if (any_guides) {
+                N.gn[slot] = make_float4(gN.x, gN.y, gN.z, 0.f);
+                N.ga[slot] = make_float4(gA.x, gA.y, gA.z, 0.f);
             }
         }
     }
 }
 
-// Adds the chunk's samples of every pixel in sample order (optx/camera_i.cu:95-101).
-__global__ void __launch_bounds__(kThreads) k_accumulate(Results res, uint32_t npix, uint32_t nsamples, int first,
-                                                         int guides, float4* __restrict__ acc,
-                                                         uint32_t* __restrict__ acc_rays, float4* __restrict__ acc_n,
-                                                         float4* __restrict__ acc_a) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= npix) return;
-    float3 c = first ? mk(0.f, 0.f, 0.f) : xyz(acc[p]);
-    uint32_t rays = first ? 0u : acc_rays[p];
-    float3 gn = mk(0.f, 0.f, 0.f), ga = mk(0.f, 0.f, 0.f);
-    if (guides && !first) {
-        gn = xyz(acc_n[p]);
-        ga = xyz(acc_a[p]);
+// One thread: flips the queues and decides whether another wave runs; inside
+// a graph it sets the WHILE condition.  The wave count is capped by an exact
+// bound, past which the loop stops with an error flag.
+__global__ void k_wave_ctrl(WaveState* st, cudaGraphConditionalHandle handle, int in_graph) {
+    const uint32_t cur = st->cur;
+    if (st->count[cur] != 0) st->iter += 1;   // a wave ran (the host loop may run empty ones)
+    const uint32_t next = cur ^ 1u;
+    st->cur = next;
+    bool more = st->count[next] != 0;
+    if (more && st->iter >= st->max_iter) {
+        st->err |= 2u;
+        more = false;
     }
-    for (uint32_t s = 0; s < nsamples; ++s) {
-        const size_t slot = size_t(s) * npix + p;
-        const float4 r = res.col[slot];
-        c = add(c, xyz(r));
-        rays += uint32_t(r.w);
-        if (guides) {
-            gn = add(gn, xyz(res.gn[slot]));
-            ga = add(ga, xyz(res.ga[slot]));
-        }
-    }
-    acc[p] = make_float4(c.x, c.y, c.z, 0.f);
-    acc_rays[p] = rays;
-    if (guides) {
-        acc_n[p] = make_float4(gn.x, gn.y, gn.z, 0.f);
-        acc_a[p] = make_float4(ga.x, ga.y, ga.z, 0.f);
-    }
+    if (in_graph) cudaGraphSetConditional(handle, more ? 1u : 0u);
 }
 
 __device__ __forceinline__ float clamp01(float x) { return 0.f > x ? 0.f : (x > 1.f ? 1.f : x); }
+__device__ __forceinline__ float fx_mean(unsigned long long s, uint32_t spp) {
+    return float(double((long long)s) * 0x1p-32 / double(spp));
+}
 
-// optx/camera_i.cu:104-113: mean = 1/spp * sum clamped to [0,1]; rpp; guides.
-__global__ void __launch_bounds__(kThreads) k_finalize(const float4* __restrict__ acc, const uint32_t* __restrict__ acc_rays,
-                                                       const float4* __restrict__ acc_n, const float4* __restrict__ acc_a,
-                                                       uint32_t npix, uint32_t spp, rt_float3* rawRGB, uint32_t* rpp,
-                                                       rt_float3* normals, rt_float3* albedos, WaveState* st) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+// optx/camera_i.cu:104-113: mean over spp clamped to [0,1]; rpp; guides.
+__global__ void __launch_bounds__(kThreads) k_finalize(const JobDev* __restrict__ jobs, uint32_t nj, Acc acc,
+                                                       uint32_t total_pix, WaveState* st) {
+    const uint32_t gp = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned long long r = 0;
-    if (p < npix) {
-        const float inv = 1.f / float(spp);
-        const float3 m = mul(inv, xyz(acc[p]));
-        rawRGB[p] = rt_float3{clamp01(m.x), clamp01(m.y), clamp01(m.z)};
-        r = acc_rays[p];
-        if (rpp) rpp[p] = acc_rays[p];
-        if (normals) {
-            const float3 n = mul(inv, xyz(acc_n[p]));
-            normals[p] = rt_float3{n.x, n.y, n.z};
-        }
-        if (albedos) {
-            const float3 al = mul(inv, xyz(acc_a[p]));
-            albedos[p] = rt_float3{al.x, al.y, al.z};
+    if (gp < total_pix) {
+        const JobDev& j = jobs[job_of_pixel(jobs, nj, gp)];
+        const uint32_t p = gp - j.pix_offset;
+        j.rawRGB[p] = rt_float3{clamp01(fx_mean(acc.col[0][gp], j.spp)), clamp01(fx_mean(acc.col[1][gp], j.spp)),
+                                clamp01(fx_mean(acc.col[2][gp], j.spp))};
+        r = acc.rays[gp];
+        if (j.rpp) j.rpp[p] = acc.rays[gp];
+        if (j.guides) {
+            j.normals[p] = rt_float3{fx_mean(acc.gd[0][gp], j.spp), fx_mean(acc.gd[1][gp], j.spp),
+                                     fx_mean(acc.gd[2][gp], j.spp)};
+            j.albedos[p] = rt_float3{fx_mean(acc.gd[3][gp], j.spp), fx_mean(acc.gd[4][gp], j.spp),
+                                     fx_mean(acc.gd[5][gp], j.spp)};
         }
     }
     for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xFFFFFFFFu, r, o);
@@ -456,21 +507,25 @@ __device__ double dist64(const float4* __restrict__ rec, float3 of, float3 df) {
     return t;
 }
 
+struct FirstHitArgs {
+    CamDev cam;
+    uint32_t W, H, seed, key1, sample, x0, y0, nx, ny;
+    int root;
+};
+
 // Primary-ray closest hit of one sample for a pixel rectangle.
-__global__ void __launch_bounds__(kThreads) k_first_hit(RenderArgs a, uint32_t sample, uint32_t x0, uint32_t y0,
-                                                        uint32_t nx, uint32_t ny, const float4* __restrict__ nodes,
-                                                        const float4* __restrict__ prims, uint32_t nprims, int* prim,
-                                                        int* thing, float* t, float* u, float* v, double* t64,
-                                                        uint32_t* err) {
+__global__ void __launch_bounds__(kThreads) k_first_hit(FirstHitArgs a, const float4* __restrict__ nodes,
+                                                        const float4* __restrict__ prims, int* prim, int* thing, float* t,
+                                                        float* u, float* v, double* t64, uint32_t* err) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nx * ny) return;
-    const uint32_t x = x0 + k % nx, y = y0 + k / nx;
+    if (k >= a.nx * a.ny) return;
+    const uint32_t x = a.x0 + k % a.nx, y = a.y0 + k / a.nx;
     const uint32_t pixel = a.W * y + x;
-    Stream s(a.seed, a.scene_id, pixel, sample, 0);
+    Stream s(a.seed, a.key1, pixel, a.sample, 0);
     float3 o, d;
     camera_ray(a.cam, x, y, a.W, a.H, s, o, d);
     uint32_t nv = 0, nt = 0;
-    const HitRec h = closest_hit<false>(nodes, prims, nprims, o, d, nv, nt);
+    const HitRec h = closest_hit<false>(nodes, prims, a.root, o, d, nv, nt);
     if (h.overflow) atomicOr(err, 1u);
     if (h.leaf < 0) {
         prim[k] = -1;
@@ -539,23 +594,8 @@ void check_params(const rt_launch_params* p) {
     RT_REQUIRE(p->image_w > 0 && p->image_h > 0, "image size must be positive");
     RT_REQUIRE(uint64_t(p->image_w) * p->image_h <= (uint64_t(1) << 28), "image has more than 2^28 pixels");
     RT_REQUIRE(p->spp >= 1, "spp must be >= 1");
+    RT_REQUIRE(uint64_t(p->image_w) * p->image_h * p->spp <= 0xFFFFFFFFull, "w*h*spp must fit in 32 bits");
     RT_REQUIRE(p->depth >= 1 && p->depth <= 255, "depth must be 1..255");
-}
-
-RenderArgs make_args(const rt_camera& cam, const rt_launch_params& p) {
-    RenderArgs a{};
-    a.cam = cam_dev(cam);
-    a.W = p.image_w;
-    a.H = p.image_h;
-    a.npix = p.image_w * p.image_h;
-    a.spp = p.spp;
-    a.depth = p.depth;
-    a.seed = p.seed;
-    a.scene_id = 0;
-    a.ambient = make_float3(p.ambient.x, p.ambient.y, p.ambient.z);
-    a.white = make_float3(p.white.x, p.white.y, p.white.z);
-    a.guides = (p.flags & RT_FLAG_GUIDES) ? 1 : 0;
-    return a;
 }
 
 uint32_t env_u32(const char* name, uint32_t dflt) {
@@ -565,14 +605,34 @@ uint32_t env_u32(const char* name, uint32_t dflt) {
     return x ? uint32_t(x) : dflt;
 }
 
-// Per-thread render workspace (queues, results, accumulators), grow-only.
+// The wave loop captured once as a graph: a conditional WHILE node whose body
+// is extend -> shade -> ctrl; rebuilt whenever a baked-in pointer or launch
+// shape changes.
+struct WaveGraph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<const void*> key;
+    void reset() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        exec = nullptr;
+        graph = nullptr;
+        key.clear();
+    }
+    ~WaveGraph() { reset(); }
+};
+
+// Per-thread render workspace (queues, accumulators, job table), grow-only.
 struct Workspace {
     DevBuf q[2][5];
-    DevBuf hits, res_col, res_gn, res_ga, acc, acc_rays, acc_n, acc_a, state;
-    uint32_t* host_count = nullptr;   // pinned
+    DevBuf hits, acc, acc_gd, jobs, state;
+    WaveState* host_state = nullptr;   // pinned
+    std::vector<JobDev> jobs_host;
     std::vector<cudaEvent_t> events;
+    WaveGraph graph;
     ~Workspace() {
-        if (host_count) cudaFreeHost(host_count);
+        graph.reset();
+        if (host_state) cudaFreeHost(host_state);
         for (auto e : events) cudaEventDestroy(e);
     }
     cudaEvent_t event(size_t k) {
@@ -609,159 +669,249 @@ int extend_variant() {
     return v;
 }
 
-void render(Scene& sc, const rt_camera& cam, const rt_launch_params& p, const rt_frame& f, cudaStream_t s,
-            rt_launch_stats* stats) {
-    check_params(&p);
-    RT_REQUIRE(f.rawRGB != nullptr, "frame.rawRGB is NULL");
-    const bool guides = (p.flags & RT_FLAG_GUIDES) != 0;
-    RT_REQUIRE(!guides || (f.normals && f.albedos), "RT_FLAG_GUIDES needs frame.normals and frame.albedos");
-    if (!sc.built || sc.topology_dirty) throw Error(RT_ERR_NOT_BUILT, "scene not built (call rt_scene_build)");
-    if (sc.xf_dirty) throw Error(RT_ERR_NOT_BUILT, "transforms changed; call rt_scene_update");
-    const bool timing = (p.flags & RT_FLAG_STAGE_TIMING) != 0;
-    const bool count = (p.flags & RT_FLAG_COUNT_VISITS) != 0;
+// Wave loop mode: graph (default) or host-driven (RTX_GRAPH=0, and always
+// when per-kernel CUDA-event timing is requested).
+bool graph_mode() {
+    const char* e = std::getenv("RTX_GRAPH");
+    return !(e && std::strcmp(e, "0") == 0);
+}
+
+struct WaveLaunch {
+    ExtendFn ext_fn;
+    unsigned ext_grid, qgrid;
+    Queues qs;
+    float4* hits;
+    WaveState* st;
+    const JobDev* jobs;
+    uint32_t nj;
+    const float4* nodes;
+    const float4* prims;
+    const ThingDev* things;
+    Acc acc;
+    int any_guides;
+};
+
+void build_wave_graph(Workspace& ws, const WaveLaunch& L) {
+    WaveGraph& G = ws.graph;
+    G.reset();
+    RT_CUDA(cudaGraphCreate(&G.graph, 0));
+    cudaGraphConditionalHandle handle;
+    RT_CUDA(cudaGraphConditionalHandleCreate(&handle, G.graph, 1u, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = handle;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t cnode;
+    RT_CUDA(cudaGraphAddNode(&cnode, G.graph, nullptr, nullptr, 0, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+
+    WaveLaunch l = L;   // kernel arguments must stay addressable while the nodes are added
+    cudaKernelNodeParams kp = {};
+    cudaGraphNode_t n_ext, n_shade, n_ctrl;
+    void* ext_args[] = {&l.qs, &l.hits, &l.st, &l.jobs, &l.nodes, &l.prims};
+    kp.func = reinterpret_cast<void*>(l.ext_fn);
+    kp.gridDim = dim3(l.ext_grid);
+    kp.blockDim = dim3(kThreads);
+    kp.kernelParams = ext_args;
+    RT_CUDA(cudaGraphAddKernelNode(&n_ext, body, nullptr, 0, &kp));
+    const float4* hits_c = l.hits;
+    void* shade_args[] = {&l.qs, &hits_c, &l.st, &l.jobs, &l.nj, &l.prims, &l.things, &l.acc, &l.any_guides};
+    kp.func = reinterpret_cast<void*>(k_shade);
+    kp.gridDim = dim3(l.qgrid);
+    kp.kernelParams = shade_args;
+    RT_CUDA(cudaGraphAddKernelNode(&n_shade, body, &n_ext, 1, &kp));
+    int in_graph = 1;
+    void* ctrl_args[] = {&l.st, &handle, &in_graph};
+    kp.func = reinterpret_cast<void*>(k_wave_ctrl);
+    kp.gridDim = dim3(1);
+    kp.blockDim = dim3(1);
+    kp.kernelParams = ctrl_args;
+    RT_CUDA(cudaGraphAddKernelNode(&n_ctrl, body, &n_shade, 1, &kp));
+    RT_CUDA(cudaGraphInstantiate(&G.exec, G.graph, 0));
+}
+
+}  // namespace
+
+void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s, rt_launch_stats* stats) {
+    RT_REQUIRE(!jobs.empty(), "no jobs to render");
+    uint32_t flags_union = 0;
+    for (const Job& j : jobs) {
+        check_params(&j.params);
+        RT_REQUIRE(j.frame.rawRGB != nullptr, "frame.rawRGB is NULL");
+        if (j.params.flags & RT_FLAG_GUIDES)
+            RT_REQUIRE(j.frame.normals && j.frame.albedos, "RT_FLAG_GUIDES needs frame.normals and frame.albedos");
+        RT_REQUIRE(j.seg < g.nsegs, "job segment out of range");
+        flags_union |= j.params.flags;
+    }
+    RT_REQUIRE(jobs.size() < (1u << 24), "too many jobs (>= 2^24)");
+    const bool stage_timing = (flags_union & RT_FLAG_STAGE_TIMING) != 0;
+    const bool count = (flags_union & RT_FLAG_COUNT_VISITS) != 0;
+    const int any_guides = (flags_union & RT_FLAG_GUIDES) ? 1 : 0;
+    const bool use_graph = graph_mode() && !stage_timing;
 
     Workspace& ws = workspace();
-    RenderArgs a = make_args(cam, p);
-    const uint32_t npix = a.npix;
-    // chunk of samples whose per-path results fit the result budget
-    const uint64_t budget = uint64_t(env_u32("RTX_RESULT_MB", 1024)) << 20;
-    const uint64_t per_sample = uint64_t(npix) * 16u * (guides ? 3u : 1u);
-    uint32_t chunk = uint32_t(std::max<uint64_t>(1, budget / per_sample));
-    chunk = std::min(chunk, p.spp);
-    chunk = uint32_t(std::min<uint64_t>(chunk, (uint64_t(1) << 31) / npix));
-    chunk = std::max(chunk, 1u);
-    const uint64_t max_paths = uint64_t(npix) * chunk;
-    const uint32_t W = uint32_t(std::min<uint64_t>(env_u32("RTX_WAVE", 1u << 21), max_paths));
+    const uint32_t nj = uint32_t(jobs.size());
+    ws.jobs_host.resize(nj);
+    unsigned long long total_paths = 0;
+    uint64_t total_pix = 0;
+    uint32_t max_depth = 1;
+    for (uint32_t k = 0; k < nj; ++k) {
+        const Job& jb = jobs[k];
+        JobDev& d = ws.jobs_host[k];
+        std::memset(&d, 0, sizeof(d));
+        d.cam = cam_dev(jb.cam);
+        d.ambient = make_float3(jb.params.ambient.x, jb.params.ambient.y, jb.params.ambient.z);
+        d.white = make_float3(jb.params.white.x, jb.params.white.y, jb.params.white.z);
+        d.W = jb.params.image_w;
+        d.H = jb.params.image_h;
+        d.npix = d.W * d.H;
+        d.spp = jb.params.spp;
+        d.depth = jb.params.depth;
+        d.seed = jb.params.seed;
+        d.key1 = 0;
+        d.root = g.root(jb.seg);
+        d.pix_offset = uint32_t(total_pix);
+        d.guides = (jb.params.flags & RT_FLAG_GUIDES) ? 1 : 0;
+        d.path_offset = total_paths;
+        d.rawRGB = jb.frame.rawRGB;
+        d.rpp = jb.frame.rpp;
+        d.normals = d.guides ? jb.frame.normals : nullptr;
+        d.albedos = d.guides ? jb.frame.albedos : nullptr;
+        total_paths += (unsigned long long)d.npix * d.spp;
+        total_pix += d.npix;
+        max_depth = std::max(max_depth, d.depth);
+    }
+    RT_REQUIRE(total_pix < (uint64_t(1) << 31), "too many pixels in one launch (>= 2^31)");
+    const uint32_t W = uint32_t(std::min<unsigned long long>(env_u32("RTX_WAVE", 1u << 21), total_paths));
+    // wave bound: the queue holds W rays while paths remain to start and a
+    // path is queued at most max_depth times
+    const uint64_t max_iter64 = total_paths * max_depth / W + max_depth + 8;
+    RT_REQUIRE(max_iter64 < 0xFFFFFFFFull, "launch too large");
 
     for (int b = 0; b < 2; ++b) {
         for (int k = 0; k < 3; ++k) ws.q[b][k].reserve(size_t(W) * 16);
-        if (guides) for (int k = 3; k < 5; ++k) ws.q[b][k].reserve(size_t(W) * 16);
+        if (any_guides) for (int k = 3; k < 5; ++k) ws.q[b][k].reserve(size_t(W) * 16);
     }
     ws.hits.reserve(size_t(W) * 16);
-    ws.res_col.reserve(size_t(max_paths) * 16);
-    if (guides) {
-        ws.res_gn.reserve(size_t(max_paths) * 16);
-        ws.res_ga.reserve(size_t(max_paths) * 16);
-        ws.acc_n.reserve(size_t(npix) * 16);
-        ws.acc_a.reserve(size_t(npix) * 16);
-    }
-    ws.acc.reserve(size_t(npix) * 16);
-    ws.acc_rays.reserve(size_t(npix) * 4);
+    ws.acc.reserve(size_t(total_pix) * 28);   // 3 x u64 colour + u32 rays
+    if (any_guides) ws.acc_gd.reserve(size_t(total_pix) * 48);
+    ws.jobs.reserve(size_t(nj) * sizeof(JobDev));
     ws.state.reserve(sizeof(WaveState));
-    if (!ws.host_count) RT_CUDA(cudaMallocHost(&ws.host_count, 64));
+    if (!ws.host_state) RT_CUDA(cudaMallocHost(&ws.host_state, sizeof(WaveState)));
 
-    Queue q[2];
+    WaveLaunch L;
     for (int b = 0; b < 2; ++b) {
-        q[b].ori = ws.q[b][0].as<float4>();
-        q[b].dir = ws.q[b][1].as<float4>();
-        q[b].thr = ws.q[b][2].as<float4>();
-        q[b].gn = guides ? ws.q[b][3].as<float4>() : nullptr;
-        q[b].ga = guides ? ws.q[b][4].as<float4>() : nullptr;
+        L.qs.q[b].ori = ws.q[b][0].as<float4>();
+        L.qs.q[b].dir = ws.q[b][1].as<float4>();
+        L.qs.q[b].thr = ws.q[b][2].as<float4>();
+        L.qs.q[b].gn = any_guides ? ws.q[b][3].as<float4>() : nullptr;
+        L.qs.q[b].ga = any_guides ? ws.q[b][4].as<float4>() : nullptr;
     }
-    Results res{ws.res_col.as<float4>(), guides ? ws.res_gn.as<float4>() : nullptr,
-                guides ? ws.res_ga.as<float4>() : nullptr};
-    WaveState* st = ws.state.as<WaveState>();
-    RT_CUDA(cudaMemsetAsync(st, 0, sizeof(WaveState), s));
-
-    const float4* nodes = sc.nodes.as<float4>();
-    const float4* prims = sc.prims.as<float4>();
-    const ThingDev* things = sc.things_dev.as<ThingDev>();
-    uint32_t launches = 1, waves = 0, ext_launches = 0;
-    size_t ev = 0;
-    std::vector<std::pair<size_t, int>> timed;   // (event index, 0 extend / 1 shade)
-    const unsigned qgrid = grid_for(W);
-    const uint32_t kBatch = 8;
     const ExtendVariant& xv = kExtendVariants[extend_variant()];
-    const ExtendFn ext_fn = xv.fn[count ? 1 : 0];
-    const unsigned ext_grid = xv.persistent ? std::min<unsigned>(qgrid, resident_grid(ext_fn)) : qgrid;
-    float4* hits_buf = ws.hits.as<float4>();
-    uint32_t nprims = sc.nprims;
+    L.ext_fn = xv.fn[count ? 1 : 0];
+    L.qgrid = grid_for(W);
+    L.ext_grid = xv.persistent ? std::min<unsigned>(L.qgrid, resident_grid(L.ext_fn)) : L.qgrid;
+    L.hits = ws.hits.as<float4>();
+    L.st = ws.state.as<WaveState>();
+    L.jobs = ws.jobs.as<JobDev>();
+    L.nj = nj;
+    L.nodes = g.nodes.as<float4>();
+    L.prims = g.prims.as<float4>();
+    L.things = g.things_dev.as<ThingDev>();
+    {
+        unsigned long long* c = ws.acc.as<unsigned long long>();
+        for (int k = 0; k < 3; ++k) L.acc.col[k] = c + size_t(k) * total_pix;
+        L.acc.rays = reinterpret_cast<uint32_t*>(c + 3 * size_t(total_pix));
+        unsigned long long* gd = any_guides ? ws.acc_gd.as<unsigned long long>() : nullptr;
+        for (int k = 0; k < 6; ++k) L.acc.gd[k] = gd ? gd + size_t(k) * total_pix : nullptr;
+    }
+    L.any_guides = any_guides;
 
-    for (uint32_t s0 = 0; s0 < p.spp; s0 += chunk) {
-        const uint32_t ns = std::min(chunk, p.spp - s0);
-        a.sample_base = s0;
-        a.npaths = npix * ns;
-        const uint32_t n0 = std::min<uint32_t>(W, a.npaths);
-        k_set_state<<<1, 1, 0, s>>>(st, n0);
-        k_generate<<<grid_for(n0), kThreads, 0, s>>>(a, q[0], n0);
-        RT_CHECK_LAUNCH();
-        launches += 2;
-        // wave loop bound: while paths remain to start the queue holds n0 rays,
-        // and a path is queued at most `depth` times, so the loop ends within
-        // npaths*depth/n0 + depth iterations
-        const uint64_t max_iters = uint64_t(a.npaths) * a.depth / n0 + a.depth + 2 * kBatch;
-        uint32_t it = 0;
+    RT_CUDA(cudaMemcpyAsync(ws.jobs.p, ws.jobs_host.data(), size_t(nj) * sizeof(JobDev), cudaMemcpyHostToDevice, s));
+    RT_CUDA(cudaMemsetAsync(ws.acc.p, 0, size_t(total_pix) * 28, s));
+    if (any_guides) RT_CUDA(cudaMemsetAsync(ws.acc_gd.p, 0, size_t(total_pix) * 48, s));
+    const uint32_t n0 = W;
+    k_init_state<<<1, 1, 0, s>>>(L.st, n0, total_paths, uint32_t(max_iter64));
+    k_generate<<<grid_for(n0), kThreads, 0, s>>>(L.jobs, nj, L.qs.q[0], n0, any_guides);
+    RT_CHECK_LAUNCH();
+    uint32_t launches = 2;
+    std::vector<std::pair<size_t, int>> timed;   // (event index, 0 extend / 1 shade)
+
+    if (use_graph) {
+        const std::vector<const void*> key = {
+            reinterpret_cast<const void*>(L.ext_fn), reinterpret_cast<const void*>(uintptr_t(L.ext_grid)),
+            reinterpret_cast<const void*>(uintptr_t(L.qgrid)), L.qs.q[0].ori, L.qs.q[0].gn, L.qs.q[1].ori,
+            L.qs.q[1].gn, L.hits, L.st, L.jobs, reinterpret_cast<const void*>(uintptr_t(nj)), L.nodes, L.prims,
+            L.things, L.acc.col[0], L.acc.gd[0], reinterpret_cast<const void*>(uintptr_t(total_pix)),
+            reinterpret_cast<const void*>(uintptr_t(any_guides))};
+        if (!ws.graph.exec || ws.graph.key != key) {
+            build_wave_graph(ws, L);
+            ws.graph.key = key;
+        }
+        RT_CUDA(cudaGraphLaunch(ws.graph.exec, s));
+    } else {
+        size_t ev = 0;
+        const uint32_t kBatch = 8;
+        void* ext_args[] = {&L.qs, &L.hits, &L.st, &L.jobs, &L.nodes, &L.prims};
+        cudaGraphConditionalHandle no_handle = 0;
         while (true) {
-            for (uint32_t b = 0; b < kBatch; ++b, ++it) {
-                const int ci = int(it & 1u);
-                if (timing) {
+            for (uint32_t b = 0; b < kBatch; ++b) {
+                if (stage_timing) {
                     RT_CUDA(cudaEventRecord(ws.event(ev), s));
                     timed.push_back({ev, 0});
                     ev += 2;
                 }
-                {
-                    const float4* qo = q[ci].ori;
-                    const float4* qd = q[ci].dir;
-                    int cur = ci;
-                    void* args[] = {&qo, &qd, &hits_buf, &st, &cur, &nodes, &prims, &nprims};
-                    RT_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(ext_fn), dim3(ext_grid), dim3(kThreads),
-                                             args, 0, s));
-                }
-                if (timing) {
+                RT_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(L.ext_fn), dim3(L.ext_grid), dim3(kThreads),
+                                         ext_args, 0, s));
+                if (stage_timing) {
                     RT_CUDA(cudaEventRecord(ws.event(ev - 1), s));
                     RT_CUDA(cudaEventRecord(ws.event(ev), s));
                     timed.push_back({ev, 1});
                     ev += 2;
                 }
-                k_shade<<<qgrid, kThreads, 0, s>>>(a, q[ci], q[ci ^ 1], ws.hits.as<float4>(), st, ci, prims, things, res);
-                if (timing) RT_CUDA(cudaEventRecord(ws.event(ev - 1), s));
+                k_shade<<<L.qgrid, kThreads, 0, s>>>(L.qs, L.hits, L.st, L.jobs, nj, L.prims, L.things, L.acc,
+                                                      any_guides);
+                if (stage_timing) RT_CUDA(cudaEventRecord(ws.event(ev - 1), s));
+                k_wave_ctrl<<<1, 1, 0, s>>>(L.st, no_handle, 0);
                 RT_CHECK_LAUNCH();
-                launches += 2;
-                ext_launches += 1;
+                launches += 3;
             }
-            RT_CUDA(cudaMemcpyAsync(ws.host_count, &st->count[it & 1u], 4, cudaMemcpyDeviceToHost, s));
+            RT_CUDA(cudaMemcpyAsync(ws.host_state, L.st, sizeof(WaveState), cudaMemcpyDeviceToHost, s));
             RT_CUDA(cudaStreamSynchronize(s));
-            if (*ws.host_count == 0) break;
-            if (it > max_iters) throw Error(RT_ERR_LIMIT, "wave loop did not drain");
+            const WaveState& hs = *ws.host_state;
+            if (hs.count[hs.cur] == 0 || hs.err) break;
         }
-        waves += it;
-        k_accumulate<<<grid_for(npix), kThreads, 0, s>>>(res, npix, ns, s0 == 0 ? 1 : 0, guides ? 1 : 0,
-                                                          ws.acc.as<float4>(), ws.acc_rays.as<uint32_t>(),
-                                                          guides ? ws.acc_n.as<float4>() : nullptr,
-                                                          guides ? ws.acc_a.as<float4>() : nullptr);
-        RT_CHECK_LAUNCH();
-        launches += 1;
     }
-    k_finalize<<<grid_for(npix), kThreads, 0, s>>>(ws.acc.as<float4>(), ws.acc_rays.as<uint32_t>(),
-                                                    guides ? ws.acc_n.as<float4>() : nullptr,
-                                                    guides ? ws.acc_a.as<float4>() : nullptr, npix, p.spp, f.rawRGB,
-                                                    f.rpp, guides ? f.normals : nullptr, guides ? f.albedos : nullptr,
-                                                    st);
+    k_finalize<<<grid_for(total_pix), kThreads, 0, s>>>(L.jobs, nj, L.acc, uint32_t(total_pix), L.st);
     RT_CHECK_LAUNCH();
     launches += 1;
-    WaveState hs;
-    RT_CUDA(cudaMemcpyAsync(&hs, st, sizeof(hs), cudaMemcpyDeviceToHost, s));
+    RT_CUDA(cudaMemcpyAsync(ws.host_state, L.st, sizeof(WaveState), cudaMemcpyDeviceToHost, s));
     RT_CUDA(cudaStreamSynchronize(s));
-    if (hs.err) throw Error(RT_ERR_LIMIT, "traversal stack overflow (LBVH deeper than the stack)");
+    const WaveState hs = *ws.host_state;
+    if (hs.err & 1u) throw Error(RT_ERR_LIMIT, "traversal stack overflow (LBVH deeper than the stack)");
+    if (hs.err & 2u) throw Error(RT_ERR_LIMIT, "wave loop exceeded its bound");
+    if (use_graph) launches += 3 * hs.iter;
     if (stats) {
         std::memset(stats, 0, sizeof(*stats));
         stats->rays = hs.rays;
-        stats->paths = uint64_t(npix) * p.spp;
+        stats->paths = total_paths;
         stats->node_visits = hs.nodes;
         stats->prim_tests = hs.prims;
-        stats->waves = waves;
+        stats->waves = hs.iter;
         stats->kernel_launches = launches;
-        stats->extend_launches = ext_launches;
+        stats->extend_launches = hs.iter;
         stats->wave_capacity = W;
-        if (timing) {
-            for (auto& tv : timed) {
-                float ms = 0.f;
-                RT_CUDA(cudaEventElapsedTime(&ms, ws.event(tv.first), ws.event(tv.first + 1)));
-                (tv.second == 0 ? stats->extend_ms : stats->shade_ms) += ms;
-            }
+        for (auto& tv : timed) {
+            float ms = 0.f;
+            RT_CUDA(cudaEventElapsedTime(&ms, ws.event(tv.first), ws.event(tv.first + 1)));
+            (tv.second == 0 ? stats->extend_ms : stats->shade_ms) += ms;
         }
+        if (!timed.empty()) stats->extend_launches = uint32_t(timed.size() / 2);
     }
 }
+
+namespace {
 
 void first_hit_rect(Scene& sc, const rt_camera& cam, const rt_launch_params& p, uint32_t sample, uint32_t x0,
                     uint32_t y0, uint32_t nx, uint32_t ny, int* prim, int* thing, float* t, float* u, float* v,
@@ -769,17 +919,39 @@ void first_hit_rect(Scene& sc, const rt_camera& cam, const rt_launch_params& p, 
     check_params(&p);
     if (!sc.built || sc.topology_dirty || sc.xf_dirty) throw Error(RT_ERR_NOT_BUILT, "scene not built or not updated");
     RT_REQUIRE(prim != nullptr, "prim is NULL");
-    const RenderArgs a = make_args(cam, p);
-    uint32_t* err = sc.misc.as<uint32_t>();
+    FirstHitArgs a{};
+    a.cam = cam_dev(cam);
+    a.W = p.image_w;
+    a.H = p.image_h;
+    a.seed = p.seed;
+    a.key1 = 0;
+    a.sample = sample;
+    a.x0 = x0;
+    a.y0 = y0;
+    a.nx = nx;
+    a.ny = ny;
+    a.root = sc.geo.root(0);
+    uint32_t* err = sc.geo.misc.as<uint32_t>();
     RT_CUDA(cudaMemsetAsync(err, 0, 4, s));
-    k_first_hit<<<grid_for(uint64_t(nx) * ny), kThreads, 0, s>>>(a, sample, x0, y0, nx, ny, sc.nodes.as<float4>(),
-                                                                  sc.prims.as<float4>(), sc.nprims, prim, thing, t, u, v,
-                                                                  t64, err);
+    k_first_hit<<<grid_for(uint64_t(nx) * ny), kThreads, 0, s>>>(a, sc.geo.nodes.as<float4>(), sc.geo.prims.as<float4>(),
+                                                                  prim, thing, t, u, v, t64, err);
     RT_CHECK_LAUNCH();
     uint32_t herr = 0;
     RT_CUDA(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, s));
     RT_CUDA(cudaStreamSynchronize(s));
     if (herr) throw Error(RT_ERR_LIMIT, "traversal stack overflow (LBVH deeper than the stack)");
+}
+
+void render_scene(Scene& sc, const rt_camera& cam, const rt_launch_params& p, const rt_frame& f, cudaStream_t s,
+                  rt_launch_stats* stats) {
+    if (!sc.built || sc.topology_dirty) throw Error(RT_ERR_NOT_BUILT, "scene not built (call rt_scene_build)");
+    if (sc.xf_dirty) throw Error(RT_ERR_NOT_BUILT, "transforms changed; call rt_scene_update");
+    std::vector<Job> jobs(1);
+    jobs[0].seg = 0;
+    jobs[0].cam = cam;
+    jobs[0].params = p;
+    jobs[0].frame = f;
+    render_jobs(sc.geo, jobs, s, stats);
 }
 
 void postproc(const rt_float3* src, rt_uchar4* dst, int w, int h, int mode, cudaStream_t s) {
@@ -812,6 +984,19 @@ Launcher* launcher_from(rt_launcher l) {
     return reinterpret_cast<Launcher*>(l);
 }
 
+// Many scenes rendered by one wavefront over one segmented geometry.
+struct Batch {
+    std::vector<Scene*> scenes;
+    std::vector<Job> jobs;
+    Geometry geo;
+    bool built = false;
+};
+
+Batch* batch_from(rt_batch b) {
+    RT_REQUIRE(b != nullptr, "batch handle is NULL");
+    return reinterpret_cast<Batch*>(b);
+}
+
 }  // namespace
 }  // namespace rt
 
@@ -823,7 +1008,7 @@ rt_status rt_launch(rt_scene scene, const rt_camera* cam, const rt_launch_params
                     void* stream) {
     return guarded([&] {
         RT_REQUIRE(cam && params && frame, "cam/params/frame is NULL");
-        render(*scene_from(scene), *cam, *params, *frame, as_stream(stream), nullptr);
+        render_scene(*scene_from(scene), *cam, *params, *frame, as_stream(stream), nullptr);
     });
 }
 
@@ -831,7 +1016,7 @@ rt_status rt_launch_ex(rt_scene scene, const rt_camera* cam, const rt_launch_par
                        void* stream, rt_launch_stats* stats) {
     return guarded([&] {
         RT_REQUIRE(cam && params && frame && stats, "cam/params/frame/stats is NULL");
-        render(*scene_from(scene), *cam, *params, *frame, as_stream(stream), stats);
+        render_scene(*scene_from(scene), *cam, *params, *frame, as_stream(stream), stats);
     });
 }
 
@@ -917,7 +1102,7 @@ rt_status rt_launcher_ignite(rt_launcher l, rt_scene scene, const rt_camera* cam
             return;
         }
         rt_frame f{L->raw.as<rt_float3>(), L->rpp.as<unsigned>(), L->nrm.as<rt_float3>(), L->alb.as<rt_float3>()};
-        render(sc, *cam, *params, f, s, stats);
+        render_scene(sc, *cam, *params, f, s, stats);
         postproc(L->raw.as<rt_float3>(), L->img.as<rt_uchar4>(), int(L->w), int(L->h), 1, s);
         RT_CUDA(cudaStreamSynchronize(s));
     });
@@ -944,6 +1129,70 @@ rt_status rt_launcher_download(rt_launcher l, rt_float3* rawRGB, unsigned int* r
         if (albedos) RT_CUDA(cudaMemcpy(albedos, L->alb.p, n * 12, cudaMemcpyDeviceToHost));
         if (image) RT_CUDA(cudaMemcpy(image, L->img.p, n * 4, cudaMemcpyDeviceToHost));
         if (pick_id) RT_CUDA(cudaMemcpy(pick_id, L->pick.p, 4, cudaMemcpyDeviceToHost));
+    });
+}
+
+rt_status rt_batch_create(rt_batch* out) {
+    return guarded([&] {
+        RT_REQUIRE(out != nullptr, "out is NULL");
+        *out = reinterpret_cast<rt_batch>(new Batch());
+    });
+}
+
+rt_status rt_batch_destroy(rt_batch b) {
+    return guarded([&] {
+        if (b) delete reinterpret_cast<Batch*>(b);
+    });
+}
+
+rt_status rt_batch_add(rt_batch b, rt_scene scene, const rt_camera* cam, const rt_launch_params* params,
+                       const rt_frame* frame, unsigned int* index) {
+    return guarded([&] {
+        Batch* B = batch_from(b);
+        Scene* sc = scene_from(scene);
+        RT_REQUIRE(cam && params && frame, "cam/params/frame is NULL");
+        check_params(params);
+        RT_REQUIRE(frame->rawRGB != nullptr, "frame.rawRGB is NULL");
+        if (params->flags & RT_FLAG_GUIDES)
+            RT_REQUIRE(frame->normals && frame->albedos, "RT_FLAG_GUIDES needs frame.normals and frame.albedos");
+        Job j;
+        j.seg = uint32_t(B->scenes.size());
+        j.cam = *cam;
+        j.params = *params;
+        j.frame = *frame;
+        B->scenes.push_back(sc);
+        B->jobs.push_back(j);
+        B->built = false;
+        if (index) *index = j.seg;
+    });
+}
+
+rt_status rt_batch_build(rt_batch b, unsigned int morton_bits, void* stream) {
+    return guarded([&] {
+        Batch* B = batch_from(b);
+        RT_REQUIRE(!B->scenes.empty(), "batch is empty");
+        build_geometry(B->geo, B->scenes, int(morton_bits), as_stream(stream));
+        B->built = true;
+    });
+}
+
+rt_status rt_batch_launch(rt_batch b, void* stream, rt_launch_stats* stats) {
+    return guarded([&] {
+        Batch* B = batch_from(b);
+        if (!B->built) throw Error(RT_ERR_NOT_BUILT, "batch not built (call rt_batch_build)");
+        rt_launch_stats st{};
+        render_jobs(B->geo, B->jobs, as_stream(stream), stats ? stats : &st);
+    });
+}
+
+rt_status rt_batch_info(rt_batch b, unsigned int* n_scenes, unsigned int* n_prims, float* build_ms,
+                        unsigned long long* device_bytes) {
+    return guarded([&] {
+        Batch* B = batch_from(b);
+        if (n_scenes) *n_scenes = unsigned(B->scenes.size());
+        if (n_prims) *n_prims = B->geo.nprims;
+        if (build_ms) *build_ms = B->geo.build_ms;
+        if (device_bytes) *device_bytes = B->geo.device_bytes();
     });
 }
 

@@ -117,11 +117,12 @@ __global__ void k_emit_mesh(const float3* __restrict__ pts, const uint32_t* __re
 }
 
 // ------------------------------------------------------------- flattening
+// One thread per global primitive: the owning thing is the last one whose
+// prim_offset <= pid; triangles are transformed to world space.
 __global__ void k_flatten(const FlatDesc* __restrict__ desc, uint32_t nthings, uint32_t nprims,
-                          float4* __restrict__ out) {
+                          float4* __restrict__ out, uint32_t* __restrict__ prim_seg) {
     const uint32_t pid = blockIdx.x * blockDim.x + threadIdx.x;
     if (pid >= nprims) return;
-    // last thing whose prim_offset <= pid
     uint32_t lo = 0, hi = nthings;
     while (hi - lo > 1) {
         const uint32_t mid = (lo + hi) >> 1;
@@ -129,6 +130,7 @@ __global__ void k_flatten(const FlatDesc* __restrict__ desc, uint32_t nthings, u
     }
     const FlatDesc& d = desc[lo];
     const uint32_t thing = lo;
+    if (prim_seg) prim_seg[pid] = d.seg;
     float4* o = out + 3 * size_t(pid);
     if (d.analytic) {
         o[0] = make_float4(d.sphere.x, d.sphere.y, d.sphere.z, __uint_as_float(thing));
@@ -167,7 +169,7 @@ __device__ __forceinline__ Box3 prim_box(const float4* __restrict__ rec) {
 
 __device__ __forceinline__ float3 centroid(const Box3& b) { return mul(0.5f, add(b.lo, b.hi)); }
 
-__device__ __forceinline__ uint32_t ford(float f) {   // float -> orderable u32 (no -0 folding needed for min/max)
+__device__ __forceinline__ uint32_t ford(float f) {   // float -> order-preserving u32
     const uint32_t b = __float_as_uint(f);
     return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
 }
@@ -175,25 +177,50 @@ __device__ __forceinline__ float fdeord(uint32_t o) {
     return __uint_as_float((o & 0x80000000u) ? (o & 0x7FFFFFFFu) : ~o);
 }
 
-__global__ void k_init_bounds(uint32_t* b) {
-    if (threadIdx.x < 3) b[threadIdx.x] = 0xFFFFFFFFu;       // min
-    else if (threadIdx.x < 6) b[threadIdx.x] = 0u;          // max
+__global__ void k_init_bounds(uint32_t* b, uint32_t nsegs) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 6 * nsegs) return;
+    b[i] = (i % 6) < 3 ? 0xFFFFFFFFu : 0u;   // min slots start high, max slots low
 }
 
-__global__ void k_centroid_bounds(const float4* __restrict__ prims, uint32_t n, uint32_t* __restrict__ bounds) {
-    __shared__ uint32_t s[6];
-    if (threadIdx.x < 3) s[threadIdx.x] = 0xFFFFFFFFu;
-    else if (threadIdx.x < 6) s[threadIdx.x] = 0u;
-    __syncthreads();
+// Centroid bounds per segment: a warp whose primitives share one segment
+// reduces in registers and issues six atomics; a mixed warp (segment border)
+// issues them per lane.
+__global__ void k_centroid_bounds(const float4* __restrict__ prims, const uint32_t* __restrict__ prim_seg,
+                                  uint32_t n, uint32_t* __restrict__ bounds) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) {
+    const bool valid = i < n;
+    uint32_t v[6] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u};
+    uint32_t seg = 0;
+    if (valid) {
         const float3 c = centroid(prim_box(prims + 3 * size_t(i)));
-        atomicMin(&s[0], ford(c.x)); atomicMin(&s[1], ford(c.y)); atomicMin(&s[2], ford(c.z));
-        atomicMax(&s[3], ford(c.x)); atomicMax(&s[4], ford(c.y)); atomicMax(&s[5], ford(c.z));
+        v[0] = v[3] = ford(c.x);
+        v[1] = v[4] = ford(c.y);
+        v[2] = v[5] = ford(c.z);
+        seg = prim_seg ? prim_seg[i] : 0u;
     }
-    __syncthreads();
-    if (threadIdx.x < 3) atomicMin(&bounds[threadIdx.x], s[threadIdx.x]);
-    else if (threadIdx.x < 6) atomicMax(&bounds[threadIdx.x], s[threadIdx.x]);
+    const uint32_t vmask = __ballot_sync(0xFFFFFFFFu, valid);
+    if (!vmask) return;
+    const uint32_t seg0 = __shfl_sync(0xFFFFFFFFu, seg, __ffs(vmask) - 1);
+    const bool uniform = __all_sync(0xFFFFFFFFu, !valid || seg == seg0);
+    if (uniform) {
+        for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+            for (int k = 0; k < 6; ++k) {
+                const uint32_t w = __shfl_down_sync(0xFFFFFFFFu, v[k], o);
+                v[k] = k < 3 ? min(v[k], w) : max(v[k], w);
+            }
+        }
+        if ((threadIdx.x & 31u) == 0) {
+            uint32_t* b = bounds + 6 * seg0;
+            atomicMin(&b[0], v[0]); atomicMin(&b[1], v[1]); atomicMin(&b[2], v[2]);
+            atomicMax(&b[3], v[3]); atomicMax(&b[4], v[4]); atomicMax(&b[5], v[5]);
+        }
+    } else if (valid) {
+        uint32_t* b = bounds + 6 * seg;
+        atomicMin(&b[0], v[0]); atomicMin(&b[1], v[1]); atomicMin(&b[2], v[2]);
+        atomicMax(&b[3], v[3]); atomicMax(&b[4], v[4]); atomicMax(&b[5], v[5]);
+    }
 }
 
 __device__ __forceinline__ uint32_t expand10(uint32_t x) {
@@ -220,12 +247,13 @@ __device__ __forceinline__ float quantf(float c, float lo, float ext, float cell
 }
 
 template <class K>
-__global__ void k_morton(const float4* __restrict__ prims, uint32_t n, const uint32_t* __restrict__ bounds,
-                         K* __restrict__ codes, uint32_t* __restrict__ ids) {
+__global__ void k_morton(const float4* __restrict__ prims, const uint32_t* __restrict__ prim_seg, uint32_t n,
+                         const uint32_t* __restrict__ bounds, K* __restrict__ codes, uint32_t* __restrict__ ids) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const float3 lo = mk(fdeord(bounds[0]), fdeord(bounds[1]), fdeord(bounds[2]));
-    const float3 hi = mk(fdeord(bounds[3]), fdeord(bounds[4]), fdeord(bounds[5]));
+    const uint32_t* b = bounds + 6 * (prim_seg ? prim_seg[i] : 0u);
+    const float3 lo = mk(fdeord(b[0]), fdeord(b[1]), fdeord(b[2]));
+    const float3 hi = mk(fdeord(b[3]), fdeord(b[4]), fdeord(b[5]));
     const float3 ext = sub(hi, lo);
     const float3 c = centroid(prim_box(prims + 3 * size_t(i)));
     if (sizeof(K) == 4) {
@@ -242,7 +270,28 @@ __global__ void k_morton(const float4* __restrict__ prims, uint32_t n, const uin
     ids[i] = i;
 }
 
-// Karras 2012 (equal keys fall back to the index bits, 64 + clz(i ^ j)).
+// Segment ids of the code-sorted primitives, and the identity permutation.
+__global__ void k_seg_keys(const uint32_t* __restrict__ prim_seg, const uint32_t* __restrict__ ids, uint32_t n,
+                           uint32_t* __restrict__ keys, uint32_t* __restrict__ perm) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    keys[i] = prim_seg[ids[i]];
+    perm[i] = i;
+}
+
+template <class K>
+__global__ void k_permute(const K* __restrict__ codes_in, const uint32_t* __restrict__ ids_in,
+                          const uint32_t* __restrict__ perm, uint32_t n, K* __restrict__ codes_out,
+                          uint32_t* __restrict__ ids_out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    codes_out[i] = codes_in[perm[i]];
+    ids_out[i] = ids_in[perm[i]];
+}
+
+// Karras 2012 over one segment's sorted codes (local indices, so a segment's
+// hierarchy is the one a standalone build of that scene gives); equal keys
+// fall back to the index bits, 64 + clz(i ^ j).
 template <class K>
 __device__ __forceinline__ int kdelta(const K* __restrict__ k, int n, int i, int j) {
     if (j < 0 || j >= n) return -1;
@@ -251,11 +300,35 @@ __device__ __forceinline__ int kdelta(const K* __restrict__ k, int n, int i, int
     return 64 + __clz(i ^ j);
 }
 
+__device__ __forceinline__ uint32_t seg_of(const SegDev* __restrict__ segs, uint32_t nsegs, uint32_t pos) {
+    uint32_t lo = 0, hi = nsegs;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (segs[mid].prim_begin <= pos) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// One thread per node slot.  Slot P + i (i < n - 1) of a segment starting at
+// P with n primitives is its internal node i; a one-primitive segment puts its
+// leaf in both child slots of node P (marked for the refit by parent -2).
 template <class K>
-__global__ void k_karras(const K* __restrict__ k, int n, float4* __restrict__ nodes, int* __restrict__ parent_leaf,
-                         int* __restrict__ parent_int) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n - 1) return;
+__global__ void k_karras(const K* __restrict__ codes, const SegDev* __restrict__ segs, uint32_t nsegs, uint32_t ntot,
+                         float4* __restrict__ nodes, int* __restrict__ parent_leaf, int* __restrict__ parent_int) {
+    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= ntot) return;
+    const SegDev sg = segs[seg_of(segs, nsegs, slot)];
+    const int n = int(sg.prim_count);
+    const int i = int(slot - sg.prim_begin);
+    const int P = int(sg.prim_begin);
+    if (n == 1) {
+        nodes[4 * size_t(P) + 3] = make_float4(__int_as_float(~P), __int_as_float(~P), 0.f, 0.f);
+        parent_leaf[P] = -2;
+        parent_int[P] = -1;
+        return;
+    }
+    if (i >= n - 1) return;   // the spare slot of the segment
+    const K* k = codes + P;
     const int d = (kdelta(k, n, i, i + 1) - kdelta(k, n, i, i - 1)) >= 0 ? 1 : -1;
     const int dmin = kdelta(k, n, i, i - d);
     int lmax = 2;
@@ -273,12 +346,12 @@ __global__ void k_karras(const K* __restrict__ k, int n, float4* __restrict__ no
     } while (t > 1);
     const int gamma = i + s * d + (d < 0 ? -1 : 0);
     const int lo = min(i, j), hi = max(i, j);
-    const int left = (lo == gamma) ? ~gamma : gamma;
-    const int right = (hi == gamma + 1) ? ~(gamma + 1) : gamma + 1;
-    nodes[4 * size_t(i) + 3] = make_float4(__int_as_float(left), __int_as_float(right), 0.f, 0.f);
-    if (left < 0) parent_leaf[~left] = i; else parent_int[left] = i;
-    if (right < 0) parent_leaf[~right] = i; else parent_int[right] = i;
-    if (i == 0) parent_int[0] = -1;
+    const int left = (lo == gamma) ? ~(P + gamma) : P + gamma;
+    const int right = (hi == gamma + 1) ? ~(P + gamma + 1) : P + gamma + 1;
+    nodes[4 * size_t(P + i) + 3] = make_float4(__int_as_float(left), __int_as_float(right), 0.f, 0.f);
+    if (left < 0) parent_leaf[~left] = P + i; else parent_int[left] = P + i;
+    if (right < 0) parent_leaf[~right] = P + i; else parent_int[right] = P + i;
+    if (i == 0) parent_int[P] = -1;
 }
 
 __global__ void k_gather_prims(const float4* __restrict__ flat, const uint32_t* __restrict__ ids, uint32_t n,
@@ -311,8 +384,13 @@ __global__ void k_refit(const float4* __restrict__ prims, uint32_t n, float4* no
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     Box3 b = prim_box(prims + 3 * size_t(i));
-    int child = ~int(i);
     int p = parent_leaf[i];
+    if (p == -2) {   // one-primitive segment: the root holds the leaf twice
+        write_child_box(nodes + 4 * size_t(i), 0, b);
+        write_child_box(nodes + 4 * size_t(i), 1, b);
+        return;
+    }
+    int child = ~int(i);
     while (p >= 0) {
         const float4 n3 = __ldcg(nodes + 4 * size_t(p) + 3);
         const int slot = (__float_as_int(n3.x) == child) ? 0 : 1;
@@ -331,22 +409,12 @@ __global__ void k_refit(const float4* __restrict__ prims, uint32_t n, float4* no
     }
 }
 
-// Single-primitive scene: node 0 holds the one leaf in both slots.
-__global__ void k_single_leaf(const float4* __restrict__ prims, float4* __restrict__ nodes) {
-    const Box3 b = prim_box(prims);
-    write_child_box(nodes, 0, b);
-    write_child_box(nodes, 1, b);
-    nodes[3] = make_float4(__int_as_float(~0), __int_as_float(~0), 0.f, 0.f);
-}
-
 __global__ void k_lbvh_snapshot_codes32(const uint32_t* __restrict__ c, uint32_t n, unsigned long long* __restrict__ o) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) o[i] = c[i];
 }
 
 // ------------------------------------------------------------- host side
-inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
-
 void check_optics(const rt_optics* o) {
     RT_REQUIRE(o != nullptr, "optics is NULL");
     RT_REQUIRE(o->type >= RT_OPTICS_DIFFUSE && o->type <= RT_OPTICS_REFRACT, "unknown optics type");
@@ -373,135 +441,199 @@ ThingDev thing_dev(const ThingHost& th) {
     return d;
 }
 
-// Uploads things + flattening descriptors and flattens into prims_flat.
-void flatten(Scene& sc, cudaStream_t s) {
-    const uint32_t nt = uint32_t(sc.things.size());
-    std::vector<FlatDesc> desc(nt);
-    std::vector<ThingDev> td(nt);
+// Uploads things + flattening descriptors of all scenes and flattens into
+// g.prims_flat (primitive-id order, segment after segment).
+void flatten(Geometry& g, const std::vector<Scene*>& scenes, cudaStream_t s) {
+    std::vector<FlatDesc> desc;
+    std::vector<ThingDev> td;
+    g.seg_host.assign(scenes.size(), SegDev{0, 0});
+    g.thing_begin.assign(scenes.size(), 0);
     uint64_t off = 0;
-    for (uint32_t k = 0; k < nt; ++k) {
-        const ThingHost& th = sc.things[k];
-        FlatDesc& d = desc[k];
-        std::memset(&d, 0, sizeof(d));
-        d.prim_offset = uint32_t(off);
-        if (th.mesh < 0) {
-            d.analytic = 1;
-            d.nprims = 1;
-            d.sphere = make_float4(th.center.x, th.center.y, th.center.z, th.radius);
-        } else {
-            const MeshDev& m = sc.meshes[th.mesh];
-            d.v = m.v.as<float3>();
-            d.idx = m.i.as<uint3>();
-            d.nprims = m.ni;
-            std::memcpy(d.T, th.T, sizeof(d.T));
+    for (size_t si = 0; si < scenes.size(); ++si) {
+        const Scene& sc = *scenes[si];
+        g.seg_host[si].prim_begin = uint32_t(off);
+        g.thing_begin[si] = uint32_t(desc.size());
+        for (const ThingHost& th : sc.things) {
+            FlatDesc d;
+            std::memset(&d, 0, sizeof(d));
+            d.prim_offset = uint32_t(off);
+            d.seg = uint32_t(si);
+            if (th.mesh < 0) {
+                d.analytic = 1;
+                d.nprims = 1;
+                d.sphere = make_float4(th.center.x, th.center.y, th.center.z, th.radius);
+            } else {
+                const MeshDev& m = sc.meshes[th.mesh];
+                d.v = m.v.as<float3>();
+                d.idx = m.i.as<uint3>();
+                d.nprims = m.ni;
+                std::memcpy(d.T, th.T, sizeof(d.T));
+            }
+            off += d.nprims;
+            RT_REQUIRE(off < (uint64_t(1) << 31), "too many primitives (>= 2^31)");
+            desc.push_back(d);
+            td.push_back(thing_dev(th));
         }
-        off += d.nprims;
-        td[k] = thing_dev(th);
+        g.seg_host[si].prim_count = uint32_t(off) - g.seg_host[si].prim_begin;
     }
-    RT_REQUIRE(off < (uint64_t(1) << 31), "scene has too many primitives (>= 2^31)");
-    sc.nprims = uint32_t(off);
-    sc.desc.reserve(std::max<size_t>(1, nt) * sizeof(FlatDesc));
-    sc.things_dev.reserve(std::max<size_t>(1, nt) * sizeof(ThingDev));
-    if (nt) {
-        RT_CUDA(cudaMemcpyAsync(sc.desc.p, desc.data(), nt * sizeof(FlatDesc), cudaMemcpyHostToDevice, s));
-        RT_CUDA(cudaMemcpyAsync(sc.things_dev.p, td.data(), nt * sizeof(ThingDev), cudaMemcpyHostToDevice, s));
+    g.nprims = uint32_t(off);
+    g.nthings = uint32_t(desc.size());
+    g.nsegs = uint32_t(scenes.size());
+    g.desc.reserve(std::max<size_t>(1, desc.size()) * sizeof(FlatDesc));
+    g.things_dev.reserve(std::max<size_t>(1, td.size()) * sizeof(ThingDev));
+    g.segs.reserve(std::max<size_t>(1, g.seg_host.size()) * sizeof(SegDev));
+    if (!desc.empty()) {
+        RT_CUDA(cudaMemcpyAsync(g.desc.p, desc.data(), desc.size() * sizeof(FlatDesc), cudaMemcpyHostToDevice, s));
+        RT_CUDA(cudaMemcpyAsync(g.things_dev.p, td.data(), td.size() * sizeof(ThingDev), cudaMemcpyHostToDevice, s));
     }
-    sc.prims_flat.reserve(std::max<size_t>(1, sc.nprims) * 48);
-    if (sc.nprims) {
-        k_flatten<<<grid_for(sc.nprims), kThreads, 0, s>>>(sc.desc.as<FlatDesc>(), nt, sc.nprims,
-                                                            sc.prims_flat.as<float4>());
+    if (!g.seg_host.empty())
+        RT_CUDA(cudaMemcpyAsync(g.segs.p, g.seg_host.data(), g.seg_host.size() * sizeof(SegDev),
+                                cudaMemcpyHostToDevice, s));
+    g.prims_flat.reserve(std::max<size_t>(1, g.nprims) * 48);
+    if (g.nsegs > 1) g.prim_seg.reserve(std::max<size_t>(1, g.nprims) * 4);
+    if (g.nprims) {
+        k_flatten<<<grid_for(g.nprims), kThreads, 0, s>>>(g.desc.as<FlatDesc>(), g.nthings, g.nprims,
+                                                           g.prims_flat.as<float4>(),
+                                                           g.nsegs > 1 ? g.prim_seg.as<uint32_t>() : nullptr);
         RT_CHECK_LAUNCH();
     }
-    // host copies of desc/td must outlive the async copies
-    RT_CUDA(cudaStreamSynchronize(s));
+    RT_CUDA(cudaStreamSynchronize(s));   // the host staging vectors must outlive the copies
 }
 
-void refit(Scene& sc, cudaStream_t s) {
-    const uint32_t n = sc.nprims;
+void refit(Geometry& g, cudaStream_t s) {
+    const uint32_t n = g.nprims;
     if (n == 0) return;
-    k_gather_prims<<<grid_for(n), kThreads, 0, s>>>(sc.prims_flat.as<float4>(), sc.ids.as<uint32_t>(), n,
-                                                     sc.prims.as<float4>());
+    k_gather_prims<<<grid_for(n), kThreads, 0, s>>>(g.prims_flat.as<float4>(), g.ids.as<uint32_t>(), n,
+                                                     g.prims.as<float4>());
     RT_CHECK_LAUNCH();
-    if (n == 1) {
-        k_single_leaf<<<1, 1, 0, s>>>(sc.prims.as<float4>(), sc.nodes.as<float4>());
-        RT_CHECK_LAUNCH();
-        return;
-    }
-    int* parents = sc.parents.as<int>();
-    RT_CUDA(cudaMemsetAsync(sc.flags.p, 0, size_t(n - 1) * sizeof(uint32_t), s));
-    k_refit<<<grid_for(n), kThreads, 0, s>>>(sc.prims.as<float4>(), n, sc.nodes.as<float4>(), parents,
-                                              parents + n, sc.flags.as<uint32_t>());
+    int* parents = g.parents.as<int>();
+    RT_CUDA(cudaMemsetAsync(g.flags.p, 0, size_t(n) * sizeof(uint32_t), s));
+    k_refit<<<grid_for(n), kThreads, 0, s>>>(g.prims.as<float4>(), n, g.nodes.as<float4>(), parents, parents + n,
+                                              g.flags.as<uint32_t>());
     RT_CHECK_LAUNCH();
 }
 
 template <class K>
-void build_topology(Scene& sc, cudaStream_t s) {
-    const uint32_t n = sc.nprims;
-    sc.codes.reserve(size_t(n) * sizeof(K));
-    sc.ids.reserve(size_t(n) * sizeof(uint32_t));
-    K* codes = sc.codes.as<K>();
-    uint32_t* ids = sc.ids.as<uint32_t>();
-    k_morton<K><<<grid_for(n), kThreads, 0, s>>>(sc.prims_flat.as<float4>(), n, sc.bounds.as<uint32_t>(), codes, ids);
+void build_topology(Geometry& g, cudaStream_t s) {
+    const uint32_t n = g.nprims;
+    g.codes.reserve(size_t(n) * sizeof(K));
+    g.ids.reserve(size_t(n) * sizeof(uint32_t));
+    K* codes = g.codes.as<K>();
+    uint32_t* ids = g.ids.as<uint32_t>();
+    const uint32_t* pseg = g.nsegs > 1 ? g.prim_seg.as<uint32_t>() : nullptr;
+    k_morton<K><<<grid_for(n), kThreads, 0, s>>>(g.prims_flat.as<float4>(), pseg, n, g.bounds.as<uint32_t>(), codes,
+                                                  ids);
     RT_CHECK_LAUNCH();
     if (sizeof(K) == 4)
-        radix_sort_pairs_u32(reinterpret_cast<uint32_t*>(codes), ids, n, sc.morton_bits, sc.sort_tmp, s);
+        radix_sort_pairs_u32(reinterpret_cast<uint32_t*>(codes), ids, n, g.morton_bits, g.sort_tmp, s);
     else
-        radix_sort_pairs_u64(reinterpret_cast<unsigned long long*>(codes), ids, n, sc.morton_bits, sc.sort_tmp, s);
-    if (n > 1) {
-        int* parents = sc.parents.as<int>();
-        k_karras<K><<<grid_for(n - 1), kThreads, 0, s>>>(codes, int(n), sc.nodes.as<float4>(), parents, parents + n);
+        radix_sort_pairs_u64(reinterpret_cast<unsigned long long*>(codes), ids, n, g.morton_bits, g.sort_tmp, s);
+    if (g.nsegs > 1) {
+        // stable second pass by segment: (segment, code) order
+        int seg_bits = 1;
+        while ((1u << seg_bits) < g.nsegs) ++seg_bits;
+        const size_t kb = size_t(n) * sizeof(K);
+        g.seg_tmp.reserve(2 * size_t(n) * 4 + kb + size_t(n) * 4);
+        uint32_t* keys = g.seg_tmp.as<uint32_t>();
+        uint32_t* perm = keys + n;
+        K* codes2 = reinterpret_cast<K*>(perm + n);
+        uint32_t* ids2 = reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(codes2) + kb);
+        k_seg_keys<<<grid_for(n), kThreads, 0, s>>>(pseg, ids, n, keys, perm);
         RT_CHECK_LAUNCH();
+        radix_sort_pairs_u32(keys, perm, n, seg_bits, g.sort_tmp, s);
+        k_permute<K><<<grid_for(n), kThreads, 0, s>>>(codes, ids, perm, n, codes2, ids2);
+        RT_CHECK_LAUNCH();
+        RT_CUDA(cudaMemcpyAsync(codes, codes2, kb, cudaMemcpyDeviceToDevice, s));
+        RT_CUDA(cudaMemcpyAsync(ids, ids2, size_t(n) * 4, cudaMemcpyDeviceToDevice, s));
     }
+    int* parents = g.parents.as<int>();
+    k_karras<K><<<grid_for(n), kThreads, 0, s>>>(codes, g.segs.as<SegDev>(), g.nsegs, n, g.nodes.as<float4>(), parents,
+                                                  parents + n);
+    RT_CHECK_LAUNCH();
 }
 
-void build(Scene& sc, int morton_bits, cudaStream_t s) {
+}  // namespace
+
+void build_geometry(Geometry& g, const std::vector<Scene*>& scenes, int morton_bits, cudaStream_t s) {
     RT_REQUIRE(morton_bits == 0 || morton_bits == 30 || morton_bits == 60, "morton_bits must be 0, 30 or 60");
-    sc.morton_bits = morton_bits == 0 ? 60 : morton_bits;
+    RT_REQUIRE(!scenes.empty(), "no scenes to build");
+    g.morton_bits = morton_bits == 0 ? 60 : morton_bits;
     cudaEvent_t e0, e1;
     RT_CUDA(cudaEventCreate(&e0));
     RT_CUDA(cudaEventCreate(&e1));
     RT_CUDA(cudaEventRecord(e0, s));
-    flatten(sc, s);
-    const uint32_t n = sc.nprims;
-    sc.prims.reserve(std::max<size_t>(1, n) * 48);
-    sc.nodes.reserve(std::max<size_t>(1, n > 1 ? n - 1 : 1) * 64);
-    sc.parents.reserve((size_t(n) * 2 + 1) * sizeof(int));
-    sc.flags.reserve(std::max<size_t>(1, n) * sizeof(uint32_t));
-    sc.bounds.reserve(6 * sizeof(uint32_t));
-    sc.misc.reserve(256);
+    flatten(g, scenes, s);
+    const uint32_t n = g.nprims;
+    g.prims.reserve(std::max<size_t>(1, n) * 48);
+    g.nodes.reserve(std::max<size_t>(1, n) * 64);
+    g.parents.reserve((size_t(n) * 2 + 1) * sizeof(int));
+    g.flags.reserve(std::max<size_t>(1, n) * sizeof(uint32_t));
+    g.bounds.reserve(size_t(g.nsegs) * 6 * sizeof(uint32_t));
+    g.misc.reserve(256);
     if (n > 0) {
-        k_init_bounds<<<1, 32, 0, s>>>(sc.bounds.as<uint32_t>());
+        k_init_bounds<<<grid_for(6 * g.nsegs), kThreads, 0, s>>>(g.bounds.as<uint32_t>(), g.nsegs);
         RT_CHECK_LAUNCH();
-        k_centroid_bounds<<<grid_for(n), kThreads, 0, s>>>(sc.prims_flat.as<float4>(), n, sc.bounds.as<uint32_t>());
+        k_centroid_bounds<<<grid_for(n), kThreads, 0, s>>>(g.prims_flat.as<float4>(),
+                                                            g.nsegs > 1 ? g.prim_seg.as<uint32_t>() : nullptr, n,
+                                                            g.bounds.as<uint32_t>());
         RT_CHECK_LAUNCH();
-        if (sc.morton_bits == 30) build_topology<uint32_t>(sc, s);
-        else build_topology<unsigned long long>(sc, s);
-        refit(sc, s);
+        if (g.morton_bits == 30) build_topology<uint32_t>(g, s);
+        else build_topology<unsigned long long>(g, s);
+        refit(g, s);
     }
     RT_CUDA(cudaEventRecord(e1, s));
     RT_CUDA(cudaEventSynchronize(e1));
-    RT_CUDA(cudaEventElapsedTime(&sc.build_ms, e0, e1));
+    RT_CUDA(cudaEventElapsedTime(&g.build_ms, e0, e1));
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+}
+
+void refit_geometry(Geometry& g, const std::vector<Scene*>& scenes, cudaStream_t s) {
+    cudaEvent_t e0, e1;
+    RT_CUDA(cudaEventCreate(&e0));
+    RT_CUDA(cudaEventCreate(&e1));
+    RT_CUDA(cudaEventRecord(e0, s));
+    const uint32_t before = g.nprims;
+    flatten(g, scenes, s);
+    RT_REQUIRE(g.nprims == before, "primitive count changed; rebuild instead of refit");
+    refit(g, s);
+    RT_CUDA(cudaEventRecord(e1, s));
+    RT_CUDA(cudaEventSynchronize(e1));
+    RT_CUDA(cudaEventElapsedTime(&g.refit_ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+}
+
+size_t Geometry::device_bytes() const {
+    return things_dev.bytes + desc.bytes + segs.bytes + prim_seg.bytes + prims_flat.bytes + prims.bytes + nodes.bytes +
+           codes.bytes + ids.bytes + parents.bytes + flags.bytes + bounds.bytes + sort_tmp.bytes + seg_tmp.bytes +
+           misc.bytes;
+}
+
+size_t Scene::device_bytes() const {
+    size_t b = geo.device_bytes();
+    for (const auto& m : meshes) b += m.v.bytes + m.i.bytes;
+    return b;
+}
+
+Scene* scene_from(rt_scene h) {
+    RT_REQUIRE(h != nullptr, "scene handle is NULL");
+    return reinterpret_cast<Scene*>(h);
+}
+
+namespace {
+
+void scene_build(Scene& sc, int morton_bits, cudaStream_t s) {
+    build_geometry(sc.geo, {&sc}, morton_bits, s);
     sc.built = true;
     sc.topology_dirty = false;
     sc.xf_dirty = false;
 }
 
-void update(Scene& sc, cudaStream_t s) {
+void scene_update(Scene& sc, cudaStream_t s) {
     if (!sc.built) throw Error(RT_ERR_NOT_BUILT, "rt_scene_update before rt_scene_build");
     if (sc.topology_dirty) throw Error(RT_ERR_NOT_BUILT, "things were added since the last build; rebuild");
-    cudaEvent_t e0, e1;
-    RT_CUDA(cudaEventCreate(&e0));
-    RT_CUDA(cudaEventCreate(&e1));
-    RT_CUDA(cudaEventRecord(e0, s));
-    flatten(sc, s);
-    refit(sc, s);
-    RT_CUDA(cudaEventRecord(e1, s));
-    RT_CUDA(cudaEventSynchronize(e1));
-    RT_CUDA(cudaEventElapsedTime(&sc.refit_ms, e0, e1));
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    refit_geometry(sc.geo, {&sc}, s);
     sc.xf_dirty = false;
 }
 
@@ -559,19 +691,6 @@ void tessellate(Scene& sc, float radius, uint32_t ndiv, cudaStream_t s, uint32_t
 }
 
 }  // namespace
-
-size_t Scene::device_bytes() const {
-    size_t b = things_dev.bytes + desc.bytes + prims_flat.bytes + prims.bytes + nodes.bytes + codes.bytes + ids.bytes +
-               parents.bytes + flags.bytes + bounds.bytes + sort_tmp.bytes + misc.bytes;
-    for (const auto& m : meshes) b += m.v.bytes + m.i.bytes;
-    return b;
-}
-
-Scene* scene_from(rt_scene h) {
-    RT_REQUIRE(h != nullptr, "scene handle is NULL");
-    return reinterpret_cast<Scene*>(h);
-}
-
 }  // namespace rt
 
 using namespace rt;
@@ -705,11 +824,11 @@ rt_status rt_scene_set_optics(rt_scene scene, unsigned int thing_id, const rt_op
 }
 
 rt_status rt_scene_build(rt_scene scene, unsigned int morton_bits, void* stream) {
-    return guarded([&] { build(*scene_from(scene), int(morton_bits), as_stream(stream)); });
+    return guarded([&] { scene_build(*scene_from(scene), int(morton_bits), as_stream(stream)); });
 }
 
 rt_status rt_scene_update(rt_scene scene, void* stream) {
-    return guarded([&] { update(*scene_from(scene), as_stream(stream)); });
+    return guarded([&] { scene_update(*scene_from(scene), as_stream(stream)); });
 }
 
 rt_status rt_scene_info_get(rt_scene scene, rt_scene_info* info) {
@@ -718,11 +837,11 @@ rt_status rt_scene_info_get(rt_scene scene, rt_scene_info* info) {
         RT_REQUIRE(info != nullptr, "info is NULL");
         info->n_meshes = unsigned(sc->meshes.size());
         info->n_things = unsigned(sc->things.size());
-        info->n_prims = sc->nprims;
-        info->morton_bits = unsigned(sc->morton_bits);
+        info->n_prims = sc->geo.nprims;
+        info->morton_bits = unsigned(sc->geo.morton_bits);
         info->device_bytes = sc->device_bytes();
-        info->build_ms = sc->build_ms;
-        info->refit_ms = sc->refit_ms;
+        info->build_ms = sc->geo.build_ms;
+        info->refit_ms = sc->geo.refit_ms;
     });
 }
 
@@ -731,24 +850,25 @@ rt_status rt_scene_get_lbvh(rt_scene scene, unsigned long long* codes, unsigned 
     return guarded([&] {
         Scene* sc = scene_from(scene);
         if (!sc->built) throw Error(RT_ERR_NOT_BUILT, "scene not built");
-        const uint32_t n = sc->nprims;
+        const Geometry& g = sc->geo;
+        const uint32_t n = g.nprims;
         if (n == 0) return;
         if (codes) {
-            if (sc->morton_bits == 30) {
+            if (g.morton_bits == 30) {
                 DevBuf tmp;
                 tmp.reserve(size_t(n) * 8);
-                k_lbvh_snapshot_codes32<<<grid_for(n), kThreads>>>(sc->codes.as<uint32_t>(), n,
+                k_lbvh_snapshot_codes32<<<grid_for(n), kThreads>>>(g.codes.as<uint32_t>(), n,
                                                                     tmp.as<unsigned long long>());
                 RT_CHECK_LAUNCH();
                 RT_CUDA(cudaMemcpy(codes, tmp.p, size_t(n) * 8, cudaMemcpyDeviceToHost));
             } else {
-                RT_CUDA(cudaMemcpy(codes, sc->codes.p, size_t(n) * 8, cudaMemcpyDeviceToHost));
+                RT_CUDA(cudaMemcpy(codes, g.codes.p, size_t(n) * 8, cudaMemcpyDeviceToHost));
             }
         }
-        if (ids) RT_CUDA(cudaMemcpy(ids, sc->ids.p, size_t(n) * 4, cudaMemcpyDeviceToHost));
+        if (ids) RT_CUDA(cudaMemcpy(ids, g.ids.p, size_t(n) * 4, cudaMemcpyDeviceToHost));
         if (n < 2) return;
         std::vector<float4> nodes(size_t(n - 1) * 4);
-        RT_CUDA(cudaMemcpy(nodes.data(), sc->nodes.p, nodes.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+        RT_CUDA(cudaMemcpy(nodes.data(), g.nodes.p, nodes.size() * sizeof(float4), cudaMemcpyDeviceToHost));
         for (uint32_t i = 0; i + 1 < n; ++i) {
             const float4 n0 = nodes[4 * i], n1 = nodes[4 * i + 1], n2 = nodes[4 * i + 2], n3 = nodes[4 * i + 3];
             int l, r;
