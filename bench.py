@@ -56,6 +56,7 @@ def parse():
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     p.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     p.add_argument("--batch-scenes", type=int, default=256, help="scenes of the batched leg (0: skip it)")
+    p.add_argument("--no-adjoint", action="store_true", help="skip the adjoint/forward leg")
     return p.parse_args()
 
 
@@ -270,6 +271,81 @@ def batched_leg(R, torch, sptr, stream, nscenes, steps):
                         "width U{128..1024} at 16:9 or 1:1, spp U{1..64}, depth 16"}
 
 
+def adjoint_leg(R, torch, sptr, stream, steps):
+    """Differentiable configuration: the final scene as analytic spheres
+    (glibc seed 1), 256x256, 64 spp, depth 8.  Target rendered from albedos
+    perturbed by N(0, 0.1) and clamped to [0, 1]; loss = pixel L2 of the
+    clamped image.  Times one forward launch and one adjoint launch (gradients
+    of albedo, fuzz and both sky colours) with CUDA events."""
+    W = H = 256
+    spp, depth = 64, 8
+    sp = R.rtow_spheres(R.RT_RECIPE_GLIBC, 1, 11)
+    sc = R.rtow_scene(None, R.RT_RECIPE_GLIBC, 1, 11)
+    n = sc.info().n_things
+    cam = R.rtow_camera(W, H)
+    params = R.launch_params(W, H, spp, depth, 4711, 0)
+    npix = W * H
+    raw = torch.empty(npix * 3, dtype=torch.float32, device="cuda")
+    rpp = torch.empty(npix, dtype=torch.int32, device="cuda")
+    frame = R.Frame(ctypes.c_void_p(raw.data_ptr()), ctypes.c_void_p(rpp.data_ptr()), None, None)
+    lib = R.lib()
+
+    def set_albedo(alb):
+        for k in range(n):
+            sc.set_optics(k, R.optics(int(sp["types"][k]), tuple(float(x) for x in alb[k]), float(sp["fuzz"][k]),
+                                      float(sp["index"][k])))
+
+    def forward():
+        st = R.LaunchStats()
+        R.check(lib.rt_launch_ex(sc.h, ctypes.byref(cam), ctypes.byref(params), ctypes.byref(frame), sptr,
+                                 ctypes.byref(st)))
+        return st
+
+    rng = np.random.default_rng(11)
+    set_albedo(np.clip(sp["albedos"] + rng.normal(0, 0.1, sp["albedos"].shape), 0, 1))
+    forward()
+    target = raw.clone().view(-1, 3).clamp(0, 1)
+    set_albedo(sp["albedos"])
+    ga = torch.zeros(n * 3, dtype=torch.float64, device="cuda")
+    gf = torch.zeros(n, dtype=torch.float64, device="cuda")
+    gs = torch.zeros(6, dtype=torch.float64, device="cuda")
+    gi = torch.empty(npix * 3, dtype=torch.float32, device="cuda")
+
+    def adjoint():
+        sc.adjoint(cam, params, ctypes.c_void_p(raw.data_ptr()), ctypes.c_void_p(gi.data_ptr()),
+                   ctypes.c_void_p(ga.data_ptr()), ctypes.c_void_p(gf.data_ptr()), ctypes.c_void_p(gs.data_ptr()),
+                   stream=sptr)
+
+    def timed(fn):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        r = fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1), r
+
+    f_ms, a_ms, rays = [], [], 0
+    for k in range(steps + 2):
+        fm, st = timed(forward)
+        gi.copy_((2.0 * (raw.view(-1, 3).clamp(0, 1) - target)).view(-1))
+        am, _ = timed(adjoint)
+        if k >= 2:
+            f_ms.append(fm)
+            a_ms.append(am)
+            rays = int(st.rays)
+    loss = float(((raw.view(-1, 3).clamp(0, 1) - target) ** 2).sum())
+    fm, am = float(np.median(f_ms)), float(np.median(a_ms))
+    return {"workload": "final scene as 488 analytic spheres (glibc seed 1), 256x256, 64 spp, depth 8; "
+                        "target from albedo + N(0, 0.1) clamped; loss = pixel L2 of the clamped image",
+            "forward_ms": fm, "adjoint_ms": am, "ratio": am / fm, "forward_rays": rays,
+            "forward_mrays_s": rays / (fm * 1e-3) / 1e6, "loss": loss,
+            "grad_albedo_l1": float(ga.abs().sum()), "grad_fuzz_l1": float(gf.abs().sum()),
+            "grad_sky": [float(x) for x in gs.cpu()],
+            "timing": "CUDA events around one rt_launch_ex and one rt_adjoint_launch, median of the timed steps"}
+
+
 def main():
     args = parse()
     world, rank, local = dist_setup()
@@ -394,6 +470,10 @@ def main():
     if rank == 0 and world == 1 and args.batch_scenes > 0:
         batched = batched_leg(R, torch, sptr, stream, args.batch_scenes, max(1, min(args.steps, 3)))
 
+    adjoint = None
+    if rank == 0 and world == 1 and not args.no_adjoint:
+        adjoint = adjoint_leg(R, torch, sptr, stream, max(3, args.steps))
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_oracle_run(args, args.cpu_seconds)
@@ -434,7 +514,8 @@ def main():
                            "build_ms": info.build_ms},
                 "rays_per_step": total_rays / args.steps / world,
                 "gpu_launches": launches,
-                "clocks": clk, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "batched": batched}
+                "clocks": clk, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "batched": batched,
+                "adjoint": adjoint}
         print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()

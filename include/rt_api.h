@@ -161,6 +161,9 @@ rt_status rt_scene_load_rtow(rt_scene scene, int rng_kind, unsigned int seed, in
  * rt_scene_update or rt_scene_build. */
 rt_status rt_scene_set_transform(rt_scene scene, unsigned int thing_id, const float transform[12]);
 rt_status rt_scene_get_transform(rt_scene scene, unsigned int thing_id, float transform[12]);
+/* Replaces a thing's optics (the reference fixes them in the shader binding
+ * table, optx/rtwo.cxx:418-447).  Takes effect at the next launch of any
+ * geometry holding the scene (its own, or a built batch); no refit. */
 rt_status rt_scene_set_optics(rt_scene scene, unsigned int thing_id, const rt_optics* optics);
 
 /* Scene::build (optx/scene.cxx:227-273, optixAccelBuild): flattens all
@@ -233,6 +236,28 @@ rt_status rt_batch_build(rt_batch b, unsigned int morton_bits, void* stream);
 rt_status rt_batch_launch(rt_batch b, void* stream, rt_launch_stats* stats);
 rt_status rt_batch_info(rt_batch b, unsigned int* n_scenes, unsigned int* n_prims, float* build_ms,
                         unsigned long long* device_bytes);
+
+/* Batched adjoint: registers scene `index`'s loss gradient and outputs
+ * (device pointers, NULL outputs skipped), then rt_batch_adjoint replays
+ * the paths of every registered scene in one launch; the image each scene's
+ * gradient is taken at is its frame's rawRGB (the last rt_batch_launch). */
+rt_status rt_batch_set_adjoint(rt_batch b, unsigned int index, const rt_float3* grad_image,
+                               double* grad_albedo, double* grad_fuzz, double* grad_sky);
+rt_status rt_batch_adjoint(rt_batch b, void* stream);
+
+/* ------------------------------------------------------------- adjoint */
+/* Gradients of an image loss (no counterpart in the reference): given the
+ * rendered image `image` of this scene, camera and params (rawRGB of a
+ * previous rt_launch) and grad_image = dL/d(clamp(image, 0, 1)), replays
+ * every path from its random stream (path replay backpropagation, visibility
+ * held fixed) and writes dL/d albedo (n_things x 3, glass entries 0),
+ * dL/d fuzz (n_things, non-metal entries 0) and dL/d sky (6: ambient rgb,
+ * then the white of the sky gradient).  All pointers are device pointers;
+ * outputs are overwritten, any may be NULL.  depth <= 16.  Synchronises
+ * `stream` before returning (it reads an error word). */
+rt_status rt_adjoint_launch(rt_scene scene, const rt_camera* cam, const rt_launch_params* params,
+                            const rt_float3* image, const rt_float3* grad_image, double* grad_albedo,
+                            double* grad_fuzz, double* grad_sky, void* stream);
 
 /* ---------------------------------------------------------- post-process */
 /* pp_sRGB / pp_none (optx/postproc.cu:49-61; declared at optx/rtwo.cxx:53-54):

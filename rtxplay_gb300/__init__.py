@@ -129,6 +129,9 @@ SIGNATURES = {
     "rt_batch_build": [_P, _U, _P],
     "rt_batch_launch": [_P, _P, ctypes.POINTER(LaunchStats)],
     "rt_batch_info": [_P, _PU, _PU, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_ulonglong)],
+    "rt_batch_set_adjoint": [_P, _U, _P, _P, _P, _P],
+    "rt_batch_adjoint": [_P, _P],
+    "rt_adjoint_launch": [_P, ctypes.POINTER(Camera), ctypes.POINTER(LaunchParams), _P, _P, _P, _P, _P, _P],
 }
 
 _lib = None
@@ -275,6 +278,11 @@ class Scene:
     def build(self, morton_bits=60, stream=None):
         check(lib().rt_scene_build(self.h, morton_bits, stream))
 
+    def adjoint(self, cam, params, image, grad_image, grad_albedo, grad_fuzz, grad_sky, stream=None):
+        """rt_adjoint_launch; every buffer argument is a device pointer (int) or None."""
+        check(lib().rt_adjoint_launch(self.h, ctypes.byref(cam), ctypes.byref(params), image, grad_image,
+                                      grad_albedo, grad_fuzz, grad_sky, stream))
+
     def update(self, stream=None):
         check(lib().rt_scene_update(self.h, stream))
 
@@ -374,6 +382,13 @@ class Batch:
         st = LaunchStats()
         check(lib().rt_batch_launch(self.h, stream, ctypes.byref(st)))
         return st
+
+    def set_adjoint(self, index, grad_image, grad_albedo, grad_fuzz, grad_sky):
+        """rt_batch_set_adjoint; device pointers (int) or None."""
+        check(lib().rt_batch_set_adjoint(self.h, index, grad_image, grad_albedo, grad_fuzz, grad_sky))
+
+    def adjoint(self, stream=None):
+        check(lib().rt_batch_adjoint(self.h, stream))
 
     def info(self):
         n, p = ctypes.c_uint(), ctypes.c_uint()

@@ -1,0 +1,434 @@
+// rt_adjoint.cu -- adjoint path replay: gradients of an image loss with
+// respect to per-thing albedo, metal fuzz and the two sky colours.
+//
+// The reference has no derivative path; this is the differentiable launch
+// beside the forward renderer of rt_render.cu.  Method: path replay
+// backpropagation (Vicini, Speierer, Jakob 2021): a path is not stored by the
+// forward pass but replayed from its counter-based random stream, which
+// reproduces the rendered path bit for bit (same camera ray, same closest
+// hits, same scatter code); visibility is held fixed.
+//
+// Loss model: L = sum over pixels and channels of f(clamp(I, 0, 1)) where I
+// is the rendered image; the caller passes dL/dI' (grad_image, with respect
+// to the clamped image) and I itself.  A pixel channel on or beyond the clamp
+// (I <= 0 or I >= 1) passes no gradient.  I = (1/spp) sum_s c_s, and a path
+// contributes c = (prod_k a_k) * sky(d_last) only when it ends in a miss
+// (absorbed and depth-limited paths are black).  Per path, with
+// g = grad_image * mask / spp (one value per channel):
+//   d/d albedo_k   = g * (prod_{i != k} a_i) * sky        (prefix x suffix products)
+//   d/d ambient    = g * prod a * s,  d/d white = g * prod a * (1 - s),
+//                    s = (unit(d_last).y + 1) / 2           (optx/camera_i.cu:133-139)
+//   d/d fuzz_k     = g * prod a * d sky / d fuzz_k, a forward tangent from the
+//                    metal vertex k (outgoing direction refl + fuzz v moves
+//                    by v) through every later vertex to the miss: hit points
+//                    move on the fixed surface, sphere normals turn with the
+//                    hit point, reflection / refraction directions are
+//                    differentiated, diffuse directions follow the normal.
+// All gradient arithmetic is in double precision, in the same operation order
+// as the FP64 CPU restatement of the method (oracle/rt_oracle.cpp,
+// orc_adjoint), so every path's terms agree bit for bit and the totals only
+// differ by summation order.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "rt_scene.h"
+
+namespace rt {
+namespace {
+
+constexpr int kAdjThreads = 128;
+constexpr uint32_t kAdjPathsPerThread = 4;                     // paths per thread, block-strided
+constexpr uint32_t kAdjPathsPerBlock = kAdjThreads * kAdjPathsPerThread;
+constexpr uint32_t kAdjMaxDepth = 16;                          // at most 15 scatter vertices per path
+constexpr uint32_t kAdjShThings = 1024;                        // per-block shared accumulators up to this many things
+
+struct AdjJob {
+    CamDev cam;
+    float3 ambient, white;
+    uint32_t W, H, npix, spp, depth, seed, key1;
+    int root;
+    uint32_t thing_begin, nthings;
+    unsigned long long path_offset;
+    const rt_float3* image;
+    const rt_float3* grad_image;
+};
+
+struct D3 {
+    double x, y, z;
+};
+__device__ __forceinline__ D3 dd3(float3 a) { return D3{double(a.x), double(a.y), double(a.z)}; }
+__device__ __forceinline__ D3 operator+(D3 a, D3 b) { return D3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ D3 operator-(D3 a, D3 b) { return D3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ D3 operator*(double s, D3 a) { return D3{s * a.x, s * a.y, s * a.z}; }
+__device__ __forceinline__ double ddot(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ double dlen(D3 a) { return sqrt(ddot(a, a)); }
+__device__ __forceinline__ D3 dmul(D3 a, D3 b) { return D3{a.x * b.x, a.y * b.y, a.z * b.z}; }
+
+// derivative of unit(d) along dd
+__device__ __forceinline__ D3 dunit(D3 d, D3 dd) {
+    const double l = dlen(d);
+    const D3 u = (1.0 / l) * d;
+    return (1.0 / l) * (dd - ddot(u, dd) * u);
+}
+
+// One scatter vertex of a replayed path.
+struct AdjVtx {
+    float3 d;        // incoming direction
+    float t;         // hit distance
+    float3 p, N;     // hit point, normal facing the incoming ray
+    float3 v;        // metal: in-ball vector of the fuzz
+    float ratio;     // glass: index ratio
+    int leaf;        // primitive record (sphere centre / radius for the tangent)
+    uint32_t thing;  // global thing
+    uint32_t bits;   // type | branch << 2 | front << 3
+    D3 pre;          // product of the albedos before this vertex
+};
+
+// Forward tangent (dO, dD) of the ray entering vertex m, carried through
+// vertices m..ne-1 to the miss direction d_last; returns d(sky)/d(.) per
+// channel.
+__device__ D3 tangent_to_sky(const AdjVtx* V, uint32_t m, uint32_t ne, const float4* __restrict__ prims, D3 dO, D3 dD,
+                             float3 d_last, float3 ambient, float3 white) {
+    for (uint32_t k = m; k < ne; ++k) {
+        const AdjVtx& v = V[k];
+        const float4 pa = __ldg(prims + 3 * v.leaf), pb = __ldg(prims + 3 * v.leaf + 1),
+                     pc = __ldg(prims + 3 * v.leaf + 2);
+        const bool sphere = __float_as_uint(pc.w) == kPrimSphere;
+        const int type = int(v.bits & 3u);
+        const int branch = int((v.bits >> 2) & 1u);
+        const bool front = ((v.bits >> 3) & 1u) != 0;
+        const D3 d = dd3(v.d), N = dd3(v.N);
+        const double t = v.t;
+        // hit point on the fixed surface: dp = q - d (n.q)/(n.d), q = dO + t dD
+        const D3 q = dO + t * dD;
+        const D3 n = sphere ? dd3(v.p) - dd3(xyz(pa)) : N;
+        const double nd = ddot(n, d);
+        const D3 dp = nd != 0.0 ? q - (ddot(n, q) / nd) * d : q;
+        D3 dN{0, 0, 0};
+        if (sphere) {   // N = +-(p - c) / r
+            const double sgn = front ? 1.0 : -1.0;
+            dN = (sgn / double(pb.x)) * dp;
+        }
+        D3 dOut;
+        if (type == RT_OPTICS_DIFFUSE) {
+            dOut = dN;   // d' = N + u, or N
+        } else {
+            const D3 d1 = (1.0 / dlen(d)) * d;
+            const D3 dd1 = dunit(d, dD);
+            const bool refl = type == RT_OPTICS_REFLECT || branch == 0;
+            if (refl) {
+                const double c = ddot(d1, N);
+                const double dc = ddot(dd1, N) + ddot(d1, dN);
+                dOut = dd1 - 2.0 * ((dc * N) + c * dN);
+            } else {
+                const double ratio = v.ratio;
+                const double raw = -ddot(d1, N);
+                const double cth = raw < 1.0 ? raw : 1.0;
+                const double dcth = raw < 1.0 ? -(ddot(dd1, N) + ddot(d1, dN)) : 0.0;
+                const D3 perp = ratio * (d1 + cth * N);
+                const D3 dperp = ratio * (dd1 + (dcth * N) + cth * dN);
+                const double qq = ddot(perp, perp);
+                const double sroot = sqrt(fabs(1.0 - qq));
+                const double dq = 2.0 * ddot(perp, dperp);
+                const double ds = sroot > 0.0 ? ((1.0 - qq) >= 0.0 ? -dq : dq) / (2.0 * sroot) : 0.0;
+                dOut = dperp - ((ds * N) + sroot * dN);
+            }
+        }
+        dO = dp;
+        dD = dOut;
+    }
+    const D3 du = dunit(dd3(d_last), dD);
+    const double ds = 0.5 * du.y;
+    return D3{ds * (double(ambient.x) - white.x), ds * (double(ambient.y) - white.y),
+              ds * (double(ambient.z) - white.z)};
+}
+
+__device__ __forceinline__ uint32_t adj_job_of(const AdjJob* __restrict__ jobs, uint32_t nj, unsigned long long g) {
+    uint32_t lo = 0, hi = nj;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (jobs[mid].path_offset <= g) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// Gradient sinks of one block: per-thing sums of the block's first job in
+// shared memory (4 doubles per thing: albedo rgb, fuzz), everything else in
+// the global sums G (4 doubles per global thing, then 6 sky values per job).
+struct Sink {
+    double* sh;         // shared sums of job j0, or nullptr
+    uint32_t j0;
+    double* G;
+    uint32_t nthings_total;
+    __device__ __forceinline__ void add(uint32_t jx, const AdjJob& j, uint32_t thing, int c, double x) const {
+        if (x == 0.0) return;
+        if (sh && jx == j0) atomicAdd(sh + 4 * (thing - j.thing_begin) + c, x);
+        else atomicAdd(G + 4 * size_t(thing) + c, x);
+    }
+};
+
+// Replays global path `path` and adds its gradient terms.  Returns 1 when the
+// traversal stack overflowed.
+__device__ uint32_t adjoint_path(const AdjJob* __restrict__ jobs, uint32_t nj, unsigned long long path,
+                                 const float4* __restrict__ nodes, const float4* __restrict__ prims,
+                                 const ThingDev* __restrict__ things, const Sink& sink, double gsky[6]) {
+    const uint32_t jx = adj_job_of(jobs, nj, path);
+    const AdjJob& j = jobs[jx];
+    const uint32_t pid = uint32_t(path - j.path_offset);
+    const uint32_t pix = pid % j.npix, smp = pid / j.npix;
+    double g[3];
+    {
+        const rt_float3 I = j.image[pix], GI = j.grad_image[pix];
+        const float Ic[3] = {I.x, I.y, I.z}, Gc[3] = {GI.x, GI.y, GI.z};
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const double mask = (Ic[c] > 0.f && Ic[c] < 1.f) ? 1.0 : 0.0;   // clamp to [0, 1]
+            g[c] = double(Gc[c]) * mask / double(j.spp);
+        }
+    }
+    if (g[0] == 0.0 && g[1] == 0.0 && g[2] == 0.0) return 0;
+
+    float3 o, d;
+    {
+        Stream s(j.seed, j.key1, pix, smp, 0);
+        camera_ray(j.cam, pix % j.W, pix / j.W, j.W, j.H, s, o, d);
+    }
+    AdjVtx V[kAdjMaxDepth - 1];
+    uint32_t ne = 0;
+    bool miss = false;
+    D3 pre{1, 1, 1};
+    for (uint32_t k = 0;; ++k) {
+        uint32_t nv = 0, nt = 0;
+        const HitRec h = closest_hit<false>(nodes, prims, j.root, o, d, nv, nt);
+        if (h.overflow) return 1;
+        if (h.leaf < 0) {
+            miss = true;
+            break;
+        }
+        if (k + 1 >= j.depth) break;   // black at the depth limit
+        Stream s(j.seed, j.key1, pix, smp, k + 1);
+        const float4 h4 = make_float4(h.t, h.u, h.v, __int_as_float(h.leaf));
+        const ScatterOut so = scatter(prims + 3 * h.leaf, things, o, d, h4, s);
+        AdjVtx& v = V[ne];
+        v.d = d;
+        v.t = h.t;
+        v.p = so.p;
+        v.N = so.N;
+        v.v = so.v;
+        v.ratio = so.ratio;
+        v.leaf = h.leaf;
+        v.thing = __float_as_uint(__ldg(prims + 3 * h.leaf).w);
+        v.bits = uint32_t(so.type) | (uint32_t(so.branch) << 2) | (uint32_t(so.front) << 3);
+        v.pre = pre;
+        const D3 a = so.type == RT_OPTICS_REFRACT ? D3{1, 1, 1} : dd3(xyz(things[v.thing].albedo_type));
+        pre = dmul(pre, a);
+        ++ne;
+        if (!so.cont) break;   // absorbed
+        o = so.p;
+        d = so.dir;
+    }
+    if (!miss) return 0;   // absorbed or depth-limited: black, no gradient
+
+    const D3 u = (1.0 / dlen(dd3(d))) * dd3(d);
+    const double sv = 0.5 * (u.y + 1.0);
+    const double skyc[3] = {(1.0 - sv) * j.white.x + sv * j.ambient.x, (1.0 - sv) * j.white.y + sv * j.ambient.y,
+                            (1.0 - sv) * j.white.z + sv * j.ambient.z};
+    const double th3[3] = {pre.x, pre.y, pre.z};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        gsky[c] += g[c] * th3[c] * sv;              // ambient
+        gsky[3 + c] += g[c] * th3[c] * (1.0 - sv);  // white
+    }
+    D3 suf{1, 1, 1};
+    for (uint32_t k = ne; k-- > 0;) {
+        const AdjVtx& v = V[k];
+        const int type = int(v.bits & 3u);
+        if (type == RT_OPTICS_REFRACT) continue;   // albedo factor 1: suffix unchanged
+        const D3 o3 = dmul(v.pre, suf);
+        sink.add(jx, j, v.thing, 0, g[0] * o3.x * skyc[0]);
+        sink.add(jx, j, v.thing, 1, g[1] * o3.y * skyc[1]);
+        sink.add(jx, j, v.thing, 2, g[2] * o3.z * skyc[2]);
+        if (type == RT_OPTICS_REFLECT) {
+            const D3 ds = tangent_to_sky(V, k + 1, ne, prims, D3{0, 0, 0}, dd3(v.v), d, j.ambient, j.white);
+            sink.add(jx, j, v.thing, 3, g[0] * th3[0] * ds.x + g[1] * th3[1] * ds.y + g[2] * th3[2] * ds.z);
+        }
+        suf = dmul(suf, dd3(xyz(things[v.thing].albedo_type)));
+    }
+    return 0;
+}
+
+// One block: kAdjPathsPerBlock consecutive global paths, thread-strided.
+__global__ void __launch_bounds__(kAdjThreads)
+    k_adjoint(const AdjJob* __restrict__ jobs, uint32_t nj, unsigned long long total, const float4* __restrict__ nodes,
+              const float4* __restrict__ prims, const ThingDev* __restrict__ things, double* G, uint32_t nthings_total,
+              uint32_t sh_things, uint32_t* err) {
+    extern __shared__ double sh[];   // [4 * sh_things] + [6]
+    const unsigned long long base = (unsigned long long)blockIdx.x * kAdjPathsPerBlock;
+    const uint32_t j0 = adj_job_of(jobs, nj, base);
+    const bool use_sh = jobs[j0].nthings <= sh_things;
+    const uint32_t nsh = use_sh ? 4 * jobs[j0].nthings : 0;
+    for (uint32_t i = threadIdx.x; i < nsh + 6; i += blockDim.x) sh[i] = 0.0;
+    __syncthreads();
+    Sink sink{use_sh ? sh : nullptr, j0, G, nthings_total};
+    double gsky[6] = {0, 0, 0, 0, 0, 0};
+    uint32_t my_err = 0;
+    for (uint32_t c = 0; c < kAdjPathsPerThread; ++c) {
+        const unsigned long long path = base + c * kAdjThreads + threadIdx.x;
+        if (path >= total) break;
+        const uint32_t jx = adj_job_of(jobs, nj, path);
+        if (jx == j0) {
+            my_err |= adjoint_path(jobs, nj, path, nodes, prims, things, sink, gsky);
+        } else {   // a block that straddles two jobs: sky terms of the later job go straight to G
+            double gs[6] = {0, 0, 0, 0, 0, 0};
+            my_err |= adjoint_path(jobs, nj, path, nodes, prims, things, sink, gs);
+            for (int k = 0; k < 6; ++k)
+                if (gs[k] != 0.0) atomicAdd(G + 4 * size_t(nthings_total) + 6 * size_t(jx) + k, gs[k]);
+        }
+    }
+    if (my_err) atomicOr(err, 1u);
+    // sky sums of job j0: warp reduction, then one shared atomic per warp
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        double x = gsky[k];
+        for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xFFFFFFFFu, x, off);
+        if ((threadIdx.x & 31u) == 0 && x != 0.0) atomicAdd(sh + nsh + k, x);
+    }
+    __syncthreads();
+    const size_t tb = jobs[j0].thing_begin;
+    for (uint32_t i = threadIdx.x; i < nsh; i += blockDim.x) {
+        const double x = sh[i];
+        if (x != 0.0) atomicAdd(G + 4 * tb + i, x);
+    }
+    if (threadIdx.x < 6) {
+        const double x = sh[nsh + threadIdx.x];
+        if (x != 0.0) atomicAdd(G + 4 * size_t(nthings_total) + 6 * size_t(j0) + threadIdx.x, x);
+    }
+}
+
+struct AdjOut {
+    double* albedo;   // [nthings x 3]
+    double* fuzz;     // [nthings]
+    double* sky;      // [6]
+    uint32_t thing_begin, nthings;
+};
+
+// Scatters the global sums into each job's output arrays.
+__global__ void k_adjoint_out(const double* __restrict__ G, uint32_t nthings_total, const AdjOut* __restrict__ outs,
+                              uint32_t nj) {
+    const uint32_t jx = blockIdx.y;
+    if (jx >= nj) return;
+    const AdjOut o = outs[jx];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < o.nthings; i += gridDim.x * blockDim.x) {
+        const double* src = G + 4 * size_t(o.thing_begin + i);
+        if (o.albedo) {
+            o.albedo[3 * size_t(i)] = src[0];
+            o.albedo[3 * size_t(i) + 1] = src[1];
+            o.albedo[3 * size_t(i) + 2] = src[2];
+        }
+        if (o.fuzz) o.fuzz[i] = src[3];
+    }
+    if (blockIdx.x == 0 && threadIdx.x < 6 && o.sky)
+        o.sky[threadIdx.x] = G[4 * size_t(nthings_total) + 6 * size_t(jx) + threadIdx.x];
+}
+
+struct AdjWorkspace {
+    DevBuf jobs, outs, G, err;
+    std::vector<AdjJob> jobs_host;
+    std::vector<AdjOut> outs_host;
+};
+
+AdjWorkspace& adj_workspace() {
+    static thread_local AdjWorkspace ws;
+    return ws;
+}
+
+}  // namespace
+
+void adjoint_jobs(const Geometry& g, const std::vector<AdjointJob>& jobs, cudaStream_t s) {
+    RT_REQUIRE(!jobs.empty(), "no adjoint jobs");
+    RT_REQUIRE(jobs.size() < (1u << 24), "too many jobs (>= 2^24)");
+    AdjWorkspace& ws = adj_workspace();
+    const uint32_t nj = uint32_t(jobs.size());
+    ws.jobs_host.resize(nj);
+    ws.outs_host.resize(nj);
+    unsigned long long total = 0;
+    uint32_t max_things = 0;
+    for (uint32_t k = 0; k < nj; ++k) {
+        const AdjointJob& a = jobs[k];
+        check_params(&a.params);
+        RT_REQUIRE(a.params.depth <= kAdjMaxDepth, "adjoint depth must be <= 16");
+        RT_REQUIRE(a.image && a.grad_image, "image / grad_image is NULL");
+        RT_REQUIRE(a.seg < g.nsegs, "job segment out of range");
+        AdjJob& d = ws.jobs_host[k];
+        std::memset(&d, 0, sizeof(d));
+        d.cam = cam_dev(a.cam);
+        d.ambient = make_float3(a.params.ambient.x, a.params.ambient.y, a.params.ambient.z);
+        d.white = make_float3(a.params.white.x, a.params.white.y, a.params.white.z);
+        d.W = a.params.image_w;
+        d.H = a.params.image_h;
+        d.npix = d.W * d.H;
+        d.spp = a.params.spp;
+        d.depth = a.params.depth;
+        d.seed = a.params.seed;
+        d.key1 = 0;
+        d.root = g.root(a.seg);
+        d.thing_begin = g.thing_begin[a.seg];
+        d.nthings = (a.seg + 1 < g.nsegs ? g.thing_begin[a.seg + 1] : g.nthings) - d.thing_begin;
+        d.path_offset = total;
+        d.image = a.image;
+        d.grad_image = a.grad_image;
+        total += (unsigned long long)d.npix * d.spp;
+        max_things = std::max(max_things, d.nthings);
+        ws.outs_host[k] = AdjOut{a.grad_albedo, a.grad_fuzz, a.grad_sky, d.thing_begin, d.nthings};
+    }
+    const size_t gsize = (4 * size_t(g.nthings) + 6 * size_t(nj)) * sizeof(double);
+    ws.jobs.reserve(nj * sizeof(AdjJob));
+    ws.outs.reserve(nj * sizeof(AdjOut));
+    ws.G.reserve(gsize);
+    ws.err.reserve(4);
+    RT_CUDA(cudaMemcpyAsync(ws.jobs.p, ws.jobs_host.data(), nj * sizeof(AdjJob), cudaMemcpyHostToDevice, s));
+    RT_CUDA(cudaMemcpyAsync(ws.outs.p, ws.outs_host.data(), nj * sizeof(AdjOut), cudaMemcpyHostToDevice, s));
+    RT_CUDA(cudaMemsetAsync(ws.G.p, 0, gsize, s));
+    RT_CUDA(cudaMemsetAsync(ws.err.p, 0, 4, s));
+    const uint32_t sh_things = std::min(max_things, kAdjShThings);
+    const size_t shmem = (4 * size_t(sh_things) + 6) * sizeof(double);
+    if (total) {
+        const unsigned grid = unsigned((total + kAdjPathsPerBlock - 1) / kAdjPathsPerBlock);
+        k_adjoint<<<grid, kAdjThreads, shmem, s>>>(ws.jobs.as<AdjJob>(), nj, total, g.nodes.as<float4>(),
+                                                   g.prims.as<float4>(), g.things_dev.as<ThingDev>(),
+                                                   ws.G.as<double>(), g.nthings, sh_things, ws.err.as<uint32_t>());
+        RT_CHECK_LAUNCH();
+    }
+    const unsigned gx = std::max(1u, std::min(64u, (max_things + 255) / 256));
+    k_adjoint_out<<<dim3(gx, nj), 256, 0, s>>>(ws.G.as<double>(), g.nthings, ws.outs.as<AdjOut>(), nj);
+    RT_CHECK_LAUNCH();
+    uint32_t herr = 0;
+    RT_CUDA(cudaMemcpyAsync(&herr, ws.err.p, 4, cudaMemcpyDeviceToHost, s));
+    RT_CUDA(cudaStreamSynchronize(s));
+    if (herr) throw Error(RT_ERR_LIMIT, "traversal stack overflow (LBVH deeper than the stack)");
+}
+
+}  // namespace rt
+
+using namespace rt;
+
+extern "C" {
+
+rt_status rt_adjoint_launch(rt_scene scene, const rt_camera* cam, const rt_launch_params* params,
+                            const rt_float3* image, const rt_float3* grad_image, double* grad_albedo,
+                            double* grad_fuzz, double* grad_sky, void* stream) {
+    return guarded([&] {
+        RT_REQUIRE(cam && params, "cam/params is NULL");
+        Scene& sc = *scene_from(scene);
+        if (!sc.built || sc.topology_dirty) throw Error(RT_ERR_NOT_BUILT, "scene not built (call rt_scene_build)");
+        if (sc.xf_dirty) throw Error(RT_ERR_NOT_BUILT, "transforms changed; call rt_scene_update");
+        cudaStream_t s = as_stream(stream);
+        sync_optics(sc.geo, {&sc}, s);
+        std::vector<AdjointJob> jobs(1);
+        jobs[0] = AdjointJob{0, *cam, *params, image, grad_image, grad_albedo, grad_fuzz, grad_sky};
+        adjoint_jobs(sc.geo, jobs, s);
+    });
+}
+
+}  // extern "C"

@@ -11,6 +11,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "rt_api.h"
+
 namespace rt {
 
 // ------------------------------------------------------------------ vectors
@@ -321,6 +323,104 @@ __device__ __forceinline__ HitRec closest_hit(const float4* __restrict__ nodes, 
     while (trav_step<kCount>(s, stack, nodes, prims, nvis, ntest)) {
     }
     return s.h;
+}
+
+// Result of a scatter event at a hit (the closest-hit programs of
+// optx/optics_i.cu:23-288): geometry, the outgoing direction and the random
+// choices that fixed it (kept for the adjoint's path replay).
+struct ScatterOut {
+    float3 p, N;      // hit point, unit normal facing the incoming ray
+    float3 dir;       // outgoing direction (when cont)
+    float3 albedo;    // throughput factor: albedo, or (1,1,1) for glass
+    float3 v;         // diffuse: unit random vector; metal: in-ball vector
+    float ratio;      // glass: index ratio
+    int type;         // optics type
+    int branch;       // diffuse: 1 = near-zero fallback; glass: 0 reflect, 1 refract
+    bool front;       // ray hits the outside
+    bool cont;        // false: absorbed (metal below the surface)
+    bool guide;       // diffuse and metal set the guide layers
+};
+
+// Hit geometry (optx/optics_i.cu:40-82 for triangles, sphere.h:40-46 for
+// spheres) and the Lambertian / fuzzy-metal / dielectric scatter
+// (optx/optics_i.cu:87-96, :168-190, :254-283; near-zero fallback of
+// optics.h:17-18; Schlick's pow 5 as products).  h4 = (t, u, v, leaf).
+__device__ __forceinline__ ScatterOut scatter(const float4* __restrict__ rec, const ThingDev* __restrict__ things,
+                                              float3 o, float3 d, float4 h4, Stream& s) {
+    const float4 pa = __ldg(rec), pb = __ldg(rec + 1), pc = __ldg(rec + 2);
+    const ThingDev th = things[__float_as_uint(pa.w)];
+    ScatterOut r;
+    r.type = __float_as_int(th.albedo_type.w);
+    r.albedo = xyz(th.albedo_type);
+    r.branch = 0;
+    r.ratio = 1.f;
+    r.v = mk(0.f, 0.f, 0.f);
+    r.cont = true;
+    r.guide = r.type != RT_OPTICS_REFRACT;
+    if (__float_as_uint(pc.w) == kPrimTriangle) {
+        const float3 A = xyz(pa), B = xyz(pb), C = xyz(pc);
+        const float u = h4.y, v = h4.z;
+        const float w = 1.f - u - v;
+        r.p = add(add(mul(w, A), mul(u, B)), mul(v, C));
+        float3 N = unitV(cross(sub(B, A), sub(C, A)));
+        if (dot(d, N) > 0.f) N = neg(N);
+        r.N = N;
+        r.front = 0.f > dot(d, sub(r.p, xyz(th.center_fuzz)));   // optx/optics_i.cu:259-267
+    } else {
+        r.p = add(o, mul(h4.x, d));
+        const float3 outward = mul(1.f / pb.x, sub(r.p, xyz(pa)));
+        r.front = 0.f > dot(d, outward);
+        r.N = r.front ? outward : neg(outward);
+    }
+    const float3 N = r.N;
+    if (r.type == RT_OPTICS_DIFFUSE) {
+        const float3 u = rndVon1sphere(s);
+        float3 dir = add(N, u);
+        r.v = u;
+        if (near0(dir)) {
+            dir = N;
+            r.branch = 1;
+        }
+        r.dir = dir;
+    } else if (r.type == RT_OPTICS_REFLECT) {
+        const float3 d1V = unitV(d);
+        const float3 refl = sub(d1V, mul(2.f * dot(d1V, N), N));
+        const float3 v = rndVin1sphere(s);
+        r.v = v;
+        r.dir = add(refl, mul(th.center_fuzz.w, v));
+        r.cont = dot(r.dir, N) > 0.f;
+    } else {
+        r.albedo = mk(1.f, 1.f, 1.f);
+        const float3 d1V = unitV(d);
+        const float cos_theta = fminf(dot(neg(d1V), N), 1.f);
+        const float sin_theta = sqrtf(1.f - cos_theta * cos_theta);
+        const float index = th.index_pad.x;
+        const float ratio = r.front ? 1.f / index : index;
+        r.ratio = ratio;
+        const bool cannot = ratio * sin_theta > 1.f;
+        float r0 = (1.f - ratio) / (1.f + ratio);
+        r0 = r0 * r0;
+        const float om = 1.f - cos_theta;
+        const float pow5 = ((om * om) * (om * om)) * om;
+        const float schlick = r0 + (1.f - r0) * pow5;
+        if (cannot || schlick > s.next()) {
+            r.dir = sub(d1V, mul(2.f * dot(d1V, N), N));
+        } else {
+            const float theta = fminf(dot(neg(d1V), N), 1.f);
+            const float3 perpen = mul(ratio, add(d1V, mul(theta, N)));
+            const float3 parall = mul(-sqrtf(fabsf(1.f - dot(perpen, perpen))), N);
+            r.dir = add(perpen, parall);
+            r.branch = 1;
+        }
+    }
+    return r;
+}
+
+// optx/camera_i.cu:133-139: sky gradient from white to ambient.
+__device__ __forceinline__ float3 sky(float3 d, float3 ambient, float3 white) {
+    const float3 unit = unitV(d);
+    const float t = .5f * (unit.y + 1.f);
+    return add(mul(1.f - t, white), mul(t, ambient));
 }
 
 }  // namespace rt

@@ -28,6 +28,29 @@
 #include "rt_scene.h"
 
 namespace rt {
+
+CamDev cam_dev(const rt_camera& c) {
+    CamDev d;
+    d.eye = make_float3(c.eye.x, c.eye.y, c.eye.z);
+    d.u = make_float3(c.u.x, c.u.y, c.u.z);
+    d.v = make_float3(c.v.x, c.v.y, c.v.z);
+    d.w = make_float3(c.w.x, c.w.y, c.w.z);
+    d.hvec = make_float3(c.hvec.x, c.hvec.y, c.hvec.z);
+    d.wvec = make_float3(c.wvec.x, c.wvec.y, c.wvec.z);
+    d.dvec = make_float3(c.dvec.x, c.dvec.y, c.dvec.z);
+    d.aperture = c.aperture;
+    return d;
+}
+
+void check_params(const rt_launch_params* p) {
+    RT_REQUIRE(p != nullptr, "params is NULL");
+    RT_REQUIRE(p->image_w > 0 && p->image_h > 0, "image size must be positive");
+    RT_REQUIRE(uint64_t(p->image_w) * p->image_h <= (uint64_t(1) << 28), "image has more than 2^28 pixels");
+    RT_REQUIRE(p->spp >= 1, "spp must be >= 1");
+    RT_REQUIRE(uint64_t(p->image_w) * p->image_h * p->spp <= 0xFFFFFFFFull, "w*h*spp must fit in 32 bits");
+    RT_REQUIRE(p->depth >= 1 && p->depth <= 255, "depth must be 1..255");
+}
+
 namespace {
 
 constexpr int kThreads = 256;
@@ -252,13 +275,6 @@ const ExtendVariant kExtendVariants[] = {
 constexpr int kNumExtendVariants = int(sizeof(kExtendVariants) / sizeof(kExtendVariants[0]));
 constexpr int kDefaultExtend = 0;
 
-__device__ __forceinline__ float3 sky(float3 d, float3 ambient, float3 white) {
-    // optx/camera_i.cu:133-139
-    const float3 unit = unitV(d);
-    const float t = .5f * (unit.y + 1.f);
-    return add(mul(1.f - t, white), mul(t, ambient));
-}
-
 // 64-bit fixed-point sample sums: round-half-even(x * 2^32) as two's
 // complement, added with integer atomics (exact, order-free).
 __device__ __forceinline__ unsigned long long fx_q(float x) {
@@ -301,73 +317,17 @@ __global__ void __launch_bounds__(kThreads)
         } else if (bounce + 1 >= j.depth) {
             ended = true;   // black at the depth limit (optx/optics_r.cu:34-42)
         } else {
-            const float4 pa = __ldg(prims + 3 * leaf), pb = __ldg(prims + 3 * leaf + 1), pc = __ldg(prims + 3 * leaf + 2);
-            const uint32_t thing = __float_as_uint(pa.w);
-            const ThingDev th = things[thing];
-            const int type = __float_as_int(th.albedo_type.w);
-            const float3 albedo = xyz(th.albedo_type);
-            // hit geometry: optx/optics_i.cu:40-82 (triangles), sphere.h:40-46 (spheres)
-            float3 p, Nn;
-            bool front;
-            if (__float_as_uint(pc.w) == kPrimTriangle) {
-                const float3 A = xyz(pa), B = xyz(pb), C = xyz(pc);
-                const float u = h4.y, v = h4.z;
-                const float w = 1.f - u - v;
-                p = add(add(mul(w, A), mul(u, B)), mul(v, C));
-                Nn = unitV(cross(sub(B, A), sub(C, A)));
-                if (dot(d, Nn) > 0.f) Nn = neg(Nn);
-                front = 0.f > dot(d, sub(p, xyz(th.center_fuzz)));   // optx/optics_i.cu:259-267
-            } else {
-                p = add(o, mul(h4.x, d));
-                const float3 outward = mul(1.f / pb.x, sub(p, xyz(pa)));
-                front = 0.f > dot(d, outward);
-                Nn = front ? outward : neg(outward);
-            }
             Stream s(j.seed, j.key1, pid % j.npix, pid / j.npix, bounce + 1);
-            if (type == RT_OPTICS_DIFFUSE) {
-                // optx/optics_i.cu:87-96, near-zero fallback of optics.h:17-18
-                float3 dir = add(Nn, rndVon1sphere(s));
-                if (near0(dir)) dir = Nn;
-                thr = mulv(thr, albedo);
-                if (isnull(gN)) gN = Nn;
-                if (isnull(gA)) gA = albedo;
-                no = p; nd = dir; nthr = thr; cont = true;
-            } else if (type == RT_OPTICS_REFLECT) {
-                // optx/optics_i.cu:168-190
-                const float3 d1V = unitV(d);
-                const float3 refl = sub(d1V, mul(2.f * dot(d1V, Nn), Nn));
-                const float3 dir = add(refl, mul(th.center_fuzz.w, rndVin1sphere(s)));
-                if (isnull(gN)) gN = Nn;
-                if (isnull(gA)) gA = albedo;
-                if (dot(dir, Nn) > 0.f) {
-                    thr = mulv(thr, albedo);
-                    no = p; nd = dir; nthr = thr; cont = true;
-                } else {
-                    ended = true;   // absorbed: black
-                }
+            const ScatterOut so = scatter(prims + 3 * leaf, things, o, d, h4, s);
+            if (so.guide) {
+                if (isnull(gN)) gN = so.N;
+                if (isnull(gA)) gA = so.albedo;
+            }
+            if (so.cont) {
+                thr = mulv(thr, so.albedo);   // glass: albedo (1,1,1), an exact no-op
+                no = so.p; nd = so.dir; nthr = thr; cont = true;
             } else {
-                // optx/optics_i.cu:254-283, Schlick's pow 5 as products
-                const float3 d1V = unitV(d);
-                const float cos_theta = fminf(dot(neg(d1V), Nn), 1.f);
-                const float sin_theta = sqrtf(1.f - cos_theta * cos_theta);
-                const float index = th.index_pad.x;
-                const float ratio = front ? 1.f / index : index;
-                const bool cannot = ratio * sin_theta > 1.f;
-                float r0 = (1.f - ratio) / (1.f + ratio);
-                r0 = r0 * r0;
-                const float om = 1.f - cos_theta;
-                const float pow5 = ((om * om) * (om * om)) * om;
-                const float schlick = r0 + (1.f - r0) * pow5;
-                float3 dir;
-                if (cannot || schlick > s.next()) {
-                    dir = sub(d1V, mul(2.f * dot(d1V, Nn), Nn));
-                } else {
-                    const float theta = fminf(dot(neg(d1V), Nn), 1.f);
-                    const float3 perpen = mul(ratio, add(d1V, mul(theta, Nn)));
-                    const float3 parall = mul(-sqrtf(fabsf(1.f - dot(perpen, perpen))), Nn);
-                    dir = add(perpen, parall);
-                }
-                no = p; nd = dir; nthr = thr; cont = true;
+                ended = true;   // absorbed: black
             }
         }
         if (ended) {
@@ -576,28 +536,6 @@ __global__ void k_pp(const rt_float3* __restrict__ src, rt_uchar4* __restrict__ 
 }
 
 // -------------------------------------------------------------- host side
-CamDev cam_dev(const rt_camera& c) {
-    CamDev d;
-    d.eye = make_float3(c.eye.x, c.eye.y, c.eye.z);
-    d.u = make_float3(c.u.x, c.u.y, c.u.z);
-    d.v = make_float3(c.v.x, c.v.y, c.v.z);
-    d.w = make_float3(c.w.x, c.w.y, c.w.z);
-    d.hvec = make_float3(c.hvec.x, c.hvec.y, c.hvec.z);
-    d.wvec = make_float3(c.wvec.x, c.wvec.y, c.wvec.z);
-    d.dvec = make_float3(c.dvec.x, c.dvec.y, c.dvec.z);
-    d.aperture = c.aperture;
-    return d;
-}
-
-void check_params(const rt_launch_params* p) {
-    RT_REQUIRE(p != nullptr, "params is NULL");
-    RT_REQUIRE(p->image_w > 0 && p->image_h > 0, "image size must be positive");
-    RT_REQUIRE(uint64_t(p->image_w) * p->image_h <= (uint64_t(1) << 28), "image has more than 2^28 pixels");
-    RT_REQUIRE(p->spp >= 1, "spp must be >= 1");
-    RT_REQUIRE(uint64_t(p->image_w) * p->image_h * p->spp <= 0xFFFFFFFFull, "w*h*spp must fit in 32 bits");
-    RT_REQUIRE(p->depth >= 1 && p->depth <= 255, "depth must be 1..255");
-}
-
 uint32_t env_u32(const char* name, uint32_t dflt) {
     const char* v = std::getenv(name);
     if (!v || !*v) return dflt;
@@ -919,6 +857,7 @@ void first_hit_rect(Scene& sc, const rt_camera& cam, const rt_launch_params& p, 
     check_params(&p);
     if (!sc.built || sc.topology_dirty || sc.xf_dirty) throw Error(RT_ERR_NOT_BUILT, "scene not built or not updated");
     RT_REQUIRE(prim != nullptr, "prim is NULL");
+    sync_optics(sc.geo, {&sc}, s);
     FirstHitArgs a{};
     a.cam = cam_dev(cam);
     a.W = p.image_w;
@@ -946,6 +885,7 @@ void render_scene(Scene& sc, const rt_camera& cam, const rt_launch_params& p, co
                   rt_launch_stats* stats) {
     if (!sc.built || sc.topology_dirty) throw Error(RT_ERR_NOT_BUILT, "scene not built (call rt_scene_build)");
     if (sc.xf_dirty) throw Error(RT_ERR_NOT_BUILT, "transforms changed; call rt_scene_update");
+    sync_optics(sc.geo, {&sc}, s);
     std::vector<Job> jobs(1);
     jobs[0].seg = 0;
     jobs[0].cam = cam;
@@ -988,6 +928,7 @@ Launcher* launcher_from(rt_launcher l) {
 struct Batch {
     std::vector<Scene*> scenes;
     std::vector<Job> jobs;
+    std::vector<AdjointJob> adj;   // per scene; grad_image NULL: not registered
     Geometry geo;
     bool built = false;
 };
@@ -1162,6 +1103,7 @@ rt_status rt_batch_add(rt_batch b, rt_scene scene, const rt_camera* cam, const r
         j.frame = *frame;
         B->scenes.push_back(sc);
         B->jobs.push_back(j);
+        B->adj.push_back(AdjointJob{j.seg, j.cam, j.params, frame->rawRGB, nullptr, nullptr, nullptr, nullptr});
         B->built = false;
         if (index) *index = j.seg;
     });
@@ -1181,7 +1123,35 @@ rt_status rt_batch_launch(rt_batch b, void* stream, rt_launch_stats* stats) {
         Batch* B = batch_from(b);
         if (!B->built) throw Error(RT_ERR_NOT_BUILT, "batch not built (call rt_batch_build)");
         rt_launch_stats st{};
+        sync_optics(B->geo, B->scenes, as_stream(stream));
         render_jobs(B->geo, B->jobs, as_stream(stream), stats ? stats : &st);
+    });
+}
+
+rt_status rt_batch_set_adjoint(rt_batch b, unsigned int index, const rt_float3* grad_image, double* grad_albedo,
+                               double* grad_fuzz, double* grad_sky) {
+    return guarded([&] {
+        Batch* B = batch_from(b);
+        RT_REQUIRE(index < B->adj.size(), "bad batch index");
+        AdjointJob& a = B->adj[index];
+        a.grad_image = grad_image;
+        a.grad_albedo = grad_albedo;
+        a.grad_fuzz = grad_fuzz;
+        a.grad_sky = grad_sky;
+    });
+}
+
+rt_status rt_batch_adjoint(rt_batch b, void* stream) {
+    return guarded([&] {
+        Batch* B = batch_from(b);
+        if (!B->built) throw Error(RT_ERR_NOT_BUILT, "batch not built (call rt_batch_build)");
+        std::vector<AdjointJob> jobs;
+        for (const AdjointJob& a : B->adj)
+            if (a.grad_image) jobs.push_back(a);
+        RT_REQUIRE(!jobs.empty(), "no scene of the batch has adjoint buffers (rt_batch_set_adjoint)");
+        cudaStream_t s = as_stream(stream);
+        sync_optics(B->geo, B->scenes, s);
+        adjoint_jobs(B->geo, jobs, s);
     });
 }
 

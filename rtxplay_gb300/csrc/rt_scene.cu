@@ -448,6 +448,7 @@ void flatten(Geometry& g, const std::vector<Scene*>& scenes, cudaStream_t s) {
     std::vector<ThingDev> td;
     g.seg_host.assign(scenes.size(), SegDev{0, 0});
     g.thing_begin.assign(scenes.size(), 0);
+    g.optics_seen.assign(scenes.size(), 0);
     uint64_t off = 0;
     for (size_t si = 0; si < scenes.size(); ++si) {
         const Scene& sc = *scenes[si];
@@ -475,6 +476,7 @@ void flatten(Geometry& g, const std::vector<Scene*>& scenes, cudaStream_t s) {
             td.push_back(thing_dev(th));
         }
         g.seg_host[si].prim_count = uint32_t(off) - g.seg_host[si].prim_begin;
+        g.optics_seen[si] = sc.optics_version;
     }
     g.nprims = uint32_t(off);
     g.nthings = uint32_t(desc.size());
@@ -602,6 +604,23 @@ void refit_geometry(Geometry& g, const std::vector<Scene*>& scenes, cudaStream_t
     RT_CUDA(cudaEventElapsedTime(&g.refit_ms, e0, e1));
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+}
+
+void sync_optics(Geometry& g, const std::vector<Scene*>& scenes, cudaStream_t s) {
+    RT_REQUIRE(scenes.size() == g.optics_seen.size(), "scene list differs from the built geometry");
+    bool stale = false;
+    for (size_t si = 0; si < scenes.size(); ++si) stale = stale || scenes[si]->optics_version != g.optics_seen[si];
+    if (!stale) return;
+    g.things_host.clear();
+    for (size_t si = 0; si < scenes.size(); ++si) {
+        for (const ThingHost& th : scenes[si]->things) g.things_host.push_back(thing_dev(th));
+        g.optics_seen[si] = scenes[si]->optics_version;
+    }
+    RT_REQUIRE(g.things_host.size() == g.nthings, "thing count changed since the build");
+    if (g.nthings)
+        RT_CUDA(cudaMemcpyAsync(g.things_dev.p, g.things_host.data(), g.things_host.size() * sizeof(ThingDev),
+                                cudaMemcpyHostToDevice, s));
+    RT_CUDA(cudaStreamSynchronize(s));
 }
 
 size_t Geometry::device_bytes() const {
@@ -819,7 +838,7 @@ rt_status rt_scene_set_optics(rt_scene scene, unsigned int thing_id, const rt_op
         RT_REQUIRE(thing_id < sc->things.size(), "bad thing id");
         check_optics(optics);
         sc->things[thing_id].optics = *optics;
-        sc->xf_dirty = true;
+        sc->optics_version += 1;   // takes effect at the next launch, no refit
     });
 }
 

@@ -68,6 +68,8 @@ struct Geometry {
     int morton_bits = 60;
     std::vector<SegDev> seg_host;
     std::vector<uint32_t> thing_begin;   // first global thing of each segment
+    std::vector<uint64_t> optics_seen;   // optics version of each segment's scene at the last upload
+    std::vector<ThingDev> things_host;   // staging copy of things_dev
     float build_ms = 0.f, refit_ms = 0.f;
 
     size_t device_bytes() const;
@@ -80,6 +82,9 @@ struct Geometry {
 void build_geometry(Geometry& g, const std::vector<Scene*>& scenes, int morton_bits, cudaStream_t s);
 // Re-flattens with the scenes' current transforms/optics and refits.
 void refit_geometry(Geometry& g, const std::vector<Scene*>& scenes, cudaStream_t s);
+// Re-uploads the per-thing optics of `g` when any scene's optics changed
+// since they were last uploaded (optics need no refit).
+void sync_optics(Geometry& g, const std::vector<Scene*>& scenes, cudaStream_t s);
 
 struct Scene {
     std::vector<MeshDev> meshes;
@@ -87,7 +92,8 @@ struct Scene {
     Geometry geo;
     bool built = false;
     bool topology_dirty = true;   // things added since the last build
-    bool xf_dirty = false;        // transforms/optics changed since the last build/update
+    bool xf_dirty = false;        // transforms changed since the last build/update
+    uint64_t optics_version = 0;  // bumped by every optics change
     size_t device_bytes() const;
 };
 
@@ -102,7 +108,27 @@ struct Job {
     rt_frame frame;
 };
 
+// Device camera of a host camera; launch-parameter validation (rt_render.cu).
+CamDev cam_dev(const rt_camera& c);
+void check_params(const rt_launch_params* p);
+
 // Renders all jobs over `g` in one wavefront (rt_render.cu).
 void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s, rt_launch_stats* stats);
+
+// One adjoint job: the rendered image of a job, dL/d(clamped image) and the
+// output gradients (device pointers; a NULL output is skipped).
+struct AdjointJob {
+    uint32_t seg;
+    rt_camera cam;
+    rt_launch_params params;
+    const rt_float3* image;
+    const rt_float3* grad_image;
+    double* grad_albedo;   // [n_things x 3]
+    double* grad_fuzz;     // [n_things]
+    double* grad_sky;      // [6]: ambient rgb, white rgb
+};
+
+// Replays the paths of all jobs and writes their gradients (rt_adjoint.cu).
+void adjoint_jobs(const Geometry& g, const std::vector<AdjointJob>& jobs, cudaStream_t s);
 
 }  // namespace rt
