@@ -139,8 +139,11 @@ def test_adjoint_against_finite_differences_through_autograd(product, cuda):
 
     h = 1e-3
     checked = 0
+    # largest gradients first; channels whose albedo is within 10 h of 0 are
+    # skipped: a central difference there steps to a negative albedo and
+    # across the clamp at 0, where the loss has a kink
     order = np.argsort(-np.abs(ga).max(1))
-    cand = [(int(k), c) for k in order[:40] if types[k] != 2 for c in range(3)]
+    cand = [(int(k), c) for k in order[:60] if types[k] != 2 for c in range(3) if sp["albedos"][k, c] > 10 * 1e-3]
     with torch.no_grad():
         for k, c in cand[:26]:
             vals = []
