@@ -52,6 +52,8 @@ def parse():
     p.add_argument("--depth", type=int, default=50)
     p.add_argument("--level", type=int, default=6)
     p.add_argument("--morton-bits", type=int, default=60)
+    p.add_argument("--layout", default="auto", choices=sorted(LAYOUTS),
+                   help="acceleration-structure layout (auto: instanced meshes, as the reference's GAS/IAS)")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample time")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     p.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
@@ -76,10 +78,14 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
-def profile_dram_bytes_per_ray():
-    """DRAM bytes per ray of k_extend from the committed ncu summary (one
-    capture of full-wave launches), or None."""
-    path = os.path.join(ROOT, "profiles", "k_extend_c1.txt")
+LAYOUTS = {"auto": 0, "flat": 1, "instanced": 2}
+
+
+def profile_dram_bytes_per_ray(layout):
+    """DRAM bytes per ray of k_extend from the committed ncu summary of the
+    layout (one capture of full-wave launches), or None."""
+    name = "k_extend_c1.txt" if layout == 1 else "k_extend_c1_instanced.txt"
+    path = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(path):
         return None
     with open(path) as f:
@@ -370,7 +376,7 @@ def main():
     # ---- scene in HBM (build excluded from the timed region, reported apart)
     sc = R.Scene()
     sc.load_rtow(R.RT_RECIPE_GLIBC, 1, 11, args.level)
-    sc.build(args.morton_bits, stream=sptr)
+    sc.build(args.morton_bits, stream=sptr, layout=LAYOUTS[args.layout])
     info = sc.info()
     cam = R.rtow_camera(W, H)
     raw = torch.empty(npix * 3, dtype=torch.float32, device="cuda")
@@ -449,7 +455,7 @@ def main():
                                              spheres["albedos"], spheres["fuzz"], spheres["index"]):
                 T = np.array([r_, 0, 0, c[0], 0, r_, 0, c[1], 0, 0, r_, c[2]], np.float32)
                 s2.add_thing(R.optics(int(t_), a_, float(f_), float(i_)), mid, T)
-            s2.build(args.morton_bits)
+            s2.build(args.morton_bits, layout=LAYOUTS[args.layout])
             params = R.launch_params(W, H, args.spp, args.depth, 4711 + k, 0)
             L.ignite(s2, cam, params)
             R.check(lib.rt_launcher_download(L.h, None, ctypes.c_void_p(rpp_host.ctypes.data), None, None,
@@ -483,7 +489,7 @@ def main():
     per_launch_ms = rst.extend_ms / ext_launches
     rays_per_launch = rst.rays / ext_launches
     achieved = bytes_per_ray * rays_per_launch / (per_launch_ms * 1e-3) / 1e9 if per_launch_ms > 0 else None
-    dram_per_ray = profile_dram_bytes_per_ray()
+    dram_per_ray = profile_dram_bytes_per_ray(info.layout)
     traffic = dram_per_ray * rays_per_launch if dram_per_ray else None
     frame_ms = elapsed_ms / args.steps
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -507,6 +513,8 @@ def main():
                 "config": {"workload": f"rtow final scene, level-{args.level} tessellation "
                                        f"({info.n_prims} triangles), {W}x{H}, {args.spp} spp, depth {args.depth}",
                            "parallelism": f"replicas x{world}", "morton_bits": info.morton_bits,
+                           "layout": {1: "flat", 2: "instanced"}.get(info.layout, str(info.layout)),
+                           "top_records": info.n_top_records, "bottom_records": info.n_bottom_records,
                            "wave_loop": "CUDA graph (conditional WHILE node)" if os.environ.get("RTX_GRAPH", "1") != "0"
                            else "host-driven",
                            "l2": "inputs larger than L2 (LBVH + triangles "

@@ -166,14 +166,38 @@ rt_status rt_scene_get_transform(rt_scene scene, unsigned int thing_id, float tr
  * geometry holding the scene (its own, or a built batch); no refit. */
 rt_status rt_scene_set_optics(rt_scene scene, unsigned int thing_id, const rt_optics* optics);
 
-/* Scene::build (optx/scene.cxx:227-273, optixAccelBuild): flattens all
- * things to world-space primitives and builds the LBVH (Morton codes, radix
- * sort, Karras hierarchy, atomic bottom-up refit).  morton_bits 30 or 60
- * (0 = 60).  Returns after the build has finished on `stream`. */
+/* Acceleration-structure layout of the next build.
+ *   FLAT: every thing flattened to world-space primitives under one LBVH
+ *     over plain Morton codes of the primitive centroids.
+ *   GROUPED (AUTO, the default): the same flat world-space LBVH, but its keys
+ *     order the things first (a 60-bit code of each thing's centre, ranked)
+ *     and a thing's primitives after (a 30-bit code inside the thing's
+ *     bounds), so the hierarchy has the shape of a two-level one -- the
+ *     reference's GAS-per-mesh / IAS-over-things split (optx/rtwo.cxx:138-244)
+ *     -- at the cost of a flat traversal step.
+ *   INSTANCED: the reference's two-level layout itself: one object-space
+ *     LBVH per mesh, a top-level LBVH over instance records, analytic spheres
+ *     and the triangles of things that cannot be instanced (non-diagonal
+ *     transforms, meshes under 16 triangles); memory-lean, more work per step.
+ * Hits, ids and images do not depend on the layout (tested bit for bit). */
+typedef enum {
+    RT_LAYOUT_AUTO = 0,
+    RT_LAYOUT_FLAT = 1,
+    RT_LAYOUT_INSTANCED = 2,
+    RT_LAYOUT_GROUPED = 3
+} rt_layout;
+rt_status rt_scene_set_layout(rt_scene scene, int layout);
+
+/* Scene::build (optx/scene.cxx:227-273, optixAccelBuild): builds the scene's
+ * LBVHs in the chosen layout (Morton codes, radix sort, Karras hierarchy,
+ * atomic bottom-up refit).  morton_bits 30 or 60 (0 = 60).  Returns after the
+ * build has finished on `stream`. */
 rt_status rt_scene_build(rt_scene scene, unsigned int morton_bits, void* stream);
 
-/* Scene::update (optx/scene.cxx:275-294, IAS refit): re-flattens the things
- * whose transform changed and refits the boxes, keeping the topology. */
+/* Scene::update (optx/scene.cxx:275-294, IAS refit): re-flattens the top
+ * level with the new transforms and refits its boxes, keeping the topology
+ * (object-space bottom levels are untouched); a thing whose transform turned
+ * from diagonal to general (or back) triggers a full build instead. */
 rt_status rt_scene_update(rt_scene scene, void* stream);
 
 typedef struct {
@@ -181,13 +205,18 @@ typedef struct {
     unsigned long long device_bytes;
     float build_ms;   /* last rt_scene_build, CUDA events */
     float refit_ms;   /* last rt_scene_update */
+    unsigned int layout;          /* resolved layout: FLAT, GROUPED or INSTANCED */
+    unsigned int n_instances;     /* instanced things */
+    unsigned int n_top_records;   /* top-level LBVH leaves */
+    unsigned int n_bottom_records;/* bottom-level triangles (all instanced meshes) */
 } rt_scene_info;
 rt_status rt_scene_info_get(rt_scene scene, rt_scene_info* info);
 
-/* LBVH snapshot for parity tests: sorted Morton codes (as 64-bit), sorted
- * primitive ids, Karras children (child >= 0 internal node, < 0 leaf ~child)
- * and per internal node the two child boxes (12 floats: lo0 hi0 lo1 hi1).
- * Host buffers sized n, n, n-1, n-1, 12*(n-1); any may be NULL. */
+/* LBVH snapshot for parity tests (the top level; with RT_LAYOUT_FLAT the
+ * whole scene): sorted Morton codes (as 64-bit), sorted record ids, Karras
+ * children (child >= 0 internal node, < 0 leaf ~child) and per internal node
+ * the two child boxes (12 floats: lo0 hi0 lo1 hi1).  Host buffers sized n,
+ * n, n-1, n-1, 12*(n-1) with n = n_top_records; any may be NULL. */
 rt_status rt_scene_get_lbvh(rt_scene scene, unsigned long long* codes, unsigned int* ids,
                             int* left, int* right, float* boxes);
 
@@ -232,6 +261,7 @@ rt_status rt_batch_create(rt_batch* out);
 rt_status rt_batch_destroy(rt_batch b);
 rt_status rt_batch_add(rt_batch b, rt_scene scene, const rt_camera* cam,
                        const rt_launch_params* params, const rt_frame* frame, unsigned int* index);
+rt_status rt_batch_set_layout(rt_batch b, int layout);
 rt_status rt_batch_build(rt_batch b, unsigned int morton_bits, void* stream);
 rt_status rt_batch_launch(rt_batch b, void* stream, rt_launch_stats* stats);
 rt_status rt_batch_info(rt_batch b, unsigned int* n_scenes, unsigned int* n_prims, float* build_ms,

@@ -22,6 +22,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <limits>
 #include <map>
 #include <numeric>
 #include <vector>
@@ -377,6 +378,7 @@ struct orc_world {
     std::vector<uint64_t> codes;         // sorted Morton codes
     std::vector<uint32_t> order;         // sorted prim ids
     int morton_bits = 60;
+    bool grouped = false;                // things-grouped keys (rank of the thing, then a code inside it)
     std::vector<int32_t> left, right;
     std::vector<Box> cbox0, cbox1;       // per internal node: child boxes
     F3 clo{0, 0, 0}, chi{0, 0, 0};
@@ -437,7 +439,35 @@ void build_lbvh(orc_world& w) {
     std::vector<uint64_t> code(n);
     std::vector<uint32_t> ids(n);
     const float lo3[3] = {lo.x, lo.y, lo.z}, hi3[3] = {hi.x, hi.y, hi.z};
-    if (w.morton_bits == 30) {
+    if (w.grouped) {
+        // Things-grouped keys: each thing's centroid bounds; a 60-bit code of
+        // their centre in the scene's centroid bounds; things ranked by (code,
+        // thing index); key = rank << 30 | 30-bit code inside the thing's bounds.
+        const size_t nt = w.things.size();
+        const float inf = std::numeric_limits<float>::infinity();
+        std::vector<F3> tlo(nt, mk(inf, inf, inf)), thi(nt, mk(-inf, -inf, -inf));
+        for (int i = 0; i < n; ++i) {
+            const int t = w.prims[i].thing;
+            tlo[t] = mk(fminf(tlo[t].x, cen[i].x), fminf(tlo[t].y, cen[i].y), fminf(tlo[t].z, cen[i].z));
+            thi[t] = mk(fmaxf(thi[t].x, cen[i].x), fmaxf(thi[t].y, cen[i].y), fmaxf(thi[t].z, cen[i].z));
+        }
+        std::vector<float> tc(3 * nt);
+        for (size_t t = 0; t < nt; ++t) st3(&tc[3 * t], mul(0.5f, add(tlo[t], thi[t])));
+        std::vector<uint64_t> tcode(nt);
+        std::vector<uint32_t> tid(nt), rank(nt);
+        orc_morton60(tc.data(), unsigned(nt), lo3, hi3, tcode.data());
+        std::iota(tid.begin(), tid.end(), 0u);
+        orc_stable_sort_pairs64(tcode.data(), tid.data(), unsigned(nt));
+        for (size_t k = 0; k < nt; ++k) rank[tid[k]] = uint32_t(k);
+        for (int i = 0; i < n; ++i) {
+            const int t = w.prims[i].thing;
+            const F3 e = sub(thi[t], tlo[t]);
+            const uint32_t qx = quant10(cen[i].x, tlo[t].x, e.x);
+            const uint32_t qy = quant10(cen[i].y, tlo[t].y, e.y);
+            const uint32_t qz = quant10(cen[i].z, tlo[t].z, e.z);
+            code[i] = (uint64_t(rank[t]) << 30) | ((expand10(qx) << 2) | (expand10(qy) << 1) | expand10(qz));
+        }
+    } else if (w.morton_bits == 30) {
         std::vector<uint32_t> c32(n);
         orc_morton30(&cen[0].x, unsigned(n), lo3, hi3, c32.data());
         for (int i = 0; i < n; ++i) code[i] = c32[i];
@@ -1120,6 +1150,15 @@ int orc_world_set_transform(orc_world* w, int thing, const float transform[12]) 
 int orc_world_build(orc_world* w, int morton_bits) {
     if (morton_bits != 30 && morton_bits != 60) return -1;
     w->morton_bits = morton_bits;
+    w->grouped = false;
+    flatten(*w);
+    build_lbvh(*w);
+    return 0;
+}
+
+int orc_world_build_grouped(orc_world* w) {
+    w->morton_bits = 60;
+    w->grouped = true;
     flatten(*w);
     build_lbvh(*w);
     return 0;

@@ -75,6 +75,10 @@ int orc_world_set_transform(orc_world* w, int thing, const float transform[12]);
 /* Flattens things into world-space primitives and builds the LBVH twin with
  * 30- or 60-bit Morton codes. */
 int orc_world_build(orc_world* w, int morton_bits);
+/* The same world with things-grouped keys: things ranked by a 60-bit code of
+ * their centroid-bounds centre, key = rank << 30 | 30-bit code inside the
+ * thing's centroid bounds (the product's RT_LAYOUT_GROUPED). */
+int orc_world_build_grouped(orc_world* w);
 unsigned orc_world_nprims(const orc_world* w);
 /* Copies out the LBVH: codes[n] (sorted), ids[n] (sorted prim ids), left/right[n-1],
  * boxes[(n-1)*12] (child0 lo,hi then child1 lo,hi per internal node), scene

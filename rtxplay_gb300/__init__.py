@@ -26,6 +26,7 @@ RT_ERR_INTERNAL = 6
 RT_OPTICS_DIFFUSE, RT_OPTICS_REFLECT, RT_OPTICS_REFRACT = 0, 1, 2
 RT_FLAG_GUIDES, RT_FLAG_STAGE_TIMING, RT_FLAG_COUNT_VISITS = 0x1, 0x2, 0x4
 RT_RECIPE_GLIBC, RT_RECIPE_COUNTER = 0, 1
+RT_LAYOUT_AUTO, RT_LAYOUT_FLAT, RT_LAYOUT_INSTANCED, RT_LAYOUT_GROUPED = 0, 1, 2, 3
 
 
 class RTError(RuntimeError):
@@ -78,7 +79,8 @@ class LaunchStats(ctypes.Structure):
 class SceneInfo(ctypes.Structure):
     _fields_ = [("n_meshes", ctypes.c_uint), ("n_things", ctypes.c_uint), ("n_prims", ctypes.c_uint),
                 ("morton_bits", ctypes.c_uint), ("device_bytes", ctypes.c_ulonglong),
-                ("build_ms", ctypes.c_float), ("refit_ms", ctypes.c_float)]
+                ("build_ms", ctypes.c_float), ("refit_ms", ctypes.c_float), ("layout", ctypes.c_uint),
+                ("n_instances", ctypes.c_uint), ("n_top_records", ctypes.c_uint), ("n_bottom_records", ctypes.c_uint)]
 
 
 _P = ctypes.c_void_p
@@ -102,6 +104,7 @@ SIGNATURES = {
     "rt_scene_set_transform": [_P, _U, _P],
     "rt_scene_get_transform": [_P, _U, _P],
     "rt_scene_set_optics": [_P, _U, ctypes.POINTER(Optics)],
+    "rt_scene_set_layout": [_P, _I],
     "rt_scene_build": [_P, _U, _P],
     "rt_scene_update": [_P, _P],
     "rt_scene_info_get": [_P, ctypes.POINTER(SceneInfo)],
@@ -126,6 +129,7 @@ SIGNATURES = {
     "rt_batch_create": [ctypes.POINTER(_P)],
     "rt_batch_destroy": [_P],
     "rt_batch_add": [_P, _P, ctypes.POINTER(Camera), ctypes.POINTER(LaunchParams), ctypes.POINTER(Frame), _PU],
+    "rt_batch_set_layout": [_P, _I],
     "rt_batch_build": [_P, _U, _P],
     "rt_batch_launch": [_P, _P, ctypes.POINTER(LaunchStats)],
     "rt_batch_info": [_P, _PU, _PU, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_ulonglong)],
@@ -275,7 +279,12 @@ class Scene:
     def set_optics(self, thing, opt):
         return lib().rt_scene_set_optics(self.h, thing, ctypes.byref(opt))
 
-    def build(self, morton_bits=60, stream=None):
+    def set_layout(self, layout):
+        check(lib().rt_scene_set_layout(self.h, layout))
+
+    def build(self, morton_bits=60, stream=None, layout=None):
+        if layout is not None:
+            self.set_layout(layout)
         check(lib().rt_scene_build(self.h, morton_bits, stream))
 
     def adjoint(self, cam, params, image, grad_image, grad_albedo, grad_fuzz, grad_sky, stream=None):
@@ -292,7 +301,8 @@ class Scene:
         return inf
 
     def lbvh(self):
-        n = self.info().n_prims
+        """Top-level LBVH snapshot (the whole scene with RT_LAYOUT_FLAT)."""
+        n = self.info().n_top_records
         codes = np.zeros(n, np.uint64)
         ids = np.zeros(n, np.uint32)
         left = np.zeros(max(n - 1, 0), np.int32)
@@ -375,7 +385,9 @@ class Batch:
         self._keep.append((scene, cam, params, frame))
         return idx.value
 
-    def build(self, morton_bits=60, stream=None):
+    def build(self, morton_bits=60, stream=None, layout=None):
+        if layout is not None:
+            check(lib().rt_batch_set_layout(self.h, layout))
         check(lib().rt_batch_build(self.h, morton_bits, stream))
 
     def launch(self, stream=None):
@@ -410,11 +422,11 @@ def render(scene, cam, params, guides=False):
     return out
 
 
-def rtow_scene(level=6, rng_kind=RT_RECIPE_GLIBC, seed=1, half_extent=11, morton_bits=60):
+def rtow_scene(level=6, rng_kind=RT_RECIPE_GLIBC, seed=1, half_extent=11, morton_bits=60, layout=RT_LAYOUT_AUTO):
     """The final scene, tessellated at `level` (None: analytic spheres), built."""
     sc = Scene()
     sc.load_rtow(rng_kind, seed, half_extent, -1 if level is None else level)
-    sc.build(morton_bits)
+    sc.build(morton_bits, layout=layout)
     return sc
 
 

@@ -79,8 +79,7 @@ struct AdjVtx {
     float3 p, N;     // hit point, normal facing the incoming ray
     float3 v;        // metal: in-ball vector of the fuzz
     float ratio;     // glass: index ratio
-    int leaf;        // primitive record (sphere centre / radius for the tangent)
-    uint32_t thing;  // global thing
+    uint32_t thing;  // global thing (sphere centre / radius for the tangent)
     uint32_t bits;   // type | branch << 2 | front << 3
     D3 pre;          // product of the albedos before this vertex
 };
@@ -88,13 +87,14 @@ struct AdjVtx {
 // Forward tangent (dO, dD) of the ray entering vertex m, carried through
 // vertices m..ne-1 to the miss direction d_last; returns d(sky)/d(.) per
 // channel.
-__device__ D3 tangent_to_sky(const AdjVtx* V, uint32_t m, uint32_t ne, const float4* __restrict__ prims, D3 dO, D3 dD,
-                             float3 d_last, float3 ambient, float3 white) {
+__device__ D3 tangent_to_sky(const AdjVtx* V, uint32_t m, uint32_t ne, const FlatDesc* __restrict__ desc, D3 dO,
+                             D3 dD, float3 d_last, float3 ambient, float3 white) {
     for (uint32_t k = m; k < ne; ++k) {
         const AdjVtx& v = V[k];
-        const float4 pa = __ldg(prims + 3 * v.leaf), pb = __ldg(prims + 3 * v.leaf + 1),
-                     pc = __ldg(prims + 3 * v.leaf + 2);
-        const bool sphere = __float_as_uint(pc.w) == kPrimSphere;
+        const FlatDesc& fd = desc[v.thing];
+        const bool sphere = fd.analytic != 0;
+        const float4 pa = sphere ? fd.sphere : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 pb = make_float4(fd.sphere.w, 0.f, 0.f, 0.f);
         const int type = int(v.bits & 3u);
         const int branch = int((v.bits >> 2) & 1u);
         const bool front = ((v.bits >> 3) & 1u) != 0;
@@ -170,8 +170,7 @@ struct Sink {
 
 // Replays global path `path` and adds its gradient terms.  Returns 1 when the
 // traversal stack overflowed.
-__device__ uint32_t adjoint_path(const AdjJob* __restrict__ jobs, uint32_t nj, unsigned long long path,
-                                 const float4* __restrict__ nodes, const float4* __restrict__ prims,
+__device__ uint32_t adjoint_path(const AdjJob* __restrict__ jobs, uint32_t nj, unsigned long long path, const GeoView& geo,
                                  const ThingDev* __restrict__ things, const Sink& sink, double gsky[6]) {
     const uint32_t jx = adj_job_of(jobs, nj, path);
     const AdjJob& j = jobs[jx];
@@ -200,16 +199,18 @@ __device__ uint32_t adjoint_path(const AdjJob* __restrict__ jobs, uint32_t nj, u
     D3 pre{1, 1, 1};
     for (uint32_t k = 0;; ++k) {
         uint32_t nv = 0, nt = 0;
-        const HitRec h = closest_hit<false>(nodes, prims, j.root, o, d, nv, nt);
+        const HitRec h = closest_hit_any<false>(geo, j.root, o, d, nv, nt);
         if (h.overflow) return 1;
-        if (h.leaf < 0) {
+        if (!h.hit) {
             miss = true;
             break;
         }
         if (k + 1 >= j.depth) break;   // black at the depth limit
         Stream s(j.seed, j.key1, pix, smp, k + 1);
-        const float4 h4 = make_float4(h.t, h.u, h.v, __int_as_float(h.leaf));
-        const ScatterOut so = scatter(prims + 3 * h.leaf, things, o, d, h4, s);
+        const float4 h4 = make_float4(h.t, h.u, h.v, 0.f);
+        float4 pa, pb, pc;
+        world_prim(geo.desc, h.thing, h.id, pa, pb, pc);
+        const ScatterOut so = scatter(pa, pb, pc, things, o, d, h4, s);
         AdjVtx& v = V[ne];
         v.d = d;
         v.t = h.t;
@@ -217,8 +218,7 @@ __device__ uint32_t adjoint_path(const AdjJob* __restrict__ jobs, uint32_t nj, u
         v.N = so.N;
         v.v = so.v;
         v.ratio = so.ratio;
-        v.leaf = h.leaf;
-        v.thing = __float_as_uint(__ldg(prims + 3 * h.leaf).w);
+        v.thing = h.thing;
         v.bits = uint32_t(so.type) | (uint32_t(so.branch) << 2) | (uint32_t(so.front) << 3);
         v.pre = pre;
         const D3 a = so.type == RT_OPTICS_REFRACT ? D3{1, 1, 1} : dd3(xyz(things[v.thing].albedo_type));
@@ -250,7 +250,7 @@ __device__ uint32_t adjoint_path(const AdjJob* __restrict__ jobs, uint32_t nj, u
         sink.add(jx, j, v.thing, 1, g[1] * o3.y * skyc[1]);
         sink.add(jx, j, v.thing, 2, g[2] * o3.z * skyc[2]);
         if (type == RT_OPTICS_REFLECT) {
-            const D3 ds = tangent_to_sky(V, k + 1, ne, prims, D3{0, 0, 0}, dd3(v.v), d, j.ambient, j.white);
+            const D3 ds = tangent_to_sky(V, k + 1, ne, geo.desc, D3{0, 0, 0}, dd3(v.v), d, j.ambient, j.white);
             sink.add(jx, j, v.thing, 3, g[0] * th3[0] * ds.x + g[1] * th3[1] * ds.y + g[2] * th3[2] * ds.z);
         }
         suf = dmul(suf, dd3(xyz(things[v.thing].albedo_type)));
@@ -259,10 +259,11 @@ __device__ uint32_t adjoint_path(const AdjJob* __restrict__ jobs, uint32_t nj, u
 }
 
 // One block: kAdjPathsPerBlock consecutive global paths, thread-strided.
-__global__ void __launch_bounds__(kAdjThreads)
-    k_adjoint(const AdjJob* __restrict__ jobs, uint32_t nj, unsigned long long total, const float4* __restrict__ nodes,
-              const float4* __restrict__ prims, const ThingDev* __restrict__ things, double* G, uint32_t nthings_total,
-              uint32_t sh_things, uint32_t* err) {
+// Four resident blocks per SM cap the registers at 128 per thread.
+__global__ void __launch_bounds__(kAdjThreads, 4)
+    k_adjoint(const AdjJob* __restrict__ jobs, uint32_t nj, unsigned long long total, GeoView geo,
+              const ThingDev* __restrict__ things, double* G, uint32_t nthings_total, uint32_t sh_things,
+              uint32_t* err) {
     extern __shared__ double sh[];   // [4 * sh_things] + [6]
     const unsigned long long base = (unsigned long long)blockIdx.x * kAdjPathsPerBlock;
     const uint32_t j0 = adj_job_of(jobs, nj, base);
@@ -278,10 +279,10 @@ __global__ void __launch_bounds__(kAdjThreads)
         if (path >= total) break;
         const uint32_t jx = adj_job_of(jobs, nj, path);
         if (jx == j0) {
-            my_err |= adjoint_path(jobs, nj, path, nodes, prims, things, sink, gsky);
+            my_err |= adjoint_path(jobs, nj, path, geo, things, sink, gsky);
         } else {   // a block that straddles two jobs: sky terms of the later job go straight to G
             double gs[6] = {0, 0, 0, 0, 0, 0};
-            my_err |= adjoint_path(jobs, nj, path, nodes, prims, things, sink, gs);
+            my_err |= adjoint_path(jobs, nj, path, geo, things, sink, gs);
             for (int k = 0; k < 6; ++k)
                 if (gs[k] != 0.0) atomicAdd(G + 4 * size_t(nthings_total) + 6 * size_t(jx) + k, gs[k]);
         }
@@ -395,9 +396,9 @@ void adjoint_jobs(const Geometry& g, const std::vector<AdjointJob>& jobs, cudaSt
     const size_t shmem = (4 * size_t(sh_things) + 6) * sizeof(double);
     if (total) {
         const unsigned grid = unsigned((total + kAdjPathsPerBlock - 1) / kAdjPathsPerBlock);
-        k_adjoint<<<grid, kAdjThreads, shmem, s>>>(ws.jobs.as<AdjJob>(), nj, total, g.nodes.as<float4>(),
-                                                   g.prims.as<float4>(), g.things_dev.as<ThingDev>(),
-                                                   ws.G.as<double>(), g.nthings, sh_things, ws.err.as<uint32_t>());
+        k_adjoint<<<grid, kAdjThreads, shmem, s>>>(ws.jobs.as<AdjJob>(), nj, total, g.view(),
+                                                   g.things_dev.as<ThingDev>(), ws.G.as<double>(), g.nthings,
+                                                   sh_things, ws.err.as<uint32_t>());
         RT_CHECK_LAUNCH();
     }
     const unsigned gx = std::max(1u, std::min(64u, (max_things + 255) / 256));

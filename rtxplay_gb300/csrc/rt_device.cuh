@@ -124,13 +124,17 @@ __device__ __forceinline__ void camera_ray(const CamDev& c, uint32_t x, uint32_t
 }
 
 // ------------------------------------------------------------------ layouts
-// Primitive record in LBVH leaf order, 48 bytes (three float4):
-//   triangle: a = (v0, thing id bits), b = (v1, prim id bits), c = (v2, 0)
-//   sphere:   a = (centre, thing id bits), b = (radius, 0, 0, prim id bits), c = (0, 0, 0, 1)
-// Leaf i of the hierarchy is record i; `prim id` is the global id in
-// thing-insertion order (the id parity tests and the picker report).
+// Primitive record, 48 bytes (three float4), in LBVH leaf order:
+//   triangle (world):  a = (v0, thing id bits), b = (v1, prim id bits), c = (v2, 0)
+//   sphere:            a = (centre, thing id bits), b = (radius, 0, 0, prim id bits), c = (0, 0, 0, 1)
+//   instance (top):    a = (world box lo, thing id bits), b = (world box hi, -), c = (0, 0, 0, 2)
+//   triangle (object, bottom level): a = (v0, local index bits), b = (v1, -), c = (v2, 0)
+// `prim id` is the global id in thing-insertion order (the id parity tests and
+// the picker report); a bottom-level triangle's global id is the instance's
+// first primitive + its local index.
 constexpr uint32_t kPrimTriangle = 0u;
 constexpr uint32_t kPrimSphere = 1u;
+constexpr uint32_t kPrimInstance = 2u;
 
 // Internal node, 64 bytes (four float4), both child boxes held by the parent:
 //   n0 = (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y)
@@ -142,6 +146,82 @@ struct ThingDev {       // 48 bytes
     float4 center_fuzz; // instance centre (transform translation), fuzz
     float4 index_pad;   // refraction index, -, -, -
 };
+
+// Per-thing descriptor: where the thing's primitives come from (mesh arrays
+// and transform, or an analytic sphere) and where they went in the two
+// levels.  The build and every kernel that rebuilds a hit primitive's
+// world-space record read it.
+struct FlatDesc {
+    const float3* v;
+    const uint3* idx;
+    uint32_t prim_offset;   // global first primitive (thing-insertion order)
+    uint32_t nprims;
+    int analytic;
+    uint32_t seg;           // segment (scene) of the thing
+    float T[12];            // 3x4 row-major object-to-world transform
+    float4 sphere;          // centre, radius
+    uint32_t top_offset;    // first top-level record of the thing
+    uint32_t ntop;          // top-level records: 1 (sphere or instance) or nprims (flattened mesh)
+    int instanced;          // 1: one instance record over a bottom-level hierarchy
+    int blas_root;          // bottom-level root node (instanced only)
+    uint32_t blas_seg;      // bottom-level segment of the thing's mesh (instanced only)
+    uint32_t pad[3];
+};
+
+// Instance data of an instanced thing (diagonal transforms only): scale
+// (sx, sy, sz), translation (tx, ty, tz), global first primitive, bottom root.
+struct InstDev {
+    float4 a;   // sx, sy, sz, tx
+    float4 b;   // ty, tz, prim_offset (bits), blas_root (bits)
+};
+
+// Device view of a built geometry.
+struct GeoView {
+    const float4* tnodes;     // top level
+    const float4* tprims;
+    const float4* bnodes;     // bottom level (instanced meshes, object space)
+    const float4* bprims;
+    const InstDev* inst;      // per thing
+    const FlatDesc* desc;     // per thing
+    int instanced;            // the top level has instance records
+};
+
+// Object-to-world transform of one vertex, in the reference's operation
+// order (optx/optics_i.cu:46-62), row-major 3x4.
+__host__ __device__ __forceinline__ float3 xform_point(const float* t, float3 a) {
+    return mk(a.x * t[0] + a.y * t[1] + a.z * t[2] + t[3], a.x * t[4] + a.y * t[5] + a.z * t[6] + t[7],
+              a.x * t[8] + a.y * t[9] + a.z * t[10] + t[11]);
+}
+
+// The same transform for a diagonal matrix whose off-diagonal entries are +0:
+// the zero products are kept, so the result has the same bits as xform_point.
+__device__ __forceinline__ float3 xform_diag(float3 sc, float3 tr, float3 a) {
+    const float z = 0.f;
+    return mk(a.x * sc.x + a.y * z + a.z * z + tr.x, a.x * z + a.y * sc.y + a.z * z + tr.y,
+              a.x * z + a.y * z + a.z * sc.z + tr.z);
+}
+
+// World-space record of global primitive `id` of thing `thing`, bit for bit
+// the record the flat layout stores (triangles transformed with
+// xform_point; spheres from the descriptor).
+__device__ __forceinline__ void world_prim(const FlatDesc* __restrict__ desc, uint32_t thing, uint32_t id,
+                                           float4& a, float4& b, float4& c) {
+    const FlatDesc& d = desc[thing];
+    if (d.analytic) {
+        a = make_float4(d.sphere.x, d.sphere.y, d.sphere.z, __uint_as_float(thing));
+        b = make_float4(d.sphere.w, 0.f, 0.f, __uint_as_float(id));
+        c = make_float4(0.f, 0.f, 0.f, __uint_as_float(kPrimSphere));
+        return;
+    }
+    const uint3 tri = d.idx[id - d.prim_offset];
+    float T[12];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) T[k] = d.T[k];
+    const float3 A = xform_point(T, d.v[tri.x]), B = xform_point(T, d.v[tri.y]), C = xform_point(T, d.v[tri.z]);
+    a = make_float4(A.x, A.y, A.z, __uint_as_float(thing));
+    b = make_float4(B.x, B.y, B.z, __uint_as_float(id));
+    c = make_float4(C.x, C.y, C.z, __uint_as_float(kPrimTriangle));
+}
 
 constexpr float kTmin = 1e-3f;   // optx/camera_i.cu:81
 constexpr float kTmax = 1e16f;   // optx/camera_i.cu:82
@@ -198,26 +278,27 @@ __device__ __forceinline__ bool sph_test(float3 c, float r, float3 o, float3 d, 
 
 struct HitRec {
     float t, u, v;
-    int leaf;       // LBVH leaf (record) index, -1 on a miss
+    int hit;        // 1 on a hit, 0 on a miss
     uint32_t id;    // global primitive id of the hit
+    uint32_t thing; // thing of the hit
     bool overflow;  // the traversal stack was full: a subtree was skipped
 };
 
-constexpr int kStackSize = 64;   // > the depth of an LBVH over 2^24 primitives in practice (50 at 8M)
+constexpr int kStackSize = 64;   // > the depth of the hierarchies in practice (50 at 8M flat triangles)
+constexpr int kInstMarker = int(0x80000000u);   // stack entry: leave the current instance
 
-struct TraceCounters {
-    unsigned long long nodes, prims;
-};
-
-// Traversal state of one ray: closest hit so far, current node, stack depth
-// (the stack itself is a separate per-thread array, so this state can stay in
-// registers).
+// Traversal state of one ray: closest hit so far, current node, stack depth,
+// and the instance being traversed (the stack itself is a separate
+// per-thread array, so this state can stay in registers).
 struct Trav {
     float3 o, d, inv;
     float best;
     HitRec h;
     int node;
     int sp;
+    bool in_inst;            // the current node is a bottom-level node
+    float3 isc, itr;         // instance scale, translation
+    uint32_t ioff, ithing;   // instance first primitive, thing
 };
 
 __device__ __forceinline__ void trav_init(Trav& s, float3 o, float3 d, int root) {
@@ -225,19 +306,29 @@ __device__ __forceinline__ void trav_init(Trav& s, float3 o, float3 d, int root)
     s.d = d;
     s.inv = mk(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
     s.best = kTmax;
-    s.h = HitRec{0.f, 0.f, 0.f, -1, 0u, false};
+    s.h = HitRec{0.f, 0.f, 0.f, 0, 0u, 0u, false};
     s.node = root;
     s.sp = 0;
+    s.in_inst = false;
 }
 
-// Tests one primitive; keeps it if it is the closest so far
-// (smallest t, equal t -> larger primitive id).
+// Keeps a hit if it is the closest so far (smallest t, equal t -> larger
+// primitive id).
+__device__ __forceinline__ void trav_keep(Trav& s, float t, float u, float v, uint32_t id, uint32_t thing) {
+    if (t > s.best) return;
+    if (!s.h.hit || t < s.h.t || (t == s.h.t && id > s.h.id)) {
+        s.h.t = t; s.h.u = u; s.h.v = v; s.h.hit = 1; s.h.id = id; s.h.thing = thing;
+        s.best = t;
+    }
+}
+
+// Tests top-level primitive record li (a world-space triangle or a sphere).
 template <bool kCount>
-__device__ __forceinline__ void trav_leaf(Trav& s, const float4* __restrict__ prims, int li, uint32_t& ntest) {
+__device__ __forceinline__ void trav_leaf_top(Trav& s, const GeoView& g, int li, uint32_t& ntest) {
     if (kCount) ++ntest;
-    const float4 a = __ldg(prims + 3 * li);
-    const float4 b = __ldg(prims + 3 * li + 1);
-    const float4 c = __ldg(prims + 3 * li + 2);
+    const float4 a = __ldg(g.tprims + 3 * li);
+    const float4 b = __ldg(g.tprims + 3 * li + 1);
+    const float4 c = __ldg(g.tprims + 3 * li + 2);
     float t, u, v;
     bool hit;
     if (__float_as_uint(c.w) == kPrimTriangle) {
@@ -246,29 +337,96 @@ __device__ __forceinline__ void trav_leaf(Trav& s, const float4* __restrict__ pr
         u = v = 0.f;
         hit = sph_test(xyz(a), b.x, s.o, s.d, t);
     }
-    if (!hit || t > s.best) return;
-    const uint32_t id = __float_as_uint(b.w);
-    if (s.h.leaf < 0 || t < s.h.t || (t == s.h.t && id > s.h.id)) {
-        s.h.t = t; s.h.u = u; s.h.v = v; s.h.leaf = li; s.h.id = id;
-        s.best = t;
+    if (hit) trav_keep(s, t, u, v, __float_as_uint(b.w), __float_as_uint(a.w));
+}
+
+// Tests bottom-level (object-space) triangle li of the current instance in
+// world space: its vertices are transformed exactly as the flat layout
+// transforms them, so the test is the flat layout's test bit for bit.
+template <bool kCount>
+__device__ __forceinline__ void trav_leaf_bottom(Trav& s, const GeoView& g, int li, uint32_t& ntest) {
+    if (kCount) ++ntest;
+    const float4 a = __ldg(g.bprims + 3 * li);
+    const float4 b = __ldg(g.bprims + 3 * li + 1);
+    const float4 c = __ldg(g.bprims + 3 * li + 2);
+    const float3 A = xform_diag(s.isc, s.itr, xyz(a));
+    const float3 B = xform_diag(s.isc, s.itr, xyz(b));
+    const float3 C = xform_diag(s.isc, s.itr, xyz(c));
+    float t, u, v;
+    if (tri_test(A, B, C, s.o, s.d, t, u, v)) trav_keep(s, t, u, v, s.ioff + __float_as_uint(a.w), s.ithing);
+}
+
+// Enters instance record li of the top level: the stack gets a marker that
+// leaves the instance when popped, traversal continues at the bottom root.
+__device__ __forceinline__ void trav_enter(Trav& s, int* stack, const GeoView& g, int li) {
+    const uint32_t thing = __float_as_uint(__ldg(g.tprims + 3 * li).w);
+    const InstDev in = g.inst[thing];
+    if (s.sp < kStackSize) stack[s.sp++] = kInstMarker;
+    else { s.h.overflow = true; return; }
+    s.in_inst = true;
+    s.isc = mk(in.a.x, in.a.y, in.a.z);
+    s.itr = mk(in.a.w, in.b.x, in.b.y);
+    s.ioff = __float_as_uint(in.b.z);
+    s.ithing = thing;
+    s.node = __float_as_int(in.b.w);
+}
+
+// World slab of a bottom-level child box under the instance's diagonal
+// transform: each bound goes through the same rounded operations as the
+// vertices (fl(fl(s x) + t), monotone in x), so the slab holds the
+// transformed triangles exactly.  A negative scale swaps the two bounds, which
+// the slab test does not mind (it takes the min and max of both distances).
+__device__ __forceinline__ void xbox(float lo, float hi, float sc, float tr, float& wlo, float& whi) {
+    wlo = lo * sc + tr;
+    whi = hi * sc + tr;
+}
+
+// Next node from the stack (markers leave instances, a negative top-level
+// entry is an instance to enter).  Returns false when the stack is empty.
+__device__ __forceinline__ bool trav_pop(Trav& s, int* stack, const GeoView& g) {
+    while (true) {
+        if (s.sp == 0) return false;
+        const int v = stack[--s.sp];
+        if (v == kInstMarker) {
+            s.in_inst = false;
+            continue;
+        }
+        if (!s.in_inst && v < 0) {
+            trav_enter(s, stack, g, ~v);
+            if (s.h.overflow) return false;
+        } else {
+            s.node = v;
+        }
+        return true;
     }
 }
 
-// One node of the traversal: both child boxes are tested; hit leaves are
-// tested at once, internal children are descended near first (the far one is
-// pushed).  Returns false when the ray is finished.  The slab distances are
+// One node of the traversal: both child boxes are tested; hit primitive
+// leaves are tested at once, internal children (and, with kInst, instances)
+// are descended near first (the far one is pushed).  Returns false when the
+// ray is finished.  kInst = false is the flat layout's step (no instances, no
+// transforms); kInst = true handles both levels.  The slab distances are
 // (b - o) * (1/d): a fused fma(b, 1/d, -o/d) form needs an absolute slack that
 // grows with |o/d| and measured 3x slower on the C1 scene (culling lost for
 // rays with a near-zero direction component).
-template <bool kCount>
-__device__ __forceinline__ bool trav_step(Trav& s, int* stack, const float4* __restrict__ nodes,
-                                          const float4* __restrict__ prims, uint32_t& nvis, uint32_t& ntest) {
+template <bool kCount, bool kInst>
+__device__ __forceinline__ bool trav_step(Trav& s, int* stack, const GeoView& g, uint32_t& nvis, uint32_t& ntest) {
     if (kCount) ++nvis;
+    const bool bottom = kInst && s.in_inst;
+    const float4* nodes = bottom ? g.bnodes : g.tnodes;
     const int node = s.node;
-    const float4 n0 = __ldg(nodes + 4 * node);
-    const float4 n1 = __ldg(nodes + 4 * node + 1);
-    const float4 n2 = __ldg(nodes + 4 * node + 2);
+    float4 n0 = __ldg(nodes + 4 * node);
+    float4 n1 = __ldg(nodes + 4 * node + 1);
+    float4 n2 = __ldg(nodes + 4 * node + 2);
     const float4 n3 = __ldg(nodes + 4 * node + 3);
+    if (bottom) {
+        xbox(n0.x, n0.y, s.isc.x, s.itr.x, n0.x, n0.y);
+        xbox(n0.z, n0.w, s.isc.y, s.itr.y, n0.z, n0.w);
+        xbox(n1.x, n1.y, s.isc.x, s.itr.x, n1.x, n1.y);
+        xbox(n1.z, n1.w, s.isc.y, s.itr.y, n1.z, n1.w);
+        xbox(n2.x, n2.y, s.isc.z, s.itr.z, n2.x, n2.y);
+        xbox(n2.z, n2.w, s.isc.z, s.itr.z, n2.z, n2.w);
+    }
     const float3 o = s.o, inv = s.inv;
     // child 0
     float a0 = (n0.x - o.x) * inv.x, b0 = (n0.y - o.x) * inv.x;
@@ -285,44 +443,70 @@ __device__ __forceinline__ bool trav_step(Trav& s, int* stack, const float4* __r
     bool h0 = tn0 <= tf0 * kSlack;
     bool h1 = tn1 <= tf1 * kSlack;
     int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
+    uint32_t k0 = __float_as_uint(n3.z), k1 = __float_as_uint(n3.w);   // leaf kinds (written by the refit)
     if (h0 && h1 && tn1 < tn0) {
         const int tc = c0; c0 = c1; c1 = tc;
+        const uint32_t tk = k0; k0 = k1; k1 = tk;
     }
     if (!h0 && h1) {   // only child 1 hit: treat it as the near child
         c0 = c1;
+        k0 = k1;
         h0 = true;
         h1 = false;
     }
-    // h0: c0 hit; h1: c1 hit too (c0 nearer)
-    if (h0 && c0 < 0) { trav_leaf<kCount>(s, prims, ~c0, ntest); h0 = false; }
-    if (h1 && c1 < 0) { trav_leaf<kCount>(s, prims, ~c1, ntest); h1 = false; }
-    if (h0 && h1) {
-        if (s.sp < kStackSize) stack[s.sp++] = c1;
-        else s.h.overflow = true;
-        s.node = c0;
-    } else if (h0) {
-        s.node = c0;
-    } else if (h1) {
-        s.node = c1;
+    // h0: c0 hit; h1: c1 hit too (c0 nearer).  Primitive leaves are tested
+    // now; what stays hit is descended (an internal node, or an instance).
+    if (bottom) {
+        if (h0 && c0 < 0) { trav_leaf_bottom<kCount>(s, g, ~c0, ntest); h0 = false; }
+        if (h1 && c1 < 0) { trav_leaf_bottom<kCount>(s, g, ~c1, ntest); h1 = false; }
     } else {
+        if (h0 && c0 < 0 && (!kInst || k0 != kPrimInstance)) { trav_leaf_top<kCount>(s, g, ~c0, ntest); h0 = false; }
+        if (h1 && c1 < 0 && (!kInst || k1 != kPrimInstance)) { trav_leaf_top<kCount>(s, g, ~c1, ntest); h1 = false; }
+    }
+    if (h0 && h1) {
+        if (s.sp < kStackSize) stack[s.sp++] = c1;   // a top-level instance stays negative (~record)
+        else s.h.overflow = true;
+    } else if (!h0 && h1) {
+        c0 = c1;
+        h0 = true;
+    }
+    if (h0) {
+        if (!kInst || c0 >= 0) {
+            s.node = c0;
+        } else {   // only the top level has descendable leaves
+            trav_enter(s, stack, g, ~c0);
+            if (s.h.overflow) return false;
+        }
+        return true;
+    }
+    if (!kInst) {
         if (s.sp == 0) return false;
         s.node = stack[--s.sp];
+        return true;
     }
-    return true;
+    return trav_pop(s, stack, g);
 }
 
-// Closest hit over the LBVH below `root` for one ray (loop over trav_step);
-// root < 0 is an empty scene.
-template <bool kCount>
-__device__ __forceinline__ HitRec closest_hit(const float4* __restrict__ nodes, const float4* __restrict__ prims,
-                                              int root, float3 o, float3 d, uint32_t& nvis, uint32_t& ntest) {
+// Closest hit below `root` for one ray (loop over trav_step); root < 0 is an
+// empty scene.
+template <bool kCount, bool kInst>
+__device__ __forceinline__ HitRec closest_hit(const GeoView& g, int root, float3 o, float3 d, uint32_t& nvis,
+                                              uint32_t& ntest) {
     Trav s;
     int stack[kStackSize];
     trav_init(s, o, d, root);
     if (root < 0) return s.h;
-    while (trav_step<kCount>(s, stack, nodes, prims, nvis, ntest)) {
+    while (trav_step<kCount, kInst>(s, stack, g, nvis, ntest)) {
     }
     return s.h;
+}
+
+// Dispatch on the geometry's layout (for kernels that serve both).
+template <bool kCount>
+__device__ __forceinline__ HitRec closest_hit_any(const GeoView& g, int root, float3 o, float3 d, uint32_t& nvis,
+                                                  uint32_t& ntest) {
+    if (g.instanced) return closest_hit<kCount, true>(g, root, o, d, nvis, ntest);
+    return closest_hit<kCount, false>(g, root, o, d, nvis, ntest);
 }
 
 // Result of a scatter event at a hit (the closest-hit programs of
@@ -344,10 +528,10 @@ struct ScatterOut {
 // Hit geometry (optx/optics_i.cu:40-82 for triangles, sphere.h:40-46 for
 // spheres) and the Lambertian / fuzzy-metal / dielectric scatter
 // (optx/optics_i.cu:87-96, :168-190, :254-283; near-zero fallback of
-// optics.h:17-18; Schlick's pow 5 as products).  h4 = (t, u, v, leaf).
-__device__ __forceinline__ ScatterOut scatter(const float4* __restrict__ rec, const ThingDev* __restrict__ things,
+// optics.h:17-18; Schlick's pow 5 as products).  (pa, pb, pc) is the hit
+// primitive's world-space record, h4 = (t, u, v, -).
+__device__ __forceinline__ ScatterOut scatter(float4 pa, float4 pb, float4 pc, const ThingDev* __restrict__ things,
                                               float3 o, float3 d, float4 h4, Stream& s) {
-    const float4 pa = __ldg(rec), pb = __ldg(rec + 1), pc = __ldg(rec + 2);
     const ThingDev th = things[__float_as_uint(pa.w)];
     ScatterOut r;
     r.type = __float_as_int(th.albedo_type.w);

@@ -163,75 +163,16 @@ __global__ void __launch_bounds__(kThreads) k_generate(const JobDev* __restrict_
     }
 }
 
-// Persistent traversal: a grid sized to the resident blocks; every lane that
-// finishes its ray takes the next one of the queue, so lanes do not idle while
-// the rest of their warp is still traversing.  A warp looks for new rays every
-// kInner traversal steps and refills once at least kRefill lanes are free
-// (one atomic per warp per refill).
-template <bool kCount, int kInner, int kRefill>
+// One thread per queued ray; kInst selects the two-level traversal.  Two
+// alternatives measured slower on C1: persistent lanes refilled with new rays
+// (active lanes per instruction 12.0 -> 16.6 of 32, but 35% more
+// instructions in an issue-bound kernel) and warp-cooperative traversal with
+// parked leaf tests (active lanes 9.6 -> 12.9, 30% more instructions: 803 vs
+// 993 Mrays/s instanced, 64 spp).
+template <bool kCount, bool kInst>
 __global__ void __launch_bounds__(kThreads)
-    k_extend_p(Queues qs, float4* __restrict__ hits, WaveState* st, const JobDev* __restrict__ jobs,
-               const float4* __restrict__ nodes, const float4* __restrict__ prims) {
-    const uint32_t cur = *((volatile uint32_t*)&st->cur);
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        st->count[cur ^ 1] = 0;   // the next queue starts empty
-        st->fetch[cur ^ 1] = 0;
-    }
-    const Queue Q = pick(qs, cur);
-    const uint32_t n = *((volatile uint32_t*)&st->count[cur]);
-    const uint32_t lane = lane_id();
-    const uint32_t lanemask_lt = (1u << lane) - 1u;
-    Trav s;
-    int stack[kStackSize];
-    int ray = -1;
-    bool exhausted = false;   // warp-uniform: the queue has no rays left to hand out
-    uint32_t nvis = 0, ntest = 0;
-    while (true) {
-        const uint32_t idle = __ballot_sync(0xFFFFFFFFu, ray < 0);
-        if (!exhausted && (idle == 0xFFFFFFFFu || __popc(idle) >= kRefill)) {
-            const int leader = __ffs(idle) - 1;
-            uint32_t base = 0;
-            if (int(lane) == leader) base = atomicAdd(&st->fetch[cur], uint32_t(__popc(idle)));
-            base = __shfl_sync(0xFFFFFFFFu, base, leader);
-            if (base + uint32_t(__popc(idle)) >= n) exhausted = true;
-            if (ray < 0) {
-                const uint32_t idx = base + __popc(idle & lanemask_lt);
-                if (idx < n) {
-                    ray = int(idx);
-                    const float4 o4 = Q.ori[idx], d4 = Q.dir[idx];
-                    trav_init(s, xyz(o4), xyz(d4), jobs[__float_as_uint(d4.w) >> 8].root);
-                }
-            }
-        }
-        if (__ballot_sync(0xFFFFFFFFu, ray >= 0) == 0) break;
-        if (ray >= 0) {
-            for (int k = 0; k < kInner; ++k) {
-                if (s.node < 0 || !trav_step<kCount>(s, stack, nodes, prims, nvis, ntest)) {
-                    hits[ray] = make_float4(s.h.t, s.h.u, s.h.v, __int_as_float(s.h.leaf));
-                    if (s.h.overflow) atomicOr(&st->err, 1u);
-                    ray = -1;
-                    break;
-                }
-            }
-        }
-    }
-    if (kCount) {
-        for (int o = 16; o > 0; o >>= 1) {
-            nvis += __shfl_down_sync(0xFFFFFFFFu, nvis, o);
-            ntest += __shfl_down_sync(0xFFFFFFFFu, ntest, o);
-        }
-        if (lane == 0 && (nvis | ntest)) {
-            atomicAdd(&st->nodes, (unsigned long long)nvis);
-            atomicAdd(&st->prims, (unsigned long long)ntest);
-        }
-    }
-}
-
-// One thread per queued ray.
-template <bool kCount>
-__global__ void __launch_bounds__(kThreads)
-    k_extend(Queues qs, float4* __restrict__ hits, WaveState* st, const JobDev* __restrict__ jobs,
-             const float4* __restrict__ nodes, const float4* __restrict__ prims) {
+    k_extend(Queues qs, float4* __restrict__ hits, uint32_t* __restrict__ hthing, WaveState* st,
+             const JobDev* __restrict__ jobs, GeoView g) {
     const uint32_t cur = *((volatile uint32_t*)&st->cur);
     if (blockIdx.x == 0 && threadIdx.x == 0) st->count[cur ^ 1] = 0;   // the next queue starts empty
     const uint32_t n = *((volatile uint32_t*)&st->count[cur]);
@@ -241,8 +182,9 @@ __global__ void __launch_bounds__(kThreads)
         const Queue Q = pick(qs, cur);
         const float4 o4 = Q.ori[i], d4 = Q.dir[i];
         const int root = jobs[__float_as_uint(d4.w) >> 8].root;
-        const HitRec h = closest_hit<kCount>(nodes, prims, root, xyz(o4), xyz(d4), nvis, ntest);
-        hits[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.leaf));
+        const HitRec h = closest_hit<kCount, kInst>(g, root, xyz(o4), xyz(d4), nvis, ntest);
+        hits[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.hit ? int(h.id) : -1));
+        hthing[i] = h.thing;
         if (h.overflow) atomicOr(&st->err, 1u);
     }
     if (kCount) {
@@ -257,23 +199,7 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
-// Traversal kernel variants, chosen by name (RTX_EXTEND) or the default; each
-// has a plain and a counting instantiation.  Measured on C1 (1200x800, 64
-// spp): one thread per ray 1194-1241 Mrays/s; persistent lanes raise the
-// active lanes per instruction from 12.0 to 16.6 of 32 but add 35% more
-// instructions to an issue-bound kernel (1172 Mrays/s).
-using ExtendFn = void (*)(Queues, float4*, WaveState*, const JobDev*, const float4*, const float4*);
-struct ExtendVariant {
-    const char* name;
-    ExtendFn fn[2];     // [counting]
-    bool persistent;
-};
-const ExtendVariant kExtendVariants[] = {
-    {"plain", {k_extend<false>, k_extend<true>}, false},
-    {"persistent", {k_extend_p<false, 4, 16>, k_extend_p<true, 4, 16>}, true},
-};
-constexpr int kNumExtendVariants = int(sizeof(kExtendVariants) / sizeof(kExtendVariants[0]));
-constexpr int kDefaultExtend = 0;
+using ExtendFn = void (*)(Queues, float4*, uint32_t*, WaveState*, const JobDev*, GeoView);
 
 // 64-bit fixed-point sample sums: round-half-even(x * 2^32) as two's
 // complement, added with integer atomics (exact, order-free).
@@ -282,8 +208,9 @@ __device__ __forceinline__ unsigned long long fx_q(float x) {
 }
 
 __global__ void __launch_bounds__(kThreads)
-    k_shade(Queues qs, const float4* __restrict__ hits, WaveState* st, const JobDev* __restrict__ jobs, uint32_t nj,
-            const float4* __restrict__ prims, const ThingDev* __restrict__ things, Acc acc, int any_guides) {
+    k_shade(Queues qs, const float4* __restrict__ hits, const uint32_t* __restrict__ hthing, WaveState* st,
+            const JobDev* __restrict__ jobs, uint32_t nj, const FlatDesc* __restrict__ desc,
+            const ThingDev* __restrict__ things, Acc acc, int any_guides) {
     const uint32_t cur = *((volatile uint32_t*)&st->cur);
     const uint32_t n = *((volatile uint32_t*)&st->count[cur]);
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -309,16 +236,18 @@ __global__ void __launch_bounds__(kThreads)
             gN = xyz(Q.gn[i]);
             gA = xyz(Q.ga[i]);
         }
-        const int leaf = __float_as_int(h4.w);
+        const int id = __float_as_int(h4.w);
         float3 color = mk(0.f, 0.f, 0.f);
-        if (leaf < 0) {
+        if (id < 0) {
             color = mulv(thr, sky(d, j.ambient, j.white));
             ended = true;
         } else if (bounce + 1 >= j.depth) {
             ended = true;   // black at the depth limit (optx/optics_r.cu:34-42)
         } else {
             Stream s(j.seed, j.key1, pid % j.npix, pid / j.npix, bounce + 1);
-            const ScatterOut so = scatter(prims + 3 * leaf, things, o, d, h4, s);
+            float4 pa, pb, pc;
+            world_prim(desc, hthing[i], uint32_t(id), pa, pb, pc);
+            const ScatterOut so = scatter(pa, pb, pc, things, o, d, h4, s);
             if (so.guide) {
                 if (isnull(gN)) gN = so.N;
                 if (isnull(gA)) gA = so.albedo;
@@ -440,8 +369,7 @@ __global__ void __launch_bounds__(kThreads) k_finalize(const JobDev* __restrict_
 // binary32 Moller-Trumbore t loses digits on grazing hits (its error grows
 // like 1/sin of the grazing angle), so the reported distance re-evaluates the
 // winner in double precision; the selection itself stays binary32.
-__device__ double dist64(const float4* __restrict__ rec, float3 of, float3 df) {
-    const float4 a = __ldg(rec), b = __ldg(rec + 1), c = __ldg(rec + 2);
+__device__ double dist64(float4 a, float4 b, float4 c, float3 of, float3 df) {
     const double o[3] = {of.x, of.y, of.z}, d[3] = {df.x, df.y, df.z};
     if (__float_as_uint(c.w) == kPrimTriangle) {
         const double A[3] = {a.x, a.y, a.z}, B[3] = {b.x, b.y, b.z}, C[3] = {c.x, c.y, c.z};
@@ -474,8 +402,7 @@ struct FirstHitArgs {
 };
 
 // Primary-ray closest hit of one sample for a pixel rectangle.
-__global__ void __launch_bounds__(kThreads) k_first_hit(FirstHitArgs a, const float4* __restrict__ nodes,
-                                                        const float4* __restrict__ prims, int* prim, int* thing, float* t,
+__global__ void __launch_bounds__(kThreads) k_first_hit(FirstHitArgs a, GeoView g, int* prim, int* thing, float* t,
                                                         float* u, float* v, double* t64, uint32_t* err) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= a.nx * a.ny) return;
@@ -485,9 +412,9 @@ __global__ void __launch_bounds__(kThreads) k_first_hit(FirstHitArgs a, const fl
     float3 o, d;
     camera_ray(a.cam, x, y, a.W, a.H, s, o, d);
     uint32_t nv = 0, nt = 0;
-    const HitRec h = closest_hit<false>(nodes, prims, a.root, o, d, nv, nt);
+    const HitRec h = closest_hit_any<false>(g, a.root, o, d, nv, nt);
     if (h.overflow) atomicOr(err, 1u);
-    if (h.leaf < 0) {
+    if (!h.hit) {
         prim[k] = -1;
         if (thing) thing[k] = -1;
         if (t) t[k] = 0.f;
@@ -497,11 +424,15 @@ __global__ void __launch_bounds__(kThreads) k_first_hit(FirstHitArgs a, const fl
         return;
     }
     prim[k] = int(h.id);
-    if (thing) thing[k] = int(__float_as_uint(__ldg(prims + 3 * h.leaf).w));
+    if (thing) thing[k] = int(h.thing);
     if (t) t[k] = h.t;
     if (u) u[k] = h.u;
     if (v) v[k] = h.v;
-    if (t64) t64[k] = dist64(prims + 3 * h.leaf, o, d);
+    if (t64) {
+        float4 pa, pb, pc;
+        world_prim(g.desc, h.thing, h.id, pa, pb, pc);
+        t64[k] = dist64(pa, pb, pc, o, d);
+    }
 }
 
 // ------------------------------------------------------------ post-process
@@ -563,7 +494,7 @@ struct WaveGraph {
 // Per-thread render workspace (queues, accumulators, job table), grow-only.
 struct Workspace {
     DevBuf q[2][5];
-    DevBuf hits, acc, acc_gd, jobs, state;
+    DevBuf hits, hthing, acc, acc_gd, jobs, state;
     WaveState* host_state = nullptr;   // pinned
     std::vector<JobDev> jobs_host;
     std::vector<cudaEvent_t> events;
@@ -588,25 +519,6 @@ Workspace& workspace() {
     return ws;
 }
 
-// Resident blocks of a traversal kernel on this device (persistent grids).
-unsigned resident_grid(ExtendFn fn) {
-    int per_sm = 0;
-    RT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, 0));
-    return unsigned(std::max(1, per_sm) * sm_count());
-}
-
-// Traversal variant of this process: RTX_EXTEND=<name> or the default.
-int extend_variant() {
-    static int v = -1;
-    if (v < 0) {
-        v = kDefaultExtend;
-        const char* e = std::getenv("RTX_EXTEND");
-        for (int k = 0; e && k < kNumExtendVariants; ++k)
-            if (std::strcmp(e, kExtendVariants[k].name) == 0) v = k;
-    }
-    return v;
-}
-
 // Wave loop mode: graph (default) or host-driven (RTX_GRAPH=0, and always
 // when per-kernel CUDA-event timing is requested).
 bool graph_mode() {
@@ -616,14 +528,14 @@ bool graph_mode() {
 
 struct WaveLaunch {
     ExtendFn ext_fn;
-    unsigned ext_grid, qgrid;
+    unsigned qgrid;
     Queues qs;
     float4* hits;
+    uint32_t* hthing;
     WaveState* st;
     const JobDev* jobs;
     uint32_t nj;
-    const float4* nodes;
-    const float4* prims;
+    GeoView geo;
     const ThingDev* things;
     Acc acc;
     int any_guides;
@@ -647,14 +559,16 @@ void build_wave_graph(Workspace& ws, const WaveLaunch& L) {
     WaveLaunch l = L;   // kernel arguments must stay addressable while the nodes are added
     cudaKernelNodeParams kp = {};
     cudaGraphNode_t n_ext, n_shade, n_ctrl;
-    void* ext_args[] = {&l.qs, &l.hits, &l.st, &l.jobs, &l.nodes, &l.prims};
+    void* ext_args[] = {&l.qs, &l.hits, &l.hthing, &l.st, &l.jobs, &l.geo};
     kp.func = reinterpret_cast<void*>(l.ext_fn);
-    kp.gridDim = dim3(l.ext_grid);
+    kp.gridDim = dim3(l.qgrid);
     kp.blockDim = dim3(kThreads);
     kp.kernelParams = ext_args;
     RT_CUDA(cudaGraphAddKernelNode(&n_ext, body, nullptr, 0, &kp));
     const float4* hits_c = l.hits;
-    void* shade_args[] = {&l.qs, &hits_c, &l.st, &l.jobs, &l.nj, &l.prims, &l.things, &l.acc, &l.any_guides};
+    const uint32_t* hthing_c = l.hthing;
+    const FlatDesc* desc_c = l.geo.desc;
+    void* shade_args[] = {&l.qs, &hits_c, &hthing_c, &l.st, &l.jobs, &l.nj, &desc_c, &l.things, &l.acc, &l.any_guides};
     kp.func = reinterpret_cast<void*>(k_shade);
     kp.gridDim = dim3(l.qgrid);
     kp.kernelParams = shade_args;
@@ -732,6 +646,7 @@ void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s
         if (any_guides) for (int k = 3; k < 5; ++k) ws.q[b][k].reserve(size_t(W) * 16);
     }
     ws.hits.reserve(size_t(W) * 16);
+    ws.hthing.reserve(size_t(W) * 4);
     ws.acc.reserve(size_t(total_pix) * 28);   // 3 x u64 colour + u32 rays
     if (any_guides) ws.acc_gd.reserve(size_t(total_pix) * 48);
     ws.jobs.reserve(size_t(nj) * sizeof(JobDev));
@@ -746,16 +661,15 @@ void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s
         L.qs.q[b].gn = any_guides ? ws.q[b][3].as<float4>() : nullptr;
         L.qs.q[b].ga = any_guides ? ws.q[b][4].as<float4>() : nullptr;
     }
-    const ExtendVariant& xv = kExtendVariants[extend_variant()];
-    L.ext_fn = xv.fn[count ? 1 : 0];
+    L.ext_fn = g.ninstances ? (count ? k_extend<true, true> : k_extend<false, true>)
+                            : (count ? k_extend<true, false> : k_extend<false, false>);
     L.qgrid = grid_for(W);
-    L.ext_grid = xv.persistent ? std::min<unsigned>(L.qgrid, resident_grid(L.ext_fn)) : L.qgrid;
     L.hits = ws.hits.as<float4>();
+    L.hthing = ws.hthing.as<uint32_t>();
     L.st = ws.state.as<WaveState>();
     L.jobs = ws.jobs.as<JobDev>();
     L.nj = nj;
-    L.nodes = g.nodes.as<float4>();
-    L.prims = g.prims.as<float4>();
+    L.geo = g.view();
     L.things = g.things_dev.as<ThingDev>();
     {
         unsigned long long* c = ws.acc.as<unsigned long long>();
@@ -778,10 +692,10 @@ void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s
 
     if (use_graph) {
         const std::vector<const void*> key = {
-            reinterpret_cast<const void*>(L.ext_fn), reinterpret_cast<const void*>(uintptr_t(L.ext_grid)),
-            reinterpret_cast<const void*>(uintptr_t(L.qgrid)), L.qs.q[0].ori, L.qs.q[0].gn, L.qs.q[1].ori,
-            L.qs.q[1].gn, L.hits, L.st, L.jobs, reinterpret_cast<const void*>(uintptr_t(nj)), L.nodes, L.prims,
-            L.things, L.acc.col[0], L.acc.gd[0], reinterpret_cast<const void*>(uintptr_t(total_pix)),
+            reinterpret_cast<const void*>(L.ext_fn), reinterpret_cast<const void*>(uintptr_t(L.qgrid)),
+            L.qs.q[0].ori, L.qs.q[0].gn, L.qs.q[1].ori, L.qs.q[1].gn, L.hits, L.hthing, L.st, L.jobs,
+            reinterpret_cast<const void*>(uintptr_t(nj)), L.geo.tnodes, L.geo.tprims, L.geo.bnodes, L.geo.bprims,
+            L.geo.inst, L.geo.desc, L.things, L.acc.col[0], L.acc.gd[0], reinterpret_cast<const void*>(uintptr_t(total_pix)),
             reinterpret_cast<const void*>(uintptr_t(any_guides))};
         if (!ws.graph.exec || ws.graph.key != key) {
             build_wave_graph(ws, L);
@@ -791,7 +705,7 @@ void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s
     } else {
         size_t ev = 0;
         const uint32_t kBatch = 8;
-        void* ext_args[] = {&L.qs, &L.hits, &L.st, &L.jobs, &L.nodes, &L.prims};
+        void* ext_args[] = {&L.qs, &L.hits, &L.hthing, &L.st, &L.jobs, &L.geo};
         cudaGraphConditionalHandle no_handle = 0;
         while (true) {
             for (uint32_t b = 0; b < kBatch; ++b) {
@@ -800,7 +714,7 @@ void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s
                     timed.push_back({ev, 0});
                     ev += 2;
                 }
-                RT_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(L.ext_fn), dim3(L.ext_grid), dim3(kThreads),
+                RT_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(L.ext_fn), dim3(L.qgrid), dim3(kThreads),
                                          ext_args, 0, s));
                 if (stage_timing) {
                     RT_CUDA(cudaEventRecord(ws.event(ev - 1), s));
@@ -808,8 +722,8 @@ void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s
                     timed.push_back({ev, 1});
                     ev += 2;
                 }
-                k_shade<<<L.qgrid, kThreads, 0, s>>>(L.qs, L.hits, L.st, L.jobs, nj, L.prims, L.things, L.acc,
-                                                      any_guides);
+                k_shade<<<L.qgrid, kThreads, 0, s>>>(L.qs, L.hits, L.hthing, L.st, L.jobs, nj, L.geo.desc,
+                                                      L.things, L.acc, any_guides);
                 if (stage_timing) RT_CUDA(cudaEventRecord(ws.event(ev - 1), s));
                 k_wave_ctrl<<<1, 1, 0, s>>>(L.st, no_handle, 0);
                 RT_CHECK_LAUNCH();
@@ -872,8 +786,7 @@ void first_hit_rect(Scene& sc, const rt_camera& cam, const rt_launch_params& p, 
     a.root = sc.geo.root(0);
     uint32_t* err = sc.geo.misc.as<uint32_t>();
     RT_CUDA(cudaMemsetAsync(err, 0, 4, s));
-    k_first_hit<<<grid_for(uint64_t(nx) * ny), kThreads, 0, s>>>(a, sc.geo.nodes.as<float4>(), sc.geo.prims.as<float4>(),
-                                                                  prim, thing, t, u, v, t64, err);
+    k_first_hit<<<grid_for(uint64_t(nx) * ny), kThreads, 0, s>>>(a, sc.geo.view(), prim, thing, t, u, v, t64, err);
     RT_CHECK_LAUNCH();
     uint32_t herr = 0;
     RT_CUDA(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, s));
@@ -929,6 +842,7 @@ struct Batch {
     std::vector<Scene*> scenes;
     std::vector<Job> jobs;
     std::vector<AdjointJob> adj;   // per scene; grad_image NULL: not registered
+    int layout = RT_LAYOUT_AUTO;
     Geometry geo;
     bool built = false;
 };
@@ -1109,11 +1023,20 @@ rt_status rt_batch_add(rt_batch b, rt_scene scene, const rt_camera* cam, const r
     });
 }
 
+rt_status rt_batch_set_layout(rt_batch b, int layout) {
+    return guarded([&] {
+        RT_REQUIRE(layout >= RT_LAYOUT_AUTO && layout <= RT_LAYOUT_GROUPED, "unknown layout");
+        Batch* B = batch_from(b);
+        if (B->layout != layout) B->built = false;
+        B->layout = layout;
+    });
+}
+
 rt_status rt_batch_build(rt_batch b, unsigned int morton_bits, void* stream) {
     return guarded([&] {
         Batch* B = batch_from(b);
         RT_REQUIRE(!B->scenes.empty(), "batch is empty");
-        build_geometry(B->geo, B->scenes, int(morton_bits), as_stream(stream));
+        build_geometry(B->geo, B->scenes, int(morton_bits), B->layout, as_stream(stream));
         B->built = true;
     });
 }

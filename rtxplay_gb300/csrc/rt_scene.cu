@@ -117,39 +117,85 @@ __global__ void k_emit_mesh(const float3* __restrict__ pts, const uint32_t* __re
 }
 
 // ------------------------------------------------------------- flattening
-// One thread per global primitive: the owning thing is the last one whose
-// prim_offset <= pid; triangles are transformed to world space.
-__global__ void k_flatten(const FlatDesc* __restrict__ desc, uint32_t nthings, uint32_t nprims,
-                          float4* __restrict__ out, uint32_t* __restrict__ prim_seg) {
-    const uint32_t pid = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pid >= nprims) return;
+// Mesh of the bottom level: its object-space triangles are records
+// [begin, begin + n) of the bottom level, one segment per mesh.
+struct BlasMesh {
+    const float3* v;
+    const uint3* idx;
+    uint32_t begin, n;
+};
+
+// One thread per bottom-level record: object-space triangle of an instanced
+// mesh, local index in a.w.
+__global__ void k_flatten_bottom(const BlasMesh* __restrict__ meshes, uint32_t nmeshes, uint32_t nrec,
+                                 float4* __restrict__ out, uint32_t* __restrict__ prim_seg) {
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrec) return;
+    uint32_t lo = 0, hi = nmeshes;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (meshes[mid].begin <= r) lo = mid; else hi = mid;
+    }
+    const BlasMesh m = meshes[lo];
+    const uint32_t local = r - m.begin;
+    const uint3 tri = m.idx[local];
+    const float3 A = m.v[tri.x], B = m.v[tri.y], C = m.v[tri.z];
+    float4* o = out + 3 * size_t(r);
+    o[0] = make_float4(A.x, A.y, A.z, __uint_as_float(local));
+    o[1] = make_float4(B.x, B.y, B.z, 0.f);
+    o[2] = make_float4(C.x, C.y, C.z, __uint_as_float(kPrimTriangle));
+    if (prim_seg) prim_seg[r] = lo;
+}
+
+// One thread per top-level record: the owning thing is the last one whose
+// top_offset <= r.  Analytic spheres and flattened mesh triangles (world
+// space, xform_point) as in a flat hierarchy; an instanced thing's record
+// holds the world box of its bottom-level root box under the instance
+// transform (the same monotone rounding as the vertices, so it is exact).
+__global__ void k_flatten_top(const FlatDesc* __restrict__ desc, uint32_t nthings, uint32_t nrec,
+                              const float4* __restrict__ bnodes, float4* __restrict__ out,
+                              uint32_t* __restrict__ prim_seg) {
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrec) return;
     uint32_t lo = 0, hi = nthings;
     while (hi - lo > 1) {
         const uint32_t mid = (lo + hi) >> 1;
-        if (desc[mid].prim_offset <= pid) lo = mid; else hi = mid;
+        if (desc[mid].top_offset <= r) lo = mid; else hi = mid;
     }
     const FlatDesc& d = desc[lo];
     const uint32_t thing = lo;
-    if (prim_seg) prim_seg[pid] = d.seg;
-    float4* o = out + 3 * size_t(pid);
+    if (prim_seg) prim_seg[r] = d.seg;
+    float4* o = out + 3 * size_t(r);
     if (d.analytic) {
         o[0] = make_float4(d.sphere.x, d.sphere.y, d.sphere.z, __uint_as_float(thing));
-        o[1] = make_float4(d.sphere.w, 0.f, 0.f, __uint_as_float(pid));
+        o[1] = make_float4(d.sphere.w, 0.f, 0.f, __uint_as_float(d.prim_offset));
         o[2] = make_float4(0.f, 0.f, 0.f, __uint_as_float(kPrimSphere));
         return;
     }
-    const uint3 tri = d.idx[pid - d.prim_offset];
-    const float* t = d.T;
-    auto xf = [&](uint32_t vi) {
-        const float3 a = d.v[vi];
-        // optx/optics_i.cu:46-62: object-to-world transform, left to right
-        return mk(a.x * t[0] + a.y * t[1] + a.z * t[2] + t[3], a.x * t[4] + a.y * t[5] + a.z * t[6] + t[7],
-                  a.x * t[8] + a.y * t[9] + a.z * t[10] + t[11]);
-    };
-    const float3 A = xf(tri.x), B = xf(tri.y), C = xf(tri.z);
-    o[0] = make_float4(A.x, A.y, A.z, __uint_as_float(thing));
-    o[1] = make_float4(B.x, B.y, B.z, __uint_as_float(pid));
-    o[2] = make_float4(C.x, C.y, C.z, __uint_as_float(kPrimTriangle));
+    if (d.instanced) {
+        const float4* n = bnodes + 4 * size_t(d.blas_root);
+        const float4 n0 = n[0], n1 = n[1], n2 = n[2];
+        const float sc[3] = {d.T[0], d.T[5], d.T[10]}, tr[3] = {d.T[3], d.T[7], d.T[11]};
+        const float blo[3] = {fminf(n0.x, n1.x), fminf(n0.z, n1.z), fminf(n2.x, n2.z)};
+        const float bhi[3] = {fmaxf(n0.y, n1.y), fmaxf(n0.w, n1.w), fmaxf(n2.y, n2.w)};
+        float wlo[3], whi[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float p = blo[k] * sc[k] + tr[k], q = bhi[k] * sc[k] + tr[k];
+            wlo[k] = fminf(p, q);
+            whi[k] = fmaxf(p, q);
+        }
+        o[0] = make_float4(wlo[0], wlo[1], wlo[2], __uint_as_float(thing));
+        o[1] = make_float4(whi[0], whi[1], whi[2], 0.f);
+        o[2] = make_float4(0.f, 0.f, 0.f, __uint_as_float(kPrimInstance));
+        return;
+    }
+    const uint32_t pid = d.prim_offset + (r - d.top_offset);
+    float4 a, b, c;
+    world_prim(desc, thing, pid, a, b, c);
+    o[0] = a;
+    o[1] = b;
+    o[2] = c;
 }
 
 // ------------------------------------------------------------------- LBVH
@@ -159,6 +205,7 @@ struct Box3 {
 
 __device__ __forceinline__ Box3 prim_box(const float4* __restrict__ rec) {
     const float4 a = rec[0], b = rec[1], c = rec[2];
+    if (__float_as_uint(c.w) == kPrimInstance) return Box3{xyz(a), xyz(b)};
     if (__float_as_uint(c.w) == kPrimTriangle) {
         return Box3{mk(fminf(fminf(a.x, b.x), c.x), fminf(fminf(a.y, b.y), c.y), fminf(fminf(a.z, b.z), c.z)),
                     mk(fmaxf(fmaxf(a.x, b.x), c.x), fmaxf(fmaxf(a.y, b.y), c.y), fmaxf(fmaxf(a.z, b.z), c.z))};
@@ -187,7 +234,7 @@ __global__ void k_init_bounds(uint32_t* b, uint32_t nsegs) {
 // reduces in registers and issues six atomics; a mixed warp (segment border)
 // issues them per lane.
 __global__ void k_centroid_bounds(const float4* __restrict__ prims, const uint32_t* __restrict__ prim_seg,
-                                  uint32_t n, uint32_t* __restrict__ bounds) {
+                                  uint32_t n, uint32_t* __restrict__ bounds, int by_thing) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < n;
     uint32_t v[6] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u};
@@ -197,7 +244,7 @@ __global__ void k_centroid_bounds(const float4* __restrict__ prims, const uint32
         v[0] = v[3] = ford(c.x);
         v[1] = v[4] = ford(c.y);
         v[2] = v[5] = ford(c.z);
-        seg = prim_seg ? prim_seg[i] : 0u;
+        seg = by_thing ? __float_as_uint(prims[3 * size_t(i)].w) : (prim_seg ? prim_seg[i] : 0u);
     }
     const uint32_t vmask = __ballot_sync(0xFFFFFFFFu, valid);
     if (!vmask) return;
@@ -267,6 +314,54 @@ __global__ void k_morton(const float4* __restrict__ prims, const uint32_t* __res
         const unsigned long long qz = (unsigned long long)(quantf(c.z, lo.z, ext.z, 1048576.f));
         codes[i] = K((expand20(qx) << 2) | (expand20(qy) << 1) | expand20(qz));
     }
+    ids[i] = i;
+}
+
+// Things-grouped keys.  Every thing gets a 60-bit code of the centre of its
+// primitives' centroid bounds within its segment's bounds; sorting the things
+// by (code, id) ranks them; a primitive's key is (rank << 30) | its 30-bit
+// Morton code within its thing's centroid bounds.  The hierarchy then splits
+// between things first and inside a thing afterwards (the shape of a two-level
+// hierarchy), while every node and primitive stays in world space.
+__global__ void k_thing_codes(const uint32_t* __restrict__ tbounds, const FlatDesc* __restrict__ desc,
+                              const uint32_t* __restrict__ sbounds, uint32_t nthings,
+                              unsigned long long* __restrict__ codes, uint32_t* __restrict__ ids) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nthings) return;
+    const uint32_t* tb = tbounds + 6 * size_t(t);
+    const float3 c = centroid(Box3{mk(fdeord(tb[0]), fdeord(tb[1]), fdeord(tb[2])),
+                                   mk(fdeord(tb[3]), fdeord(tb[4]), fdeord(tb[5]))});
+    const uint32_t* b = sbounds + 6 * size_t(desc[t].seg);
+    const float3 lo = mk(fdeord(b[0]), fdeord(b[1]), fdeord(b[2]));
+    const float3 hi = mk(fdeord(b[3]), fdeord(b[4]), fdeord(b[5]));
+    const float3 ext = sub(hi, lo);
+    const unsigned long long qx = (unsigned long long)(quantf(c.x, lo.x, ext.x, 1048576.f));
+    const unsigned long long qy = (unsigned long long)(quantf(c.y, lo.y, ext.y, 1048576.f));
+    const unsigned long long qz = (unsigned long long)(quantf(c.z, lo.z, ext.z, 1048576.f));
+    codes[t] = (expand20(qx) << 2) | (expand20(qy) << 1) | expand20(qz);
+    ids[t] = t;
+}
+
+__global__ void k_thing_rank(const uint32_t* __restrict__ sorted_ids, uint32_t nthings, uint32_t* __restrict__ rank) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < nthings) rank[sorted_ids[k]] = k;
+}
+
+__global__ void k_morton_grouped(const float4* __restrict__ prims, uint32_t n, const uint32_t* __restrict__ tbounds,
+                                 const uint32_t* __restrict__ rank, unsigned long long* __restrict__ codes,
+                                 uint32_t* __restrict__ ids) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t t = __float_as_uint(prims[3 * size_t(i)].w);
+    const uint32_t* tb = tbounds + 6 * size_t(t);
+    const float3 lo = mk(fdeord(tb[0]), fdeord(tb[1]), fdeord(tb[2]));
+    const float3 hi = mk(fdeord(tb[3]), fdeord(tb[4]), fdeord(tb[5]));
+    const float3 ext = sub(hi, lo);
+    const float3 c = centroid(prim_box(prims + 3 * size_t(i)));
+    const uint32_t qx = uint32_t(quantf(c.x, lo.x, ext.x, 1024.f));
+    const uint32_t qy = uint32_t(quantf(c.y, lo.y, ext.y, 1024.f));
+    const uint32_t qz = uint32_t(quantf(c.z, lo.z, ext.z, 1024.f));
+    codes[i] = ((unsigned long long)rank[t] << 30) | ((expand10(qx) << 2) | (expand10(qy) << 1) | expand10(qz));
     ids[i] = i;
 }
 
@@ -388,9 +483,19 @@ __global__ void k_refit(const float4* __restrict__ prims, uint32_t n, float4* no
     if (p == -2) {   // one-primitive segment: the root holds the leaf twice
         write_child_box(nodes + 4 * size_t(i), 0, b);
         write_child_box(nodes + 4 * size_t(i), 1, b);
+        float* f = reinterpret_cast<float*>(nodes + 4 * size_t(i) + 3);
+        f[2] = f[3] = prims[3 * size_t(i) + 2].w;
         return;
     }
     int child = ~int(i);
+    // the leaf's record kind goes next to its child reference (n3.z / n3.w),
+    // so traversal knows an instance from a primitive without loading the record
+    const uint32_t kind = __float_as_uint(prims[3 * size_t(i) + 2].w);
+    {
+        const float4 n3 = __ldcg(nodes + 4 * size_t(p) + 3);
+        float* f = reinterpret_cast<float*>(nodes + 4 * size_t(p) + 3);
+        f[(__float_as_int(n3.x) == child) ? 2 : 3] = __uint_as_float(kind);
+    }
     while (p >= 0) {
         const float4 n3 = __ldcg(nodes + 4 * size_t(p) + 3);
         const int slot = (__float_as_int(n3.x) == child) ? 0 : 1;
@@ -441,27 +546,64 @@ ThingDev thing_dev(const ThingHost& th) {
     return d;
 }
 
-// Uploads things + flattening descriptors of all scenes and flattens into
-// g.prims_flat (primitive-id order, segment after segment).
-void flatten(Geometry& g, const std::vector<Scene*>& scenes, cudaStream_t s) {
+// In the instanced layout a mesh thing is instanced (one top-level record
+// over a bottom-level hierarchy of its mesh) when its transform is diagonal
+// with +0 off-diagonal entries, so the on-the-fly world vertices and boxes
+// round exactly like the flat layout's, and its mesh is large enough for a
+// hierarchy of its own to pay.
+constexpr uint32_t kInstanceMinTris = 16;
+
+bool diagonal_pos0(const float* T) {
+    const int off[6] = {1, 2, 4, 6, 8, 9};
+    for (int k : off) {
+        uint32_t b;
+        std::memcpy(&b, &T[k], 4);
+        if (b != 0u) return false;
+    }
+    return true;
+}
+
+bool instance_thing(const ThingHost& th, const Scene& sc, int layout) {
+    if (layout != RT_LAYOUT_INSTANCED || th.mesh < 0) return false;
+    return diagonal_pos0(th.T) && sc.meshes[th.mesh].ni >= kInstanceMinTris;
+}
+
+// Host plan of a geometry: per-thing descriptors, optics, instance data and
+// the bottom-level mesh table.
+struct Plan {
     std::vector<FlatDesc> desc;
     std::vector<ThingDev> td;
-    g.seg_host.assign(scenes.size(), SegDev{0, 0});
-    g.thing_begin.assign(scenes.size(), 0);
-    g.optics_seen.assign(scenes.size(), 0);
-    uint64_t off = 0;
+    std::vector<InstDev> inst;
+    std::vector<BlasMesh> meshes;
+    std::vector<SegDev> top_segs, bottom_segs;
+    std::vector<uint32_t> thing_begin;
+    std::vector<int> inst_class;
+    uint64_t nprims = 0, ntop = 0, nbottom = 0;
+    uint32_t ninstances = 0;
+};
+
+Plan make_plan(const std::vector<Scene*>& scenes, int layout) {
+    Plan P;
+    P.thing_begin.assign(scenes.size(), 0);
+    P.top_segs.assign(scenes.size(), SegDev{0, 0});
     for (size_t si = 0; si < scenes.size(); ++si) {
         const Scene& sc = *scenes[si];
-        g.seg_host[si].prim_begin = uint32_t(off);
-        g.thing_begin[si] = uint32_t(desc.size());
+        P.thing_begin[si] = uint32_t(P.desc.size());
+        P.top_segs[si].prim_begin = uint32_t(P.ntop);
+        std::vector<int> mesh_seg(sc.meshes.size(), -1);   // bottom-level segment of each mesh of this scene
         for (const ThingHost& th : sc.things) {
             FlatDesc d;
             std::memset(&d, 0, sizeof(d));
-            d.prim_offset = uint32_t(off);
+            d.prim_offset = uint32_t(P.nprims);
             d.seg = uint32_t(si);
+            d.top_offset = uint32_t(P.ntop);
+            d.blas_root = -1;
+            InstDev in;
+            std::memset(&in, 0, sizeof(in));
             if (th.mesh < 0) {
                 d.analytic = 1;
                 d.nprims = 1;
+                d.ntop = 1;
                 d.sphere = make_float4(th.center.x, th.center.y, th.center.z, th.radius);
             } else {
                 const MeshDev& m = sc.meshes[th.mesh];
@@ -469,120 +611,229 @@ void flatten(Geometry& g, const std::vector<Scene*>& scenes, cudaStream_t s) {
                 d.idx = m.i.as<uint3>();
                 d.nprims = m.ni;
                 std::memcpy(d.T, th.T, sizeof(d.T));
+                if (instance_thing(th, sc, layout)) {
+                    if (mesh_seg[th.mesh] < 0) {
+                        mesh_seg[th.mesh] = int(P.meshes.size());
+                        P.meshes.push_back(BlasMesh{d.v, d.idx, uint32_t(P.nbottom), m.ni});
+                        P.bottom_segs.push_back(SegDev{uint32_t(P.nbottom), m.ni});
+                        P.nbottom += m.ni;
+                        RT_REQUIRE(P.nbottom < (uint64_t(1) << 31), "too many bottom-level triangles (>= 2^31)");
+                    }
+                    const SegDev& bs = P.bottom_segs[mesh_seg[th.mesh]];
+                    d.instanced = 1;
+                    d.ntop = 1;
+                    d.blas_seg = uint32_t(mesh_seg[th.mesh]);
+                    d.blas_root = int(bs.prim_begin);   // a segment's root is its first node slot
+                    in.a = make_float4(th.T[0], th.T[5], th.T[10], th.T[3]);
+                    uint32_t po = d.prim_offset;
+                    float pof, rootf;
+                    std::memcpy(&pof, &po, 4);
+                    std::memcpy(&rootf, &d.blas_root, 4);
+                    in.b = make_float4(th.T[7], th.T[11], pof, rootf);
+                    P.ninstances += 1;
+                } else {
+                    d.ntop = m.ni;
+                }
             }
-            off += d.nprims;
-            RT_REQUIRE(off < (uint64_t(1) << 31), "too many primitives (>= 2^31)");
-            desc.push_back(d);
-            td.push_back(thing_dev(th));
+            P.nprims += d.nprims;
+            P.ntop += d.ntop;
+            RT_REQUIRE(P.nprims < (uint64_t(1) << 31), "too many primitives (>= 2^31)");
+            RT_REQUIRE(P.ntop < (uint64_t(1) << 31), "too many top-level records (>= 2^31)");
+            P.inst_class.push_back(d.instanced);
+            P.desc.push_back(d);
+            P.td.push_back(thing_dev(th));
+            P.inst.push_back(in);
         }
-        g.seg_host[si].prim_count = uint32_t(off) - g.seg_host[si].prim_begin;
-        g.optics_seen[si] = sc.optics_version;
+        P.top_segs[si].prim_count = uint32_t(P.ntop) - P.top_segs[si].prim_begin;
     }
-    g.nprims = uint32_t(off);
-    g.nthings = uint32_t(desc.size());
-    g.nsegs = uint32_t(scenes.size());
-    g.desc.reserve(std::max<size_t>(1, desc.size()) * sizeof(FlatDesc));
-    g.things_dev.reserve(std::max<size_t>(1, td.size()) * sizeof(ThingDev));
-    g.segs.reserve(std::max<size_t>(1, g.seg_host.size()) * sizeof(SegDev));
-    if (!desc.empty()) {
-        RT_CUDA(cudaMemcpyAsync(g.desc.p, desc.data(), desc.size() * sizeof(FlatDesc), cudaMemcpyHostToDevice, s));
-        RT_CUDA(cudaMemcpyAsync(g.things_dev.p, td.data(), td.size() * sizeof(ThingDev), cudaMemcpyHostToDevice, s));
-    }
-    if (!g.seg_host.empty())
-        RT_CUDA(cudaMemcpyAsync(g.segs.p, g.seg_host.data(), g.seg_host.size() * sizeof(SegDev),
-                                cudaMemcpyHostToDevice, s));
-    g.prims_flat.reserve(std::max<size_t>(1, g.nprims) * 48);
-    if (g.nsegs > 1) g.prim_seg.reserve(std::max<size_t>(1, g.nprims) * 4);
-    if (g.nprims) {
-        k_flatten<<<grid_for(g.nprims), kThreads, 0, s>>>(g.desc.as<FlatDesc>(), g.nthings, g.nprims,
-                                                           g.prims_flat.as<float4>(),
-                                                           g.nsegs > 1 ? g.prim_seg.as<uint32_t>() : nullptr);
-        RT_CHECK_LAUNCH();
-    }
-    RT_CUDA(cudaStreamSynchronize(s));   // the host staging vectors must outlive the copies
+    return P;
 }
 
-void refit(Geometry& g, cudaStream_t s) {
-    const uint32_t n = g.nprims;
-    if (n == 0) return;
-    k_gather_prims<<<grid_for(n), kThreads, 0, s>>>(g.prims_flat.as<float4>(), g.ids.as<uint32_t>(), n,
-                                                     g.prims.as<float4>());
+void upload_lbvh_segments(Lbvh& L, const std::vector<SegDev>& segs, uint64_t nrec, cudaStream_t s) {
+    L.seg_host = segs;
+    L.nsegs = uint32_t(segs.size());
+    L.nprims = uint32_t(nrec);
+    L.segs.reserve(std::max<size_t>(1, segs.size()) * sizeof(SegDev));
+    if (!segs.empty())
+        RT_CUDA(cudaMemcpyAsync(L.segs.p, segs.data(), segs.size() * sizeof(SegDev), cudaMemcpyHostToDevice, s));
+    L.prims_flat.reserve(std::max<size_t>(1, nrec) * 48);
+    if (L.nsegs > 1) L.prim_seg.reserve(std::max<size_t>(1, nrec) * 4);
+}
+
+// Uploads the plan (descriptors, optics, instance data, segment tables).
+void upload_plan(Geometry& g, const Plan& P, size_t nscenes, cudaStream_t s) {
+    g.nprims = uint32_t(P.nprims);
+    g.nthings = uint32_t(P.desc.size());
+    g.nsegs = uint32_t(nscenes);
+    g.ninstances = P.ninstances;
+    g.thing_begin = P.thing_begin;
+    g.inst_class = P.inst_class;
+    g.desc_host = P.desc;
+    g.desc.reserve(std::max<size_t>(1, P.desc.size()) * sizeof(FlatDesc));
+    g.things_dev.reserve(std::max<size_t>(1, P.td.size()) * sizeof(ThingDev));
+    g.inst.reserve(std::max<size_t>(1, P.inst.size()) * sizeof(InstDev));
+    if (!P.desc.empty()) {
+        RT_CUDA(cudaMemcpyAsync(g.desc.p, P.desc.data(), P.desc.size() * sizeof(FlatDesc), cudaMemcpyHostToDevice, s));
+        RT_CUDA(cudaMemcpyAsync(g.things_dev.p, P.td.data(), P.td.size() * sizeof(ThingDev), cudaMemcpyHostToDevice, s));
+        RT_CUDA(cudaMemcpyAsync(g.inst.p, P.inst.data(), P.inst.size() * sizeof(InstDev), cudaMemcpyHostToDevice, s));
+    }
+    upload_lbvh_segments(g.top, P.top_segs, P.ntop, s);
+    upload_lbvh_segments(g.blas, P.bottom_segs, P.nbottom, s);
+}
+
+void flatten_bottom(Geometry& g, const Plan& P, cudaStream_t s) {
+    if (g.blas.nprims == 0) return;
+    DevBuf meshes;
+    meshes.reserve(P.meshes.size() * sizeof(BlasMesh));
+    RT_CUDA(cudaMemcpyAsync(meshes.p, P.meshes.data(), P.meshes.size() * sizeof(BlasMesh), cudaMemcpyHostToDevice, s));
+    k_flatten_bottom<<<grid_for(g.blas.nprims), kThreads, 0, s>>>(
+        meshes.as<BlasMesh>(), uint32_t(P.meshes.size()), g.blas.nprims, g.blas.prims_flat.as<float4>(),
+        g.blas.nsegs > 1 ? g.blas.prim_seg.as<uint32_t>() : nullptr);
     RT_CHECK_LAUNCH();
-    int* parents = g.parents.as<int>();
-    RT_CUDA(cudaMemsetAsync(g.flags.p, 0, size_t(n) * sizeof(uint32_t), s));
-    k_refit<<<grid_for(n), kThreads, 0, s>>>(g.prims.as<float4>(), n, g.nodes.as<float4>(), parents, parents + n,
-                                              g.flags.as<uint32_t>());
+    RT_CUDA(cudaStreamSynchronize(s));   // `meshes` and the plan's host arrays must outlive the copies
+}
+
+void flatten_top(Geometry& g, cudaStream_t s) {
+    if (g.top.nprims == 0) return;
+    k_flatten_top<<<grid_for(g.top.nprims), kThreads, 0, s>>>(
+        g.desc.as<FlatDesc>(), g.nthings, g.top.nprims, g.blas.nodes.p ? g.blas.nodes.as<float4>() : nullptr,
+        g.top.prims_flat.as<float4>(), g.top.nsegs > 1 ? g.top.prim_seg.as<uint32_t>() : nullptr);
+    RT_CHECK_LAUNCH();
+}
+
+void refit(Lbvh& L, cudaStream_t s) {
+    const uint32_t n = L.nprims;
+    if (n == 0) return;
+    k_gather_prims<<<grid_for(n), kThreads, 0, s>>>(L.prims_flat.as<float4>(), L.ids.as<uint32_t>(), n,
+                                                     L.prims.as<float4>());
+    RT_CHECK_LAUNCH();
+    int* parents = L.parents.as<int>();
+    RT_CUDA(cudaMemsetAsync(L.flags.p, 0, size_t(n) * sizeof(uint32_t), s));
+    k_refit<<<grid_for(n), kThreads, 0, s>>>(L.prims.as<float4>(), n, L.nodes.as<float4>(), parents, parents + n,
+                                              L.flags.as<uint32_t>());
     RT_CHECK_LAUNCH();
 }
 
 template <class K>
-void build_topology(Geometry& g, cudaStream_t s) {
-    const uint32_t n = g.nprims;
-    g.codes.reserve(size_t(n) * sizeof(K));
-    g.ids.reserve(size_t(n) * sizeof(uint32_t));
-    K* codes = g.codes.as<K>();
-    uint32_t* ids = g.ids.as<uint32_t>();
-    const uint32_t* pseg = g.nsegs > 1 ? g.prim_seg.as<uint32_t>() : nullptr;
-    k_morton<K><<<grid_for(n), kThreads, 0, s>>>(g.prims_flat.as<float4>(), pseg, n, g.bounds.as<uint32_t>(), codes,
-                                                  ids);
+void build_topology(Lbvh& L, cudaStream_t s) {
+    const uint32_t n = L.nprims;
+    L.codes.reserve(size_t(n) * sizeof(K));
+    L.ids.reserve(size_t(n) * sizeof(uint32_t));
+    K* codes = L.codes.as<K>();
+    uint32_t* ids = L.ids.as<uint32_t>();
+    const uint32_t* pseg = L.nsegs > 1 ? L.prim_seg.as<uint32_t>() : nullptr;
+    int key_bits = L.morton_bits;
+    if (L.grouped) {
+        k_morton_grouped<<<grid_for(n), kThreads, 0, s>>>(L.prims_flat.as<float4>(), n, L.tbounds.as<uint32_t>(),
+                                                           L.trank.as<uint32_t>(),
+                                                           reinterpret_cast<unsigned long long*>(codes), ids);
+        int rank_bits = 1;
+        while ((uint64_t(1) << rank_bits) < L.nthings) ++rank_bits;
+        key_bits = 30 + rank_bits;
+    } else {
+        k_morton<K><<<grid_for(n), kThreads, 0, s>>>(L.prims_flat.as<float4>(), pseg, n, L.bounds.as<uint32_t>(),
+                                                      codes, ids);
+    }
     RT_CHECK_LAUNCH();
     if (sizeof(K) == 4)
-        radix_sort_pairs_u32(reinterpret_cast<uint32_t*>(codes), ids, n, g.morton_bits, g.sort_tmp, s);
+        radix_sort_pairs_u32(reinterpret_cast<uint32_t*>(codes), ids, n, key_bits, L.sort_tmp, s);
     else
-        radix_sort_pairs_u64(reinterpret_cast<unsigned long long*>(codes), ids, n, g.morton_bits, g.sort_tmp, s);
-    if (g.nsegs > 1) {
+        radix_sort_pairs_u64(reinterpret_cast<unsigned long long*>(codes), ids, n, key_bits, L.sort_tmp, s);
+    if (L.nsegs > 1) {
         // stable second pass by segment: (segment, code) order
         int seg_bits = 1;
-        while ((1u << seg_bits) < g.nsegs) ++seg_bits;
+        while ((1u << seg_bits) < L.nsegs) ++seg_bits;
         const size_t kb = size_t(n) * sizeof(K);
-        g.seg_tmp.reserve(2 * size_t(n) * 4 + kb + size_t(n) * 4);
-        uint32_t* keys = g.seg_tmp.as<uint32_t>();
+        L.seg_tmp.reserve(2 * size_t(n) * 4 + kb + size_t(n) * 4);
+        uint32_t* keys = L.seg_tmp.as<uint32_t>();
         uint32_t* perm = keys + n;
         K* codes2 = reinterpret_cast<K*>(perm + n);
         uint32_t* ids2 = reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(codes2) + kb);
         k_seg_keys<<<grid_for(n), kThreads, 0, s>>>(pseg, ids, n, keys, perm);
         RT_CHECK_LAUNCH();
-        radix_sort_pairs_u32(keys, perm, n, seg_bits, g.sort_tmp, s);
+        radix_sort_pairs_u32(keys, perm, n, seg_bits, L.sort_tmp, s);
         k_permute<K><<<grid_for(n), kThreads, 0, s>>>(codes, ids, perm, n, codes2, ids2);
         RT_CHECK_LAUNCH();
         RT_CUDA(cudaMemcpyAsync(codes, codes2, kb, cudaMemcpyDeviceToDevice, s));
         RT_CUDA(cudaMemcpyAsync(ids, ids2, size_t(n) * 4, cudaMemcpyDeviceToDevice, s));
     }
-    int* parents = g.parents.as<int>();
-    k_karras<K><<<grid_for(n), kThreads, 0, s>>>(codes, g.segs.as<SegDev>(), g.nsegs, n, g.nodes.as<float4>(), parents,
+    int* parents = L.parents.as<int>();
+    k_karras<K><<<grid_for(n), kThreads, 0, s>>>(codes, L.segs.as<SegDev>(), L.nsegs, n, L.nodes.as<float4>(), parents,
                                                   parents + n);
     RT_CHECK_LAUNCH();
 }
 
+// Morton codes (or things-grouped keys, for top-level records whose a.w is
+// the thing), sort, hierarchy and refit of an LBVH whose records are in
+// prims_flat.
+void build_lbvh(Lbvh& L, int morton_bits, cudaStream_t s, const FlatDesc* desc = nullptr, uint32_t nthings = 0) {
+    L.morton_bits = morton_bits;
+    L.grouped = desc != nullptr && nthings > 0;
+    L.nthings = nthings;
+    const uint32_t n = L.nprims;
+    L.prims.reserve(std::max<size_t>(1, n) * 48);
+    L.nodes.reserve(std::max<size_t>(1, n) * 64);
+    L.parents.reserve((size_t(n) * 2 + 1) * sizeof(int));
+    L.flags.reserve(std::max<size_t>(1, n) * sizeof(uint32_t));
+    L.bounds.reserve(std::max<size_t>(1, L.nsegs) * 6 * sizeof(uint32_t));
+    if (n == 0) return;
+    k_init_bounds<<<grid_for(6 * L.nsegs), kThreads, 0, s>>>(L.bounds.as<uint32_t>(), L.nsegs);
+    RT_CHECK_LAUNCH();
+    k_centroid_bounds<<<grid_for(n), kThreads, 0, s>>>(L.prims_flat.as<float4>(),
+                                                        L.nsegs > 1 ? L.prim_seg.as<uint32_t>() : nullptr, n,
+                                                        L.bounds.as<uint32_t>(), 0);
+    RT_CHECK_LAUNCH();
+    if (L.grouped) {
+        L.tbounds.reserve(size_t(nthings) * 6 * sizeof(uint32_t));
+        L.tcodes.reserve(size_t(nthings) * 8);
+        L.tids.reserve(size_t(nthings) * 4);
+        L.trank.reserve(size_t(nthings) * 4);
+        k_init_bounds<<<grid_for(6 * nthings), kThreads, 0, s>>>(L.tbounds.as<uint32_t>(), nthings);
+        RT_CHECK_LAUNCH();
+        k_centroid_bounds<<<grid_for(n), kThreads, 0, s>>>(L.prims_flat.as<float4>(), nullptr, n,
+                                                            L.tbounds.as<uint32_t>(), 1);
+        RT_CHECK_LAUNCH();
+        k_thing_codes<<<grid_for(nthings), kThreads, 0, s>>>(L.tbounds.as<uint32_t>(), desc, L.bounds.as<uint32_t>(),
+                                                              nthings, L.tcodes.as<unsigned long long>(),
+                                                              L.tids.as<uint32_t>());
+        RT_CHECK_LAUNCH();
+        radix_sort_pairs_u64(L.tcodes.as<unsigned long long>(), L.tids.as<uint32_t>(), nthings, 60, L.sort_tmp, s);
+        k_thing_rank<<<grid_for(nthings), kThreads, 0, s>>>(L.tids.as<uint32_t>(), nthings, L.trank.as<uint32_t>());
+        RT_CHECK_LAUNCH();
+        build_topology<unsigned long long>(L, s);
+    } else if (morton_bits == 30) {
+        build_topology<uint32_t>(L, s);
+    } else {
+        build_topology<unsigned long long>(L, s);
+    }
+    refit(L, s);
+}
+
 }  // namespace
 
-void build_geometry(Geometry& g, const std::vector<Scene*>& scenes, int morton_bits, cudaStream_t s) {
+void build_geometry(Geometry& g, const std::vector<Scene*>& scenes, int morton_bits, int layout, cudaStream_t s) {
     RT_REQUIRE(morton_bits == 0 || morton_bits == 30 || morton_bits == 60, "morton_bits must be 0, 30 or 60");
+    RT_REQUIRE(layout >= RT_LAYOUT_AUTO && layout <= RT_LAYOUT_GROUPED, "unknown layout");
     RT_REQUIRE(!scenes.empty(), "no scenes to build");
     g.morton_bits = morton_bits == 0 ? 60 : morton_bits;
+    g.layout_req = layout;
     cudaEvent_t e0, e1;
     RT_CUDA(cudaEventCreate(&e0));
     RT_CUDA(cudaEventCreate(&e1));
     RT_CUDA(cudaEventRecord(e0, s));
-    flatten(g, scenes, s);
-    const uint32_t n = g.nprims;
-    g.prims.reserve(std::max<size_t>(1, n) * 48);
-    g.nodes.reserve(std::max<size_t>(1, n) * 64);
-    g.parents.reserve((size_t(n) * 2 + 1) * sizeof(int));
-    g.flags.reserve(std::max<size_t>(1, n) * sizeof(uint32_t));
-    g.bounds.reserve(size_t(g.nsegs) * 6 * sizeof(uint32_t));
+    const Plan P = make_plan(scenes, layout);
+    upload_plan(g, P, scenes.size(), s);
+    g.layout = P.ninstances ? RT_LAYOUT_INSTANCED
+                            : (layout == RT_LAYOUT_AUTO || layout == RT_LAYOUT_GROUPED) ? RT_LAYOUT_GROUPED
+                                                                                       : RT_LAYOUT_FLAT;
+    g.optics_seen.assign(scenes.size(), 0);
+    for (size_t si = 0; si < scenes.size(); ++si) g.optics_seen[si] = scenes[si]->optics_version;
     g.misc.reserve(256);
-    if (n > 0) {
-        k_init_bounds<<<grid_for(6 * g.nsegs), kThreads, 0, s>>>(g.bounds.as<uint32_t>(), g.nsegs);
-        RT_CHECK_LAUNCH();
-        k_centroid_bounds<<<grid_for(n), kThreads, 0, s>>>(g.prims_flat.as<float4>(),
-                                                            g.nsegs > 1 ? g.prim_seg.as<uint32_t>() : nullptr, n,
-                                                            g.bounds.as<uint32_t>());
-        RT_CHECK_LAUNCH();
-        if (g.morton_bits == 30) build_topology<uint32_t>(g, s);
-        else build_topology<unsigned long long>(g, s);
-        refit(g, s);
-    }
+    flatten_bottom(g, P, s);
+    build_lbvh(g.blas, g.morton_bits, s);   // object space, before the instance boxes are taken
+    flatten_top(g, s);
+    const bool grouped = layout == RT_LAYOUT_AUTO || layout == RT_LAYOUT_GROUPED;
+    build_lbvh(g.top, g.morton_bits, s, grouped ? g.desc.as<FlatDesc>() : nullptr, grouped ? g.nthings : 0);
     RT_CUDA(cudaEventRecord(e1, s));
     RT_CUDA(cudaEventSynchronize(e1));
     RT_CUDA(cudaEventElapsedTime(&g.build_ms, e0, e1));
@@ -591,16 +842,28 @@ void build_geometry(Geometry& g, const std::vector<Scene*>& scenes, int morton_b
 }
 
 void refit_geometry(Geometry& g, const std::vector<Scene*>& scenes, cudaStream_t s) {
+    const Plan P = make_plan(scenes, g.layout_req);
+    if (P.inst_class != g.inst_class || P.ntop != g.top.nprims || P.nbottom != g.blas.nprims) {
+        // a thing changed between instanced and flattened: the hierarchy changes
+        build_geometry(g, scenes, g.morton_bits, g.layout_req, s);
+        g.refit_ms = g.build_ms;
+        return;
+    }
     cudaEvent_t e0, e1;
     RT_CUDA(cudaEventCreate(&e0));
     RT_CUDA(cudaEventCreate(&e1));
     RT_CUDA(cudaEventRecord(e0, s));
-    const uint32_t before = g.nprims;
-    flatten(g, scenes, s);
-    RT_REQUIRE(g.nprims == before, "primitive count changed; rebuild instead of refit");
-    refit(g, s);
+    // transforms only reach the descriptors, instance data and the top level;
+    // the bottom level is in object space and stays as built
+    g.desc_host = P.desc;
+    RT_CUDA(cudaMemcpyAsync(g.desc.p, P.desc.data(), P.desc.size() * sizeof(FlatDesc), cudaMemcpyHostToDevice, s));
+    RT_CUDA(cudaMemcpyAsync(g.things_dev.p, P.td.data(), P.td.size() * sizeof(ThingDev), cudaMemcpyHostToDevice, s));
+    RT_CUDA(cudaMemcpyAsync(g.inst.p, P.inst.data(), P.inst.size() * sizeof(InstDev), cudaMemcpyHostToDevice, s));
+    for (size_t si = 0; si < scenes.size(); ++si) g.optics_seen[si] = scenes[si]->optics_version;
+    flatten_top(g, s);
+    refit(g.top, s);
     RT_CUDA(cudaEventRecord(e1, s));
-    RT_CUDA(cudaEventSynchronize(e1));
+    RT_CUDA(cudaEventSynchronize(e1));   // the plan's host arrays must outlive the copies
     RT_CUDA(cudaEventElapsedTime(&g.refit_ms, e0, e1));
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -623,10 +886,25 @@ void sync_optics(Geometry& g, const std::vector<Scene*>& scenes, cudaStream_t s)
     RT_CUDA(cudaStreamSynchronize(s));
 }
 
+size_t Lbvh::device_bytes() const {
+    return segs.bytes + prim_seg.bytes + prims_flat.bytes + prims.bytes + nodes.bytes + codes.bytes + ids.bytes +
+           parents.bytes + flags.bytes + bounds.bytes + sort_tmp.bytes + seg_tmp.bytes;
+}
+
 size_t Geometry::device_bytes() const {
-    return things_dev.bytes + desc.bytes + segs.bytes + prim_seg.bytes + prims_flat.bytes + prims.bytes + nodes.bytes +
-           codes.bytes + ids.bytes + parents.bytes + flags.bytes + bounds.bytes + sort_tmp.bytes + seg_tmp.bytes +
-           misc.bytes;
+    return things_dev.bytes + desc.bytes + inst.bytes + misc.bytes + top.device_bytes() + blas.device_bytes();
+}
+
+GeoView Geometry::view() const {
+    GeoView v;
+    v.tnodes = top.nodes.as<float4>();
+    v.tprims = top.prims.as<float4>();
+    v.bnodes = blas.nodes.as<float4>();
+    v.bprims = blas.prims.as<float4>();
+    v.inst = inst.as<InstDev>();
+    v.desc = desc.as<FlatDesc>();
+    v.instanced = ninstances > 0 ? 1 : 0;
+    return v;
 }
 
 size_t Scene::device_bytes() const {
@@ -643,7 +921,7 @@ Scene* scene_from(rt_scene h) {
 namespace {
 
 void scene_build(Scene& sc, int morton_bits, cudaStream_t s) {
-    build_geometry(sc.geo, {&sc}, morton_bits, s);
+    build_geometry(sc.geo, {&sc}, morton_bits, sc.layout, s);
     sc.built = true;
     sc.topology_dirty = false;
     sc.xf_dirty = false;
@@ -842,6 +1120,15 @@ rt_status rt_scene_set_optics(rt_scene scene, unsigned int thing_id, const rt_op
     });
 }
 
+rt_status rt_scene_set_layout(rt_scene scene, int layout) {
+    return guarded([&] {
+        RT_REQUIRE(layout >= RT_LAYOUT_AUTO && layout <= RT_LAYOUT_GROUPED, "unknown layout");
+        Scene* sc = scene_from(scene);
+        if (sc->layout != layout) sc->topology_dirty = true;
+        sc->layout = layout;
+    });
+}
+
 rt_status rt_scene_build(rt_scene scene, unsigned int morton_bits, void* stream) {
     return guarded([&] { scene_build(*scene_from(scene), int(morton_bits), as_stream(stream)); });
 }
@@ -861,6 +1148,10 @@ rt_status rt_scene_info_get(rt_scene scene, rt_scene_info* info) {
         info->device_bytes = sc->device_bytes();
         info->build_ms = sc->geo.build_ms;
         info->refit_ms = sc->geo.refit_ms;
+        info->layout = unsigned(sc->geo.layout);
+        info->n_instances = sc->geo.ninstances;
+        info->n_top_records = sc->geo.top.nprims;
+        info->n_bottom_records = sc->geo.blas.nprims;
     });
 }
 
@@ -869,7 +1160,7 @@ rt_status rt_scene_get_lbvh(rt_scene scene, unsigned long long* codes, unsigned 
     return guarded([&] {
         Scene* sc = scene_from(scene);
         if (!sc->built) throw Error(RT_ERR_NOT_BUILT, "scene not built");
-        const Geometry& g = sc->geo;
+        const Lbvh& g = sc->geo.top;
         const uint32_t n = g.nprims;
         if (n == 0) return;
         if (codes) {

@@ -23,70 +23,84 @@ struct ThingHost {
     float radius = 0.f;     // analytic sphere radius
 };
 
-// Flattening descriptor of one thing (device copy in Geometry::desc).
-struct FlatDesc {
-    const float3* v;
-    const uint3* idx;
-    uint32_t prim_offset;   // global first primitive
-    uint32_t nprims;
-    int analytic;
-    uint32_t seg;           // segment (scene) of the thing
-    float T[12];
-    float4 sphere;          // centre, radius
-};
-
-// Segment (one scene) of a geometry: its primitives are [prim_begin,
-// prim_begin + prim_count) in leaf order and its internal nodes occupy node
-// slots [prim_begin, prim_begin + prim_count - 1); the root is node prim_begin.
+// Segment of an LBVH: its primitives are [prim_begin, prim_begin +
+// prim_count) in leaf order and its internal nodes occupy node slots
+// [prim_begin, prim_begin + prim_count - 1); the root is node prim_begin.
 struct SegDev {
     uint32_t prim_begin, prim_count;
 };
 
-struct Scene;
-
-// Device arrays of one or more scenes built together: primitive records in
-// leaf order, LBVH nodes, per-thing optics.  A single scene is a geometry of
-// one segment; a batch concatenates many scenes into segments and builds all
-// their hierarchies in one segmented pass.
-struct Geometry {
-    DevBuf things_dev;      // ThingDev[n_things]
-    DevBuf desc;            // FlatDesc[n_things]
+// One LBVH over 48-B primitive records, possibly segmented (one independent
+// hierarchy per segment, all built in one pass).
+struct Lbvh {
     DevBuf segs;            // SegDev[n_segs]
-    DevBuf prim_seg;        // segment of each primitive (primitive-id order)
-    DevBuf prims_flat;      // 3 float4 per primitive, primitive-id order
-    DevBuf prims;           // 3 float4 per primitive, LBVH leaf order
-    DevBuf nodes;           // 4 float4 per node slot (one slot per primitive)
+    DevBuf prim_seg;        // segment of each record (record-id order), n_segs > 1 only
+    DevBuf prims_flat;      // 3 float4 per record, record-id order
+    DevBuf prims;           // 3 float4 per record, leaf order
+    DevBuf nodes;           // 4 float4 per node slot (one slot per record)
     DevBuf codes;           // sorted Morton codes (u32 or u64)
-    DevBuf ids;             // sorted primitive ids
+    DevBuf ids;             // sorted record ids
     DevBuf parents;         // leaf parents [n] then node parents [n]
     DevBuf flags;           // refit arrival counters [n]
     DevBuf bounds;          // centroid bounds per segment, 6 orderable u32 each
     DevBuf sort_tmp, seg_tmp;
-    DevBuf misc;            // small device scratch (error words)
-
-    uint32_t nprims = 0, nthings = 0, nsegs = 0;
+    DevBuf tbounds, tcodes, tids, trank;   // things-grouped keys: per-thing bounds, codes, order, rank
+    uint32_t nprims = 0, nsegs = 0, nthings = 0;
     int morton_bits = 60;
+    int grouped = 0;
     std::vector<SegDev> seg_host;
-    std::vector<uint32_t> thing_begin;   // first global thing of each segment
-    std::vector<uint64_t> optics_seen;   // optics version of each segment's scene at the last upload
-    std::vector<ThingDev> things_host;   // staging copy of things_dev
-    float build_ms = 0.f, refit_ms = 0.f;
-
     size_t device_bytes() const;
     int root(uint32_t seg) const { return seg_host[seg].prim_count ? int(seg_host[seg].prim_begin) : -1; }
 };
 
-// (Re)builds `g` from the things of `scenes` (one segment each): flattening,
-// per-segment centroid bounds, Morton codes, sort by (segment, code), Karras
-// hierarchy per segment, bottom-up refit.  Synchronous on `s`.
-void build_geometry(Geometry& g, const std::vector<Scene*>& scenes, int morton_bits, cudaStream_t s);
-// Re-flattens with the scenes' current transforms/optics and refits.
+struct Scene;
+
+// Device arrays of one or more scenes built together.  The top level holds,
+// per scene segment, one record per analytic sphere, one instance record per
+// instanced mesh thing and the world-space triangles of flattened mesh things;
+// the bottom level holds, per instanced mesh, its object-space triangles.  The
+// flat layout (every mesh flattened, no bottom level) is the same structure
+// with no instances.
+struct Geometry {
+    DevBuf things_dev;      // ThingDev[n_things]
+    DevBuf desc;            // FlatDesc[n_things]
+    DevBuf inst;            // InstDev[n_things]
+    DevBuf misc;            // small device scratch (error words)
+    Lbvh top, blas;
+
+    uint32_t nprims = 0;    // global primitives (what the scene renders)
+    uint32_t nthings = 0, nsegs = 0, ninstances = 0;
+    int morton_bits = 60;
+    int layout = RT_LAYOUT_FLAT;      // resolved layout of the last build
+    int layout_req = RT_LAYOUT_AUTO;  // layout requested at the last build
+    std::vector<FlatDesc> desc_host;
+    std::vector<uint32_t> thing_begin;   // first global thing of each segment
+    std::vector<uint64_t> optics_seen;   // optics version of each segment's scene at the last upload
+    std::vector<ThingDev> things_host;   // staging copy of things_dev
+    std::vector<int> inst_class;         // per thing: 1 instanced, 0 not (for refit consistency)
+    float build_ms = 0.f, refit_ms = 0.f;
+
+    size_t device_bytes() const;
+    int root(uint32_t seg) const { return top.root(seg); }
+    GeoView view() const;
+};
+
+// (Re)builds `g` from the things of `scenes` (one segment each): the bottom
+// level over the instanced meshes (one segment each, object space), then the
+// top level (one segment per scene); each level is flattened to records, its
+// per-segment centroid bounds reduced, Morton codes sorted by (segment, code),
+// a Karras hierarchy emitted per segment and refit bottom-up.  Synchronous on
+// `s`.
+void build_geometry(Geometry& g, const std::vector<Scene*>& scenes, int morton_bits, int layout, cudaStream_t s);
+// Re-flattens the top level with the scenes' current transforms and refits it
+// (a full build when a thing changed between instanced and flattened).
 void refit_geometry(Geometry& g, const std::vector<Scene*>& scenes, cudaStream_t s);
 // Re-uploads the per-thing optics of `g` when any scene's optics changed
 // since they were last uploaded (optics need no refit).
 void sync_optics(Geometry& g, const std::vector<Scene*>& scenes, cudaStream_t s);
 
 struct Scene {
+    int layout = RT_LAYOUT_AUTO;  // requested layout of the next build
     std::vector<MeshDev> meshes;
     std::vector<ThingHost> things;
     Geometry geo;

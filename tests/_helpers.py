@@ -36,10 +36,12 @@ def golden_scene(seed):
     return np.loadtxt(os.path.join(GOLDEN, f"rtow_scene_seed{seed}.txt"))
 
 
-def rtow_pair(R, O, level, rng_kind=0, seed=1, half_extent=11, morton_bits=60):
-    """The same final scene in the product (GPU) and in the oracle (CPU)."""
-    sc = R.rtow_scene(level, rng_kind, seed, half_extent, morton_bits)
-    w, _ = O.rtow_world(level, rng_kind, seed, half_extent, morton_bits)
+def rtow_pair(R, O, level, rng_kind=0, seed=1, half_extent=11, morton_bits=60, layout=0):
+    """The same final scene in the product (GPU, any layout) and in the oracle
+    (CPU; flat LBVH, with things-grouped keys when the product's layout is
+    the default or RT_LAYOUT_GROUPED)."""
+    sc = R.rtow_scene(level, rng_kind, seed, half_extent, morton_bits, layout=layout)
+    w, _ = O.rtow_world(level, rng_kind, seed, half_extent, morton_bits, grouped=layout in (0, 3))
     return sc, w
 
 

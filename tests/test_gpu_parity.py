@@ -62,10 +62,12 @@ def test_radix_sort_stable_bit_exact(product, cuda, bits, n):
 
 
 # ------------------------------------------------------------------------ LBVH
-@pytest.mark.parametrize("bits", [30, 60])
+@pytest.mark.parametrize("bits,layout", [(30, 1), (60, 1), (60, 3)])
 @pytest.mark.parametrize("level", [None, 2, 3])
-def test_lbvh_bit_exact_vs_oracle_twin(product, oracle, cuda, bits, level):
-    sc, w = rtow_pair(product, oracle, level, morton_bits=bits)
+def test_lbvh_bit_exact_vs_oracle_twin(product, oracle, cuda, bits, level, layout):
+    """Morton (flat) or things-grouped (grouped) keys, sorted ids, Karras
+    children and refit boxes equal the oracle twin's bit for bit."""
+    sc, w = rtow_pair(product, oracle, level, morton_bits=bits, layout=layout)
     a, b = sc.lbvh(), w.lbvh()
     assert np.array_equal(a["codes"], b["codes"])
     assert np.array_equal(a["ids"], b["ids"])
@@ -74,8 +76,9 @@ def test_lbvh_bit_exact_vs_oracle_twin(product, oracle, cuda, bits, level):
     assert np.array_equal(a["boxes"].view(np.uint32), b["boxes"].view(np.uint32))
 
 
-def test_lbvh_topology_is_a_binary_tree(product, cuda):
-    sc = product.rtow_scene(3)
+@pytest.mark.parametrize("layout", [1, 2, 3])
+def test_lbvh_topology_is_a_binary_tree(product, cuda, layout):
+    sc = product.rtow_scene(3, layout=layout)
     t = sc.lbvh()
     n = len(t["ids"])
     seen_leaf = np.zeros(n, bool)
@@ -93,10 +96,11 @@ def test_lbvh_topology_is_a_binary_tree(product, cuda):
 
 
 # ------------------------------------------------------------------- first hit
+@pytest.mark.parametrize("layout", [1, 2, 3])
 @pytest.mark.parametrize("level,w,h", [(None, 192, 108), (2, 192, 108), (3, 320, 180)])
-def test_first_hit_bit_exact_vs_oracle(product, oracle, cuda, level, w, h):
+def test_first_hit_bit_exact_vs_oracle(product, oracle, cuda, level, w, h, layout):
     R, O = product, oracle
-    sc, wd = rtow_pair(R, O, level)
+    sc, wd = rtow_pair(R, O, level, layout=layout)
     cam = R.rtow_camera(w, h)
     params = R.launch_params(w, h, 1, seed=4711)
     g = device_first_hit(R, cuda, sc, cam, params)
@@ -108,9 +112,10 @@ def test_first_hit_bit_exact_vs_oracle(product, oracle, cuda, level, w, h):
     assert (g["prim"] >= 0).mean() > 0.5
 
 
-def test_first_hit_equals_brute_force(product, oracle, cuda):
+@pytest.mark.parametrize("layout", [1, 2, 3])
+def test_first_hit_equals_brute_force(product, oracle, cuda, layout):
     R, O = product, oracle
-    sc, wd = rtow_pair(R, O, 1, half_extent=4)
+    sc, wd = rtow_pair(R, O, 1, half_extent=4, layout=layout)
     cam = R.rtow_camera(96, 64)
     params = R.launch_params(96, 64, 1, seed=7)
     g = device_first_hit(R, cuda, sc, cam, params, sample=3)
@@ -119,9 +124,10 @@ def test_first_hit_equals_brute_force(product, oracle, cuda):
     assert np.array_equal(g["t"].view(np.uint32), c["t"].view(np.uint32))
 
 
-def test_first_hit_t_within_1e5_of_fp64(product, oracle, cuda):
+@pytest.mark.parametrize("layout", [1, 2, 3])
+def test_first_hit_t_within_1e5_of_fp64(product, oracle, cuda, layout):
     R, O = product, oracle
-    sc, wd = rtow_pair(R, O, 3)
+    sc, wd = rtow_pair(R, O, 3, layout=layout)
     cam = R.rtow_camera(256, 144)
     params = R.launch_params(256, 144, 1, seed=11)
     g = device_first_hit(R, cuda, sc, cam, params)
@@ -150,11 +156,12 @@ def test_picker_matches_first_hit(product, oracle, cuda):
 
 
 # ----------------------------------------------------------------------- render
+@pytest.mark.parametrize("layout", [1, 2, 3])
 @pytest.mark.parametrize("level,w,h,spp,depth", [(None, 64, 36, 4, 50), (2, 64, 36, 3, 50), (3, 48, 32, 2, 8),
                                                  (2, 40, 30, 5, 1)])
-def test_render_bit_exact_vs_oracle(product, oracle, cuda, level, w, h, spp, depth):
+def test_render_bit_exact_vs_oracle(product, oracle, cuda, level, w, h, spp, depth, layout):
     R, O = product, oracle
-    sc, wd = rtow_pair(R, O, level)
+    sc, wd = rtow_pair(R, O, level, layout=layout)
     cam = R.rtow_camera(w, h)
     params = R.launch_params(w, h, spp, depth=depth, seed=4711, flags=R.RT_FLAG_GUIDES)
     out = R.render(sc, cam, params, guides=True)
@@ -166,10 +173,9 @@ def test_render_bit_exact_vs_oracle(product, oracle, cuda, level, w, h, spp, dep
     assert np.array_equal(out["albedos"].view(np.uint32), ref["albedos"].view(np.uint32))
 
 
-def test_render_chunked_and_small_waves_match(product, oracle, cuda, monkeypatch):
-    """Tiny result budget / wave size force many chunks and regenerations."""
+def test_render_small_waves_match(product, oracle, cuda, monkeypatch):
+    """A tiny wave forces many waves and regenerations."""
     R, O = product, oracle
-    monkeypatch.setenv("RTX_RESULT_MB", "1")
     monkeypatch.setenv("RTX_WAVE", "1000")
     sc, wd = rtow_pair(R, O, 2)
     cam = R.rtow_camera(128, 96)
@@ -201,9 +207,10 @@ def test_postproc_vs_oracle(product, oracle, cuda):
 
 
 # -------------------------------------------------------------- update / refit
-def test_update_refit_after_transform_edit(product, oracle, cuda):
+@pytest.mark.parametrize("layout", [1, 2, 3])
+def test_update_refit_after_transform_edit(product, oracle, cuda, layout):
     R, O = product, oracle
-    sc, wd = rtow_pair(R, O, 2)
+    sc, wd = rtow_pair(R, O, 2, layout=layout)
     moved = {0: None, 5: (1.5, 0.0, -2.0), 100: (0.0, 0.6, 0.3), 486: (-1.0, 0.5, 1.0)}
     for tid, dv in moved.items():
         st, T = sc.get_transform(tid)
