@@ -439,33 +439,26 @@ void build_lbvh(orc_world& w) {
     std::vector<uint64_t> code(n);
     std::vector<uint32_t> ids(n);
     const float lo3[3] = {lo.x, lo.y, lo.z}, hi3[3] = {hi.x, hi.y, hi.z};
+    // things-grouped hierarchy (see below): per-thing centroid bounds
+    const size_t nt = w.things.size();
+    std::vector<F3> tlo, thi;
     if (w.grouped) {
-        // Things-grouped keys: each thing's centroid bounds; a 60-bit code of
-        // their centre in the scene's centroid bounds; things ranked by (code,
-        // thing index); key = rank << 30 | 30-bit code inside the thing's bounds.
-        const size_t nt = w.things.size();
         const float inf = std::numeric_limits<float>::infinity();
-        std::vector<F3> tlo(nt, mk(inf, inf, inf)), thi(nt, mk(-inf, -inf, -inf));
+        tlo.assign(nt, mk(inf, inf, inf));
+        thi.assign(nt, mk(-inf, -inf, -inf));
         for (int i = 0; i < n; ++i) {
             const int t = w.prims[i].thing;
             tlo[t] = mk(fminf(tlo[t].x, cen[i].x), fminf(tlo[t].y, cen[i].y), fminf(tlo[t].z, cen[i].z));
             thi[t] = mk(fmaxf(thi[t].x, cen[i].x), fmaxf(thi[t].y, cen[i].y), fmaxf(thi[t].z, cen[i].z));
         }
-        std::vector<float> tc(3 * nt);
-        for (size_t t = 0; t < nt; ++t) st3(&tc[3 * t], mul(0.5f, add(tlo[t], thi[t])));
-        std::vector<uint64_t> tcode(nt);
-        std::vector<uint32_t> tid(nt), rank(nt);
-        orc_morton60(tc.data(), unsigned(nt), lo3, hi3, tcode.data());
-        std::iota(tid.begin(), tid.end(), 0u);
-        orc_stable_sort_pairs64(tcode.data(), tid.data(), unsigned(nt));
-        for (size_t k = 0; k < nt; ++k) rank[tid[k]] = uint32_t(k);
+        // key = thing << 30 | 30-bit Morton code inside the thing's centroid bounds
         for (int i = 0; i < n; ++i) {
             const int t = w.prims[i].thing;
             const F3 e = sub(thi[t], tlo[t]);
             const uint32_t qx = quant10(cen[i].x, tlo[t].x, e.x);
             const uint32_t qy = quant10(cen[i].y, tlo[t].y, e.y);
             const uint32_t qz = quant10(cen[i].z, tlo[t].z, e.z);
-            code[i] = (uint64_t(rank[t]) << 30) | ((expand10(qx) << 2) | (expand10(qy) << 1) | expand10(qz));
+            code[i] = (uint64_t(t) << 30) | ((expand10(qx) << 2) | (expand10(qy) << 1) | expand10(qz));
         }
     } else if (w.morton_bits == 30) {
         std::vector<uint32_t> c32(n);
@@ -480,8 +473,58 @@ void build_lbvh(orc_world& w) {
     w.order = ids;
     w.left.assign(n > 1 ? n - 1 : 0, 0);
     w.right.assign(n > 1 ? n - 1 : 0, 0);
-    if (n > 1) karras(code.data(), n, w.left.data(), w.right.data());
+    if (n > 1 && !w.grouped) karras(code.data(), n, w.left.data(), w.right.data());
     w.root = n > 1 ? 0 : ~0;
+    if (n > 1 && w.grouped) {
+        // Things-grouped hierarchy: a Karras hierarchy per thing over its keys
+        // (node slots b + i of a thing whose records start at b), then one over
+        // the things sorted by a 60-bit code of their centroid-bounds centre;
+        // internal node j of the thing tree lives in the spare slot of thing j
+        // (b_j + n_j - 1), a thing leaf points at the thing's subtree root (or
+        // its single record).
+        std::vector<uint32_t> tb(nt), tn(nt, 0);
+        for (size_t t = 0; t < nt; ++t) tb[t] = w.things[t].prim_offset;
+        for (int i = 0; i < n; ++i) tn[w.prims[i].thing] += 1;
+        std::vector<int32_t> L, R;
+        for (size_t t = 0; t < nt; ++t) {
+            const int m = int(tn[t]);
+            if (m < 2) continue;
+            L.assign(m - 1, 0);
+            R.assign(m - 1, 0);
+            karras(code.data() + tb[t], m, L.data(), R.data());
+            const int b0 = int(tb[t]);
+            auto g = [&](int32_t x) { return x >= 0 ? b0 + x : ~(b0 + ~x); };
+            for (int i = 0; i < m - 1; ++i) {
+                w.left[b0 + i] = g(L[i]);
+                w.right[b0 + i] = g(R[i]);
+            }
+        }
+        if (nt == 1) {
+            w.root = 0;   // n > 1 records of the one thing
+        } else {
+            std::vector<float> tc(3 * nt);
+            for (size_t t = 0; t < nt; ++t) st3(&tc[3 * t], mul(0.5f, add(tlo[t], thi[t])));
+            std::vector<uint64_t> tcode(nt);
+            std::vector<uint32_t> tsorted(nt);
+            orc_morton60(tc.data(), unsigned(nt), lo3, hi3, tcode.data());
+            std::iota(tsorted.begin(), tsorted.end(), 0u);
+            orc_stable_sort_pairs64(tcode.data(), tsorted.data(), unsigned(nt));
+            L.assign(nt - 1, 0);
+            R.assign(nt - 1, 0);
+            karras(tcode.data(), int(nt), L.data(), R.data());
+            auto spare = [&](size_t t) { return int(tb[t] + tn[t]) - 1; };
+            auto ref = [&](int32_t x) {
+                if (x >= 0) return spare(size_t(x));
+                const uint32_t t = tsorted[~x];
+                return tn[t] >= 2 ? int(tb[t]) : ~int(tb[t]);
+            };
+            for (size_t j = 0; j + 1 < nt; ++j) {
+                w.left[spare(j)] = ref(L[j]);
+                w.right[spare(j)] = ref(R[j]);
+            }
+            w.root = spare(0);
+        }
+    }
     // bottom-up refit (post order, iterative)
     w.cbox0.assign(n > 1 ? n - 1 : 0, Box{});
     w.cbox1.assign(n > 1 ? n - 1 : 0, Box{});
@@ -494,7 +537,7 @@ void build_lbvh(orc_world& w) {
         }
         // children of a Karras node always have larger or smaller index ranges;
         // a DFS post-order is the safe order.
-        std::vector<int> stack{0}, post;
+        std::vector<int> stack{w.root}, post;
         post.reserve(n - 1);
         while (!stack.empty()) {
             const int i = stack.back();
@@ -554,7 +597,7 @@ Hit closest_bvh(const orc_world& w, F3 o, F3 d) {
     }
     int stack[128];
     int sp = 0;
-    int node = 0;
+    int node = w.root;
     while (true) {
         float tn0, tn1;
         const bool h0 = slab(w.cbox0[node], o, inv, kTmin, best, tn0);

@@ -281,6 +281,7 @@ struct HitRec {
     int hit;        // 1 on a hit, 0 on a miss
     uint32_t id;    // global primitive id of the hit
     uint32_t thing; // thing of the hit
+    int leaf;       // top-level record of the hit, -1 for a bottom-level (instanced) triangle
     bool overflow;  // the traversal stack was full: a subtree was skipped
 };
 
@@ -306,7 +307,7 @@ __device__ __forceinline__ void trav_init(Trav& s, float3 o, float3 d, int root)
     s.d = d;
     s.inv = mk(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
     s.best = kTmax;
-    s.h = HitRec{0.f, 0.f, 0.f, 0, 0u, 0u, false};
+    s.h = HitRec{0.f, 0.f, 0.f, 0, 0u, 0u, -1, false};
     s.node = root;
     s.sp = 0;
     s.in_inst = false;
@@ -314,10 +315,10 @@ __device__ __forceinline__ void trav_init(Trav& s, float3 o, float3 d, int root)
 
 // Keeps a hit if it is the closest so far (smallest t, equal t -> larger
 // primitive id).
-__device__ __forceinline__ void trav_keep(Trav& s, float t, float u, float v, uint32_t id, uint32_t thing) {
+__device__ __forceinline__ void trav_keep(Trav& s, float t, float u, float v, uint32_t id, uint32_t thing, int leaf) {
     if (t > s.best) return;
     if (!s.h.hit || t < s.h.t || (t == s.h.t && id > s.h.id)) {
-        s.h.t = t; s.h.u = u; s.h.v = v; s.h.hit = 1; s.h.id = id; s.h.thing = thing;
+        s.h.t = t; s.h.u = u; s.h.v = v; s.h.hit = 1; s.h.id = id; s.h.thing = thing; s.h.leaf = leaf;
         s.best = t;
     }
 }
@@ -337,7 +338,7 @@ __device__ __forceinline__ void trav_leaf_top(Trav& s, const GeoView& g, int li,
         u = v = 0.f;
         hit = sph_test(xyz(a), b.x, s.o, s.d, t);
     }
-    if (hit) trav_keep(s, t, u, v, __float_as_uint(b.w), __float_as_uint(a.w));
+    if (hit) trav_keep(s, t, u, v, __float_as_uint(b.w), __float_as_uint(a.w), li);
 }
 
 // Tests bottom-level (object-space) triangle li of the current instance in
@@ -353,7 +354,7 @@ __device__ __forceinline__ void trav_leaf_bottom(Trav& s, const GeoView& g, int 
     const float3 B = xform_diag(s.isc, s.itr, xyz(b));
     const float3 C = xform_diag(s.isc, s.itr, xyz(c));
     float t, u, v;
-    if (tri_test(A, B, C, s.o, s.d, t, u, v)) trav_keep(s, t, u, v, s.ioff + __float_as_uint(a.w), s.ithing);
+    if (tri_test(A, B, C, s.o, s.d, t, u, v)) trav_keep(s, t, u, v, s.ioff + __float_as_uint(a.w), s.ithing, -1);
 }
 
 // Enters instance record li of the top level: the stack gets a marker that
@@ -525,14 +526,40 @@ struct ScatterOut {
     bool guide;       // diffuse and metal set the guide layers
 };
 
-// Hit geometry (optx/optics_i.cu:40-82 for triangles, sphere.h:40-46 for
-// spheres) and the Lambertian / fuzzy-metal / dielectric scatter
-// (optx/optics_i.cu:87-96, :168-190, :254-283; near-zero fallback of
-// optics.h:17-18; Schlick's pow 5 as products).  (pa, pb, pc) is the hit
-// primitive's world-space record, h4 = (t, u, v, -).
-__device__ __forceinline__ ScatterOut scatter(float4 pa, float4 pb, float4 pc, const ThingDev* __restrict__ things,
-                                              float3 o, float3 d, float4 h4, Stream& s) {
-    const ThingDev th = things[__float_as_uint(pa.w)];
+// Geometry at a hit (optx/optics_i.cu:40-82 for triangles, sphere.h:40-46
+// for spheres): hit point, unit normal facing the incoming ray, and whether
+// the ray hits the outside (triangles: against the thing's centre,
+// optx/optics_i.cu:259-267).  (pa, pb, pc) is the hit primitive's world-space
+// record.
+struct HitGeo {
+    float3 p, N;
+    bool front;
+};
+
+__device__ __forceinline__ HitGeo hit_geometry(float4 pa, float4 pb, float4 pc, float3 center, float3 o, float3 d,
+                                               float t, float u, float v) {
+    HitGeo g;
+    if (__float_as_uint(pc.w) == kPrimTriangle) {
+        const float3 A = xyz(pa), B = xyz(pb), C = xyz(pc);
+        const float w = 1.f - u - v;
+        g.p = add(add(mul(w, A), mul(u, B)), mul(v, C));
+        float3 N = unitV(cross(sub(B, A), sub(C, A)));
+        if (dot(d, N) > 0.f) N = neg(N);
+        g.N = N;
+        g.front = 0.f > dot(d, sub(g.p, center));
+    } else {
+        g.p = add(o, mul(t, d));
+        const float3 outward = mul(1.f / pb.x, sub(g.p, xyz(pa)));
+        g.front = 0.f > dot(d, outward);
+        g.N = g.front ? outward : neg(outward);
+    }
+    return g;
+}
+
+// The Lambertian / fuzzy-metal / dielectric scatter at a hit of geometry g
+// on a thing of optics th (optx/optics_i.cu:87-96, :168-190, :254-283;
+// near-zero fallback of optics.h:17-18; Schlick's pow 5 as products).
+__device__ __forceinline__ ScatterOut scatter_at(const HitGeo& g, const ThingDev& th, float3 d, Stream& s) {
     ScatterOut r;
     r.type = __float_as_int(th.albedo_type.w);
     r.albedo = xyz(th.albedo_type);
@@ -541,21 +568,9 @@ __device__ __forceinline__ ScatterOut scatter(float4 pa, float4 pb, float4 pc, c
     r.v = mk(0.f, 0.f, 0.f);
     r.cont = true;
     r.guide = r.type != RT_OPTICS_REFRACT;
-    if (__float_as_uint(pc.w) == kPrimTriangle) {
-        const float3 A = xyz(pa), B = xyz(pb), C = xyz(pc);
-        const float u = h4.y, v = h4.z;
-        const float w = 1.f - u - v;
-        r.p = add(add(mul(w, A), mul(u, B)), mul(v, C));
-        float3 N = unitV(cross(sub(B, A), sub(C, A)));
-        if (dot(d, N) > 0.f) N = neg(N);
-        r.N = N;
-        r.front = 0.f > dot(d, sub(r.p, xyz(th.center_fuzz)));   // optx/optics_i.cu:259-267
-    } else {
-        r.p = add(o, mul(h4.x, d));
-        const float3 outward = mul(1.f / pb.x, sub(r.p, xyz(pa)));
-        r.front = 0.f > dot(d, outward);
-        r.N = r.front ? outward : neg(outward);
-    }
+    r.p = g.p;
+    r.N = g.N;
+    r.front = g.front;
     const float3 N = r.N;
     if (r.type == RT_OPTICS_DIFFUSE) {
         const float3 u = rndVon1sphere(s);
@@ -598,6 +613,14 @@ __device__ __forceinline__ ScatterOut scatter(float4 pa, float4 pb, float4 pc, c
         }
     }
     return r;
+}
+
+// Geometry and scatter of a hit on world-space record (pa, pb, pc); h4 = (t, u, v, -).
+__device__ __forceinline__ ScatterOut scatter(float4 pa, float4 pb, float4 pc, const ThingDev* __restrict__ things,
+                                              float3 o, float3 d, float4 h4, Stream& s) {
+    const ThingDev th = things[__float_as_uint(pa.w)];
+    const HitGeo g = hit_geometry(pa, pb, pc, xyz(th.center_fuzz), o, d, h4.x, h4.y, h4.z);
+    return scatter_at(g, th, d, s);
 }
 
 // optx/camera_i.cu:133-139: sky gradient from white to ambient.

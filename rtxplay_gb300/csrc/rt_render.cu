@@ -169,6 +169,9 @@ __global__ void __launch_bounds__(kThreads) k_generate(const JobDev* __restrict_
 // instructions in an issue-bound kernel) and warp-cooperative traversal with
 // parked leaf tests (active lanes 9.6 -> 12.9, 30% more instructions: 803 vs
 // 993 Mrays/s instanced, 64 spp).
+// Writing the hit geometry (point, normal, facing) here instead, so shading
+// needs no gather of the primitive, measured slower on C1 (1146 vs 1216
+// Mrays/s, 64 spp): the shading time did not drop and traversal grew.
 template <bool kCount, bool kInst>
 __global__ void __launch_bounds__(kThreads)
     k_extend(Queues qs, float4* __restrict__ hits, uint32_t* __restrict__ hthing, WaveState* st,
@@ -183,8 +186,11 @@ __global__ void __launch_bounds__(kThreads)
         const float4 o4 = Q.ori[i], d4 = Q.dir[i];
         const int root = jobs[__float_as_uint(d4.w) >> 8].root;
         const HitRec h = closest_hit<kCount, kInst>(g, root, xyz(o4), xyz(d4), nvis, ntest);
-        hits[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.hit ? int(h.id) : -1));
-        hthing[i] = h.thing;
+        // hit reference: top-level record (>= 0), miss (-1), or an instanced
+        // triangle's global id as -2 - id with its thing beside
+        const int ref = !h.hit ? -1 : (h.leaf >= 0 ? h.leaf : -2 - int(h.id));
+        hits[i] = make_float4(h.t, h.u, h.v, __int_as_float(ref));
+        if (kInst && ref <= -2) hthing[i] = h.thing;
         if (h.overflow) atomicOr(&st->err, 1u);
     }
     if (kCount) {
@@ -207,10 +213,12 @@ __device__ __forceinline__ unsigned long long fx_q(float x) {
     return (unsigned long long)__float2ll_rn(x * 4294967296.0f);
 }
 
-__global__ void __launch_bounds__(kThreads)
+// Four resident blocks per SM (64 registers): more warps in flight for the
+// latency-bound gathers.
+__global__ void __launch_bounds__(kThreads, 4)
     k_shade(Queues qs, const float4* __restrict__ hits, const uint32_t* __restrict__ hthing, WaveState* st,
-            const JobDev* __restrict__ jobs, uint32_t nj, const FlatDesc* __restrict__ desc,
-            const ThingDev* __restrict__ things, Acc acc, int any_guides) {
+            const JobDev* __restrict__ jobs, uint32_t nj, const float4* __restrict__ tprims,
+            const FlatDesc* __restrict__ desc, const ThingDev* __restrict__ things, Acc acc, int any_guides) {
     const uint32_t cur = *((volatile uint32_t*)&st->cur);
     const uint32_t n = *((volatile uint32_t*)&st->count[cur]);
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -236,9 +244,9 @@ __global__ void __launch_bounds__(kThreads)
             gN = xyz(Q.gn[i]);
             gA = xyz(Q.ga[i]);
         }
-        const int id = __float_as_int(h4.w);
+        const int ref = __float_as_int(h4.w);
         float3 color = mk(0.f, 0.f, 0.f);
-        if (id < 0) {
+        if (ref == -1) {
             color = mulv(thr, sky(d, j.ambient, j.white));
             ended = true;
         } else if (bounce + 1 >= j.depth) {
@@ -246,7 +254,13 @@ __global__ void __launch_bounds__(kThreads)
         } else {
             Stream s(j.seed, j.key1, pid % j.npix, pid / j.npix, bounce + 1);
             float4 pa, pb, pc;
-            world_prim(desc, hthing[i], uint32_t(id), pa, pb, pc);
+            if (ref >= 0) {   // the world-space record itself
+                pa = __ldg(tprims + 3 * ref);
+                pb = __ldg(tprims + 3 * ref + 1);
+                pc = __ldg(tprims + 3 * ref + 2);
+            } else {          // an instanced triangle, rebuilt exactly as the flat layout stores it
+                world_prim(desc, hthing[i], uint32_t(-2 - ref), pa, pb, pc);
+            }
             const ScatterOut so = scatter(pa, pb, pc, things, o, d, h4, s);
             if (so.guide) {
                 if (isnull(gN)) gN = so.N;
@@ -530,8 +544,8 @@ struct WaveLaunch {
     ExtendFn ext_fn;
     unsigned qgrid;
     Queues qs;
-    float4* hits;
-    uint32_t* hthing;
+    float4* hits;      // t, u, v, hit reference
+    uint32_t* hthing;  // thing of an instanced hit
     WaveState* st;
     const JobDev* jobs;
     uint32_t nj;
@@ -567,8 +581,10 @@ void build_wave_graph(Workspace& ws, const WaveLaunch& L) {
     RT_CUDA(cudaGraphAddKernelNode(&n_ext, body, nullptr, 0, &kp));
     const float4* hits_c = l.hits;
     const uint32_t* hthing_c = l.hthing;
+    const float4* tprims_c = l.geo.tprims;
     const FlatDesc* desc_c = l.geo.desc;
-    void* shade_args[] = {&l.qs, &hits_c, &hthing_c, &l.st, &l.jobs, &l.nj, &desc_c, &l.things, &l.acc, &l.any_guides};
+    void* shade_args[] = {&l.qs,      &hits_c, &hthing_c, &l.st,  &l.jobs,       &l.nj,
+                          &tprims_c, &desc_c, &l.things, &l.acc, &l.any_guides};
     kp.func = reinterpret_cast<void*>(k_shade);
     kp.gridDim = dim3(l.qgrid);
     kp.kernelParams = shade_args;
@@ -635,7 +651,8 @@ void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s
         max_depth = std::max(max_depth, d.depth);
     }
     RT_REQUIRE(total_pix < (uint64_t(1) << 31), "too many pixels in one launch (>= 2^31)");
-    const uint32_t W = uint32_t(std::min<unsigned long long>(env_u32("RTX_WAVE", 1u << 21), total_paths));
+    // wave capacity: measured on C1 (64 spp) 2^22: 1217, 2^21: 1210, 2^20: 1137, 2^19: 1020 Mrays/s
+    const uint32_t W = uint32_t(std::min<unsigned long long>(env_u32("RTX_WAVE", 1u << 22), total_paths));
     // wave bound: the queue holds W rays while paths remain to start and a
     // path is queued at most max_depth times
     const uint64_t max_iter64 = total_paths * max_depth / W + max_depth + 8;
@@ -722,8 +739,8 @@ void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s
                     timed.push_back({ev, 1});
                     ev += 2;
                 }
-                k_shade<<<L.qgrid, kThreads, 0, s>>>(L.qs, L.hits, L.hthing, L.st, L.jobs, nj, L.geo.desc,
-                                                      L.things, L.acc, any_guides);
+                k_shade<<<L.qgrid, kThreads, 0, s>>>(L.qs, L.hits, L.hthing, L.st, L.jobs, nj, L.geo.tprims,
+                                                      L.geo.desc, L.things, L.acc, any_guides);
                 if (stage_timing) RT_CUDA(cudaEventRecord(ws.event(ev - 1), s));
                 k_wave_ctrl<<<1, 1, 0, s>>>(L.st, no_handle, 0);
                 RT_CHECK_LAUNCH();

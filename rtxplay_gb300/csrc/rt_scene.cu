@@ -317,12 +317,23 @@ __global__ void k_morton(const float4* __restrict__ prims, const uint32_t* __res
     ids[i] = i;
 }
 
-// Things-grouped keys.  Every thing gets a 60-bit code of the centre of its
-// primitives' centroid bounds within its segment's bounds; sorting the things
-// by (code, id) ranks them; a primitive's key is (rank << 30) | its 30-bit
-// Morton code within its thing's centroid bounds.  The hierarchy then splits
-// between things first and inside a thing afterwards (the shape of a two-level
-// hierarchy), while every node and primitive stays in world space.
+__device__ __forceinline__ uint32_t seg_of(const SegDev* __restrict__ segs, uint32_t nsegs, uint32_t pos) {
+    uint32_t lo = 0, hi = nsegs;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (segs[mid].prim_begin <= pos) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// Things-grouped hierarchy (a flat, world-space LBVH with the shape of a
+// two-level one).  Primitives are keyed (thing << 30) | (30-bit Morton code of
+// the centroid inside the thing's centroid bounds); a Karras hierarchy per
+// thing (segments = things) gives each thing its subtree; the things of a
+// scene are sorted by a 60-bit code of their centre in the scene's bounds and
+// get a Karras hierarchy of their own, whose internal nodes are stitched into
+// the spare node slot of each thing (a thing of n primitives uses n - 1 of its
+// n slots).  Splits therefore never mix two things below the thing level.
 __global__ void k_thing_codes(const uint32_t* __restrict__ tbounds, const FlatDesc* __restrict__ desc,
                               const uint32_t* __restrict__ sbounds, uint32_t nthings,
                               unsigned long long* __restrict__ codes, uint32_t* __restrict__ ids) {
@@ -342,14 +353,8 @@ __global__ void k_thing_codes(const uint32_t* __restrict__ tbounds, const FlatDe
     ids[t] = t;
 }
 
-__global__ void k_thing_rank(const uint32_t* __restrict__ sorted_ids, uint32_t nthings, uint32_t* __restrict__ rank) {
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < nthings) rank[sorted_ids[k]] = k;
-}
-
 __global__ void k_morton_grouped(const float4* __restrict__ prims, uint32_t n, const uint32_t* __restrict__ tbounds,
-                                 const uint32_t* __restrict__ rank, unsigned long long* __restrict__ codes,
-                                 uint32_t* __restrict__ ids) {
+                                 unsigned long long* __restrict__ codes, uint32_t* __restrict__ ids) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t t = __float_as_uint(prims[3 * size_t(i)].w);
@@ -361,8 +366,50 @@ __global__ void k_morton_grouped(const float4* __restrict__ prims, uint32_t n, c
     const uint32_t qx = uint32_t(quantf(c.x, lo.x, ext.x, 1024.f));
     const uint32_t qy = uint32_t(quantf(c.y, lo.y, ext.y, 1024.f));
     const uint32_t qz = uint32_t(quantf(c.z, lo.z, ext.z, 1024.f));
-    codes[i] = ((unsigned long long)rank[t] << 30) | ((expand10(qx) << 2) | (expand10(qy) << 1) | expand10(qz));
+    codes[i] = ((unsigned long long)t << 30) | ((expand10(qx) << 2) | (expand10(qy) << 1) | expand10(qz));
     ids[i] = i;
+}
+
+// Spare node slot of thing t (its last slot; a thing of n records has n - 1 internal nodes).
+__device__ __forceinline__ int spare_slot(const SegDev* __restrict__ tsegs, uint32_t t) {
+    return int(tsegs[t].prim_begin + tsegs[t].prim_count) - 1;
+}
+
+// One thread per top-level (thing-tree) slot j: the thing tree's internal node
+// j of a scene with at least two things moves to the spare slot of thing j;
+// its children are remapped (internal -> their spare slots, thing leaf -> the
+// thing's subtree root, or its single record) and their parents set.
+__global__ void k_stitch(const float4* __restrict__ tnodes, const SegDev* __restrict__ scene_things, uint32_t nsegs,
+                         const uint32_t* __restrict__ sorted_things, const SegDev* __restrict__ tsegs, uint32_t nthings,
+                         float4* __restrict__ nodes, int* __restrict__ parent_leaf, int* __restrict__ parent_int) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nthings) return;
+    const SegDev sc = scene_things[seg_of(scene_things, nsegs, j)];
+    if (sc.prim_count < 2 || j - sc.prim_begin >= sc.prim_count - 1) return;
+    const int D = spare_slot(tsegs, j);
+    const float4 n3 = tnodes[4 * size_t(j) + 3];
+    int ref[2];
+    const int child[2] = {__float_as_int(n3.x), __float_as_int(n3.y)};
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const int c = child[k];
+        if (c >= 0) {
+            ref[k] = spare_slot(tsegs, uint32_t(c));
+            parent_int[ref[k]] = D;
+        } else {
+            const uint32_t t = sorted_things[~c];
+            const SegDev ts = tsegs[t];
+            if (ts.prim_count >= 2) {
+                ref[k] = int(ts.prim_begin);
+                parent_int[ts.prim_begin] = D;
+            } else {
+                ref[k] = ~int(ts.prim_begin);
+                parent_leaf[ts.prim_begin] = D;
+            }
+        }
+    }
+    nodes[4 * size_t(D) + 3] = make_float4(__int_as_float(ref[0]), __int_as_float(ref[1]), 0.f, 0.f);
+    if (j == sc.prim_begin) parent_int[D] = -1;   // the scene's root
 }
 
 // Segment ids of the code-sorted primitives, and the identity permutation.
@@ -393,15 +440,6 @@ __device__ __forceinline__ int kdelta(const K* __restrict__ k, int n, int i, int
     const unsigned long long a = (unsigned long long)k[i], b = (unsigned long long)k[j];
     if (a != b) return __clzll((long long)(a ^ b));
     return 64 + __clz(i ^ j);
-}
-
-__device__ __forceinline__ uint32_t seg_of(const SegDev* __restrict__ segs, uint32_t nsegs, uint32_t pos) {
-    uint32_t lo = 0, hi = nsegs;
-    while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (segs[mid].prim_begin <= pos) lo = mid; else hi = mid;
-    }
-    return lo;
 }
 
 // One thread per node slot.  Slot P + i (i < n - 1) of a segment starting at
@@ -725,11 +763,10 @@ void build_topology(Lbvh& L, cudaStream_t s) {
     int key_bits = L.morton_bits;
     if (L.grouped) {
         k_morton_grouped<<<grid_for(n), kThreads, 0, s>>>(L.prims_flat.as<float4>(), n, L.tbounds.as<uint32_t>(),
-                                                           L.trank.as<uint32_t>(),
                                                            reinterpret_cast<unsigned long long*>(codes), ids);
-        int rank_bits = 1;
-        while ((uint64_t(1) << rank_bits) < L.nthings) ++rank_bits;
-        key_bits = 30 + rank_bits;
+        int thing_bits = 1;
+        while ((uint64_t(1) << thing_bits) < L.nthings) ++thing_bits;
+        key_bits = 30 + thing_bits;
     } else {
         k_morton<K><<<grid_for(n), kThreads, 0, s>>>(L.prims_flat.as<float4>(), pseg, n, L.bounds.as<uint32_t>(),
                                                       codes, ids);
@@ -739,7 +776,7 @@ void build_topology(Lbvh& L, cudaStream_t s) {
         radix_sort_pairs_u32(reinterpret_cast<uint32_t*>(codes), ids, n, key_bits, L.sort_tmp, s);
     else
         radix_sort_pairs_u64(reinterpret_cast<unsigned long long*>(codes), ids, n, key_bits, L.sort_tmp, s);
-    if (L.nsegs > 1) {
+    if (L.nsegs > 1 && !L.grouped) {   // grouped keys are thing-major, hence segment-major already
         // stable second pass by segment: (segment, code) order
         int seg_bits = 1;
         while ((1u << seg_bits) < L.nsegs) ++seg_bits;
@@ -758,18 +795,51 @@ void build_topology(Lbvh& L, cudaStream_t s) {
         RT_CUDA(cudaMemcpyAsync(ids, ids2, size_t(n) * 4, cudaMemcpyDeviceToDevice, s));
     }
     int* parents = L.parents.as<int>();
-    k_karras<K><<<grid_for(n), kThreads, 0, s>>>(codes, L.segs.as<SegDev>(), L.nsegs, n, L.nodes.as<float4>(), parents,
-                                                  parents + n);
+    if (L.grouped) {   // one hierarchy per thing now, the thing trees are stitched on top afterwards
+        k_karras<K><<<grid_for(n), kThreads, 0, s>>>(codes, L.tsegs.as<SegDev>(), L.nthings, n, L.nodes.as<float4>(),
+                                                      parents, parents + n);
+    } else {
+        k_karras<K><<<grid_for(n), kThreads, 0, s>>>(codes, L.segs.as<SegDev>(), L.nsegs, n, L.nodes.as<float4>(),
+                                                      parents, parents + n);
+    }
     RT_CHECK_LAUNCH();
 }
 
 // Morton codes (or things-grouped keys, for top-level records whose a.w is
 // the thing), sort, hierarchy and refit of an LBVH whose records are in
 // prims_flat.
-void build_lbvh(Lbvh& L, int morton_bits, cudaStream_t s, const FlatDesc* desc = nullptr, uint32_t nthings = 0) {
+void build_lbvh(Lbvh& L, int morton_bits, cudaStream_t s, const FlatDesc* desc = nullptr,
+                const std::vector<FlatDesc>* desc_host = nullptr, const std::vector<uint32_t>* thing_begin = nullptr) {
     L.morton_bits = morton_bits;
-    L.grouped = desc != nullptr && nthings > 0;
+    const uint32_t nthings = desc_host ? uint32_t(desc_host->size()) : 0u;
+    L.grouped = desc != nullptr && nthings > 0 && L.nprims > 0;
     L.nthings = nthings;
+    L.roots.clear();
+    if (L.grouped) {
+        // host tables: per-thing record range and scene, per-scene thing range and root
+        std::vector<SegDev> tsegs(nthings), scene_things(L.nsegs);
+        std::vector<uint32_t> tseg(nthings);
+        for (uint32_t t = 0; t < nthings; ++t) {
+            tsegs[t] = SegDev{(*desc_host)[t].top_offset, (*desc_host)[t].ntop};
+            tseg[t] = (*desc_host)[t].seg;
+        }
+        L.roots.assign(L.nsegs, -1);
+        for (uint32_t sg = 0; sg < L.nsegs; ++sg) {
+            const uint32_t tb = (*thing_begin)[sg];
+            const uint32_t te = sg + 1 < L.nsegs ? (*thing_begin)[sg + 1] : nthings;
+            scene_things[sg] = SegDev{tb, te - tb};
+            if (te - tb >= 2) L.roots[sg] = int(tsegs[tb].prim_begin + tsegs[tb].prim_count) - 1;
+            else if (te - tb == 1) L.roots[sg] = int(tsegs[tb].prim_begin);
+        }
+        L.tsegs.reserve(size_t(nthings) * sizeof(SegDev));
+        L.scene_things.reserve(std::max<size_t>(1, L.nsegs) * sizeof(SegDev));
+        L.tseg.reserve(size_t(nthings) * 4);
+        RT_CUDA(cudaMemcpyAsync(L.tsegs.p, tsegs.data(), tsegs.size() * sizeof(SegDev), cudaMemcpyHostToDevice, s));
+        RT_CUDA(cudaMemcpyAsync(L.scene_things.p, scene_things.data(), scene_things.size() * sizeof(SegDev),
+                                cudaMemcpyHostToDevice, s));
+        RT_CUDA(cudaMemcpyAsync(L.tseg.p, tseg.data(), tseg.size() * 4, cudaMemcpyHostToDevice, s));
+        RT_CUDA(cudaStreamSynchronize(s));   // the host tables must outlive the copies
+    }
     const uint32_t n = L.nprims;
     L.prims.reserve(std::max<size_t>(1, n) * 48);
     L.nodes.reserve(std::max<size_t>(1, n) * 64);
@@ -784,23 +854,51 @@ void build_lbvh(Lbvh& L, int morton_bits, cudaStream_t s, const FlatDesc* desc =
                                                         L.bounds.as<uint32_t>(), 0);
     RT_CHECK_LAUNCH();
     if (L.grouped) {
-        L.tbounds.reserve(size_t(nthings) * 6 * sizeof(uint32_t));
-        L.tcodes.reserve(size_t(nthings) * 8);
-        L.tids.reserve(size_t(nthings) * 4);
-        L.trank.reserve(size_t(nthings) * 4);
-        k_init_bounds<<<grid_for(6 * nthings), kThreads, 0, s>>>(L.tbounds.as<uint32_t>(), nthings);
+        const uint32_t T = nthings;
+        L.tbounds.reserve(size_t(T) * 6 * sizeof(uint32_t));
+        L.tcodes.reserve(size_t(T) * 8 * 2);
+        L.tids.reserve(size_t(T) * 4 * 2);
+        L.ttmp.reserve(size_t(T) * 64 + size_t(T) * 8 + 64);
+        k_init_bounds<<<grid_for(6 * T), kThreads, 0, s>>>(L.tbounds.as<uint32_t>(), T);
         RT_CHECK_LAUNCH();
         k_centroid_bounds<<<grid_for(n), kThreads, 0, s>>>(L.prims_flat.as<float4>(), nullptr, n,
                                                             L.tbounds.as<uint32_t>(), 1);
         RT_CHECK_LAUNCH();
-        k_thing_codes<<<grid_for(nthings), kThreads, 0, s>>>(L.tbounds.as<uint32_t>(), desc, L.bounds.as<uint32_t>(),
-                                                              nthings, L.tcodes.as<unsigned long long>(),
-                                                              L.tids.as<uint32_t>());
-        RT_CHECK_LAUNCH();
-        radix_sort_pairs_u64(L.tcodes.as<unsigned long long>(), L.tids.as<uint32_t>(), nthings, 60, L.sort_tmp, s);
-        k_thing_rank<<<grid_for(nthings), kThreads, 0, s>>>(L.tids.as<uint32_t>(), nthings, L.trank.as<uint32_t>());
-        RT_CHECK_LAUNCH();
+        // thing subtrees (segments = things)
         build_topology<unsigned long long>(L, s);
+        // the things of each scene in 60-bit code order, scene-major
+        unsigned long long* tc = L.tcodes.as<unsigned long long>();
+        uint32_t* tid = L.tids.as<uint32_t>();
+        k_thing_codes<<<grid_for(T), kThreads, 0, s>>>(L.tbounds.as<uint32_t>(), desc, L.bounds.as<uint32_t>(), T, tc,
+                                                        tid);
+        RT_CHECK_LAUNCH();
+        radix_sort_pairs_u64(tc, tid, T, 60, L.sort_tmp, s);
+        if (L.nsegs > 1) {
+            int seg_bits = 1;
+            while ((1u << seg_bits) < L.nsegs) ++seg_bits;
+            L.seg_tmp.reserve(size_t(T) * 8);
+            uint32_t* keys = L.seg_tmp.as<uint32_t>();
+            uint32_t* perm = keys + T;
+            unsigned long long* tc2 = tc + T;
+            uint32_t* tid2 = tid + T;
+            k_seg_keys<<<grid_for(T), kThreads, 0, s>>>(L.tseg.as<uint32_t>(), tid, T, keys, perm);
+            RT_CHECK_LAUNCH();
+            radix_sort_pairs_u32(keys, perm, T, seg_bits, L.sort_tmp, s);
+            k_permute<unsigned long long><<<grid_for(T), kThreads, 0, s>>>(tc, tid, perm, T, tc2, tid2);
+            RT_CHECK_LAUNCH();
+            RT_CUDA(cudaMemcpyAsync(tc, tc2, size_t(T) * 8, cudaMemcpyDeviceToDevice, s));
+            RT_CUDA(cudaMemcpyAsync(tid, tid2, size_t(T) * 4, cudaMemcpyDeviceToDevice, s));
+        }
+        // the thing tree of each scene, into scratch, then stitched into the spare slots
+        float4* tnodes = L.ttmp.as<float4>();
+        int* tpar = reinterpret_cast<int*>(tnodes + 4 * size_t(T));
+        k_karras<unsigned long long><<<grid_for(T), kThreads, 0, s>>>(tc, L.scene_things.as<SegDev>(), L.nsegs, T,
+                                                                       tnodes, tpar, tpar + T);
+        RT_CHECK_LAUNCH();
+        int* parents = L.parents.as<int>();
+        k_stitch<<<grid_for(T), kThreads, 0, s>>>(tnodes, L.scene_things.as<SegDev>(), L.nsegs, tid,
+                                                  L.tsegs.as<SegDev>(), T, L.nodes.as<float4>(), parents, parents + n);
+        RT_CHECK_LAUNCH();
     } else if (morton_bits == 30) {
         build_topology<uint32_t>(L, s);
     } else {
@@ -832,8 +930,9 @@ void build_geometry(Geometry& g, const std::vector<Scene*>& scenes, int morton_b
     flatten_bottom(g, P, s);
     build_lbvh(g.blas, g.morton_bits, s);   // object space, before the instance boxes are taken
     flatten_top(g, s);
-    const bool grouped = layout == RT_LAYOUT_AUTO || layout == RT_LAYOUT_GROUPED;
-    build_lbvh(g.top, g.morton_bits, s, grouped ? g.desc.as<FlatDesc>() : nullptr, grouped ? g.nthings : 0);
+    const bool grouped = (layout == RT_LAYOUT_AUTO || layout == RT_LAYOUT_GROUPED) && P.ninstances == 0;
+    build_lbvh(g.top, g.morton_bits, s, grouped ? g.desc.as<FlatDesc>() : nullptr, grouped ? &g.desc_host : nullptr,
+               &g.thing_begin);
     RT_CUDA(cudaEventRecord(e1, s));
     RT_CUDA(cudaEventSynchronize(e1));
     RT_CUDA(cudaEventElapsedTime(&g.build_ms, e0, e1));

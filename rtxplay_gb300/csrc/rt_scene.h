@@ -44,13 +44,19 @@ struct Lbvh {
     DevBuf flags;           // refit arrival counters [n]
     DevBuf bounds;          // centroid bounds per segment, 6 orderable u32 each
     DevBuf sort_tmp, seg_tmp;
-    DevBuf tbounds, tcodes, tids, trank;   // things-grouped keys: per-thing bounds, codes, order, rank
+    // things-grouped hierarchy: per-thing centroid bounds, thing codes and order,
+    // per-thing record ranges, per-scene thing ranges, thing -> scene, scratch
+    DevBuf tbounds, tcodes, tids, tsegs, scene_things, tseg, ttmp;
     uint32_t nprims = 0, nsegs = 0, nthings = 0;
     int morton_bits = 60;
     int grouped = 0;
     std::vector<SegDev> seg_host;
+    std::vector<int> roots;   // per segment, grouped hierarchies only
     size_t device_bytes() const;
-    int root(uint32_t seg) const { return seg_host[seg].prim_count ? int(seg_host[seg].prim_begin) : -1; }
+    int root(uint32_t seg) const {
+        if (grouped) return roots[seg];
+        return seg_host[seg].prim_count ? int(seg_host[seg].prim_begin) : -1;
+    }
 };
 
 struct Scene;

@@ -83,8 +83,11 @@ def test_lbvh_topology_is_a_binary_tree(product, cuda, layout):
     n = len(t["ids"])
     seen_leaf = np.zeros(n, bool)
     seen_int = np.zeros(n - 1, bool)
-    seen_int[0] = True
-    for c in np.concatenate([t["left"], t["right"]]):
+    kids = np.concatenate([t["left"], t["right"]])
+    roots = np.setdiff1d(np.arange(n - 1), kids[kids >= 0])
+    assert len(roots) == 1   # the root: the one internal node no node points at
+    seen_int[roots[0]] = True
+    for c in kids:
         if c < 0:
             assert not seen_leaf[~c]
             seen_leaf[~c] = True
