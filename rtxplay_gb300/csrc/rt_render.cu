@@ -219,11 +219,15 @@ __global__ void __launch_bounds__(kThreads, 4)
     k_shade(Queues qs, const float4* __restrict__ hits, const uint32_t* __restrict__ hthing, WaveState* st,
             const JobDev* __restrict__ jobs, uint32_t nj, const float4* __restrict__ tprims,
             const FlatDesc* __restrict__ desc, const ThingDev* __restrict__ things, Acc acc, int any_guides) {
+    // per-warp counts, turned into block-exclusive offsets by thread 0, and the
+    // block's bases from one global atomic per block (not one per warp)
+    __shared__ uint32_t s_warp[kThreads / 32];
+    __shared__ unsigned long long s_base;
     const uint32_t cur = *((volatile uint32_t*)&st->cur);
     const uint32_t n = *((volatile uint32_t*)&st->count[cur]);
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t lane = lane_id();
-    if (i - lane >= n) return;   // whole warp past the queue end
+    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+    if (blockIdx.x * blockDim.x >= n) return;   // whole block past the queue end
     const bool active = i < n;
     const Queue Q = pick(qs, cur), N = pick(qs, cur ^ 1);
 
@@ -293,14 +297,22 @@ __global__ void __launch_bounds__(kThreads, 4)
 
     // regenerate: every ended path is replaced by the next camera path
     const uint32_t want = __ballot_sync(0xFFFFFFFFu, ended);
+    if (lane == 0) s_warp[warp] = __popc(want);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t tot = 0;
+        for (uint32_t w = 0; w < kThreads / 32; ++w) {
+            const uint32_t c = s_warp[w];
+            s_warp[w] = tot;
+            tot += c;
+        }
+        s_base = tot ? atomicAdd(&st->next_path, (unsigned long long)tot) : 0ull;
+    }
+    __syncthreads();
     bool fresh = false;
     if (want) {
-        unsigned long long base = 0;
-        const int leader = __ffs(want) - 1;
-        if (int(lane) == leader) base = atomicAdd(&st->next_path, (unsigned long long)__popc(want));
-        base = __shfl_sync(0xFFFFFFFFu, base, leader);
         if (ended) {
-            const unsigned long long g = base + __popc(want & ((1u << lane) - 1u));
+            const unsigned long long g = s_base + s_warp[warp] + __popc(want & ((1u << lane) - 1u));
             if (g < st->total_paths) {
                 jx = job_of_path(jobs, nj, g);
                 const JobDev& j = jobs[jx];
@@ -317,11 +329,21 @@ __global__ void __launch_bounds__(kThreads, 4)
     if (cont) bounce += 1;
     const bool push = cont || fresh;
     const uint32_t pm = __ballot_sync(0xFFFFFFFFu, push);
+    __syncthreads();   // every warp has read its regeneration offset
+    if (lane == 0) s_warp[warp] = __popc(pm);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t tot = 0;
+        for (uint32_t w = 0; w < kThreads / 32; ++w) {
+            const uint32_t c = s_warp[w];
+            s_warp[w] = tot;
+            tot += c;
+        }
+        s_base = tot ? (unsigned long long)atomicAdd(&st->count[cur ^ 1], tot) : 0ull;
+    }
+    __syncthreads();
     if (pm) {
-        uint32_t base = 0;
-        const int leader = __ffs(pm) - 1;
-        if (int(lane) == leader) base = atomicAdd(&st->count[cur ^ 1], uint32_t(__popc(pm)));
-        base = __shfl_sync(0xFFFFFFFFu, base, leader);
+        const uint32_t base = uint32_t(s_base) + s_warp[warp];
         if (push) {
             const uint32_t slot = base + __popc(pm & ((1u << lane) - 1u));
             N.ori[slot] = make_float4(no.x, no.y, no.z, __uint_as_float(pid));
