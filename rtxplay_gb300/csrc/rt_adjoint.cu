@@ -24,10 +24,11 @@
 //                    move on the fixed surface, sphere normals turn with the
 //                    hit point, reflection / refraction directions are
 //                    differentiated, diffuse directions follow the normal.
-// All gradient arithmetic is in double precision, in the same operation order
-// as the FP64 CPU restatement of the method (oracle/rt_oracle.cpp,
-// orc_adjoint), so every path's terms agree bit for bit and the totals only
-// differ by summation order.
+// The albedo and sky terms are computed in double precision in the same
+// operation order as the FP64 CPU restatement of the method
+// (oracle/rt_oracle.cpp, orc_adjoint), so every path's terms agree bit for
+// bit and the totals only differ by summation order; the fuzz tangent runs in
+// binary32 (agreeing with the FP64 restatement to single precision).
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -50,6 +51,7 @@ struct AdjJob {
     int root;
     uint32_t thing_begin, nthings;
     unsigned long long path_offset;
+    uint32_t pix_offset;     // first pixel of the job in the per-pixel gradient array
     const rt_float3* image;
     const rt_float3* grad_image;
 };
@@ -85,63 +87,67 @@ struct AdjVtx {
 };
 
 // Forward tangent (dO, dD) of the ray entering vertex m, carried through
-// vertices m..ne-1 to the miss direction d_last; returns d(sky)/d(.) per
-// channel.
-__device__ D3 tangent_to_sky(const AdjVtx* V, uint32_t m, uint32_t ne, const FlatDesc* __restrict__ desc, D3 dO,
-                             D3 dD, float3 d_last, float3 ambient, float3 white) {
+// vertices m..ne-1 to the miss direction d_last; returns d(unit(d_last).y)/d(.)
+// (the sky's derivative is 0.5 times this times (ambient - white) per
+// channel).  Mostly binary32 (GB300's FP64 rate made an all-double version 45 %
+// of the adjoint's time); the two places where grazing geometry cancels
+// digits stay in double: the projection onto the surface plane (n.q / n.d,
+// with n = p - c exact for spheres) and the refraction branch (1 - |perp|^2
+// near total internal reflection).
+__device__ float tangent_to_sky(const AdjVtx* V, uint32_t m, uint32_t ne, const FlatDesc* __restrict__ desc, float3 dO,
+                                float3 dD, float3 d_last) {
     for (uint32_t k = m; k < ne; ++k) {
         const AdjVtx& v = V[k];
         const FlatDesc& fd = desc[v.thing];
         const bool sphere = fd.analytic != 0;
-        const float4 pa = sphere ? fd.sphere : make_float4(0.f, 0.f, 0.f, 0.f);
-        const float4 pb = make_float4(fd.sphere.w, 0.f, 0.f, 0.f);
         const int type = int(v.bits & 3u);
         const int branch = int((v.bits >> 2) & 1u);
         const bool front = ((v.bits >> 3) & 1u) != 0;
-        const D3 d = dd3(v.d), N = dd3(v.N);
-        const double t = v.t;
+        const float3 d = v.d, N = v.N;
         // hit point on the fixed surface: dp = q - d (n.q)/(n.d), q = dO + t dD
-        const D3 q = dO + t * dD;
-        const D3 n = sphere ? dd3(v.p) - dd3(xyz(pa)) : N;
-        const double nd = ddot(n, d);
-        const D3 dp = nd != 0.0 ? q - (ddot(n, q) / nd) * d : q;
-        D3 dN{0, 0, 0};
-        if (sphere) {   // N = +-(p - c) / r
-            const double sgn = front ? 1.0 : -1.0;
-            dN = (sgn / double(pb.x)) * dp;
-        }
-        D3 dOut;
+        const float3 q = add(dO, mul(v.t, dD));
+        const D3 n = sphere ? dd3(v.p) - dd3(xyz(fd.sphere)) : dd3(N);
+        const double nd = ddot(n, dd3(d));   // both dot products exact to double rounding,
+        const double nq = ddot(n, dd3(q));   // their quotient then needs single precision only
+        const float3 dp = nd != 0.0 ? sub(q, mul(float(nq) / float(nd), d)) : q;
+        float3 dN = mk(0.f, 0.f, 0.f);
+        if (sphere) dN = mul((front ? 1.f : -1.f) / fd.sphere.w, dp);   // N = +-(p - c) / r
+        float3 dOut;
         if (type == RT_OPTICS_DIFFUSE) {
             dOut = dN;   // d' = N + u, or N
         } else {
-            const D3 d1 = (1.0 / dlen(d)) * d;
-            const D3 dd1 = dunit(d, dD);
+            const float il = 1.f / sqrtf(dot(d, d));
+            const float3 d1 = mul(il, d);
+            const float3 dd1 = mul(il, sub(dD, mul(dot(d1, dD), d1)));
             const bool refl = type == RT_OPTICS_REFLECT || branch == 0;
             if (refl) {
-                const double c = ddot(d1, N);
-                const double dc = ddot(dd1, N) + ddot(d1, dN);
-                dOut = dd1 - 2.0 * ((dc * N) + c * dN);
+                const float c = dot(d1, N);
+                const float dc = dot(dd1, N) + dot(d1, dN);
+                dOut = sub(dd1, mul(2.f, add(mul(dc, N), mul(c, dN))));
             } else {
+                const D3 dd = dd3(d), DN = dd3(N), dDd = dd3(dD), dNd = dd3(dN);
+                const D3 e1 = (1.0 / dlen(dd)) * dd;
+                const D3 de1 = dunit(dd, dDd);
                 const double ratio = v.ratio;
-                const double raw = -ddot(d1, N);
+                const double raw = -ddot(e1, DN);
                 const double cth = raw < 1.0 ? raw : 1.0;
-                const double dcth = raw < 1.0 ? -(ddot(dd1, N) + ddot(d1, dN)) : 0.0;
-                const D3 perp = ratio * (d1 + cth * N);
-                const D3 dperp = ratio * (dd1 + (dcth * N) + cth * dN);
+                const double dcth = raw < 1.0 ? -(ddot(de1, DN) + ddot(e1, dNd)) : 0.0;
+                const D3 perp = ratio * (e1 + cth * DN);
+                const D3 dperp = ratio * (de1 + (dcth * DN) + cth * dNd);
                 const double qq = ddot(perp, perp);
                 const double sroot = sqrt(fabs(1.0 - qq));
                 const double dq = 2.0 * ddot(perp, dperp);
                 const double ds = sroot > 0.0 ? ((1.0 - qq) >= 0.0 ? -dq : dq) / (2.0 * sroot) : 0.0;
-                dOut = dperp - ((ds * N) + sroot * dN);
+                const D3 o = dperp - ((ds * DN) + sroot * dNd);
+                dOut = mk(float(o.x), float(o.y), float(o.z));
             }
         }
         dO = dp;
         dD = dOut;
     }
-    const D3 du = dunit(dd3(d_last), dD);
-    const double ds = 0.5 * du.y;
-    return D3{ds * (double(ambient.x) - white.x), ds * (double(ambient.y) - white.y),
-              ds * (double(ambient.z) - white.z)};
+    const float il = 1.f / sqrtf(dot(d_last, d_last));
+    const float3 u = mul(il, d_last);
+    return il * (dD.y - dot(u, dD) * u.y);
 }
 
 __device__ __forceinline__ uint32_t adj_job_of(const AdjJob* __restrict__ jobs, uint32_t nj, unsigned long long g) {
@@ -171,20 +177,18 @@ struct Sink {
 // Replays global path `path` and adds its gradient terms.  Returns 1 when the
 // traversal stack overflowed.
 __device__ uint32_t adjoint_path(const AdjJob* __restrict__ jobs, uint32_t nj, unsigned long long path, const GeoView& geo,
-                                 const ThingDev* __restrict__ things, const Sink& sink, double gsky[6]) {
+                                 const ThingDev* __restrict__ things, const double* __restrict__ gpix, const Sink& sink,
+                                 double gsky[6]) {
     const uint32_t jx = adj_job_of(jobs, nj, path);
     const AdjJob& j = jobs[jx];
     const uint32_t pid = uint32_t(path - j.path_offset);
     const uint32_t pix = pid % j.npix, smp = pid / j.npix;
     double g[3];
     {
-        const rt_float3 I = j.image[pix], GI = j.grad_image[pix];
-        const float Ic[3] = {I.x, I.y, I.z}, Gc[3] = {GI.x, GI.y, GI.z};
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            const double mask = (Ic[c] > 0.f && Ic[c] < 1.f) ? 1.0 : 0.0;   // clamp to [0, 1]
-            g[c] = double(Gc[c]) * mask / double(j.spp);
-        }
+        const double* gp = gpix + 3 * (size_t(j.pix_offset) + pix);
+        g[0] = gp[0];
+        g[1] = gp[1];
+        g[2] = gp[2];
     }
     if (g[0] == 0.0 && g[1] == 0.0 && g[2] == 0.0) return 0;
 
@@ -250,20 +254,45 @@ __device__ uint32_t adjoint_path(const AdjJob* __restrict__ jobs, uint32_t nj, u
         sink.add(jx, j, v.thing, 1, g[1] * o3.y * skyc[1]);
         sink.add(jx, j, v.thing, 2, g[2] * o3.z * skyc[2]);
         if (type == RT_OPTICS_REFLECT) {
-            const D3 ds = tangent_to_sky(V, k + 1, ne, geo.desc, D3{0, 0, 0}, dd3(v.v), d, j.ambient, j.white);
-            sink.add(jx, j, v.thing, 3, g[0] * th3[0] * ds.x + g[1] * th3[1] * ds.y + g[2] * th3[2] * ds.z);
+            const double duy = tangent_to_sky(V, k + 1, ne, geo.desc, mk(0.f, 0.f, 0.f), v.v, d);
+            const double ds = 0.5 * duy;
+            const D3 dsc{ds * (double(j.ambient.x) - j.white.x), ds * (double(j.ambient.y) - j.white.y),
+                         ds * (double(j.ambient.z) - j.white.z)};
+            sink.add(jx, j, v.thing, 3, g[0] * th3[0] * dsc.x + g[1] * th3[1] * dsc.y + g[2] * th3[2] * dsc.z);
         }
         suf = dmul(suf, dd3(xyz(things[v.thing].albedo_type)));
     }
     return 0;
 }
 
+// Per pixel and channel, the loss gradient each of the pixel's paths carries:
+// g = dL/dI' * [0 < I < 1] / spp (once per pixel instead of once per path).
+__global__ void k_adjoint_pixel_g(const AdjJob* __restrict__ jobs, uint32_t nj, uint32_t total_pix,
+                                  double* __restrict__ gpix) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= total_pix) return;
+    uint32_t lo = 0, hi = nj;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (jobs[mid].pix_offset <= p) lo = mid; else hi = mid;
+    }
+    const AdjJob& j = jobs[lo];
+    const uint32_t pix = p - j.pix_offset;
+    const rt_float3 I = j.image[pix], GI = j.grad_image[pix];
+    const float Ic[3] = {I.x, I.y, I.z}, Gc[3] = {GI.x, GI.y, GI.z};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const double mask = (Ic[c] > 0.f && Ic[c] < 1.f) ? 1.0 : 0.0;   // clamp to [0, 1]
+        gpix[3 * size_t(p) + c] = double(Gc[c]) * mask / double(j.spp);
+    }
+}
+
 // One block: kAdjPathsPerBlock consecutive global paths, thread-strided.
 // Four resident blocks per SM cap the registers at 128 per thread.
 __global__ void __launch_bounds__(kAdjThreads, 4)
     k_adjoint(const AdjJob* __restrict__ jobs, uint32_t nj, unsigned long long total, GeoView geo,
-              const ThingDev* __restrict__ things, double* G, uint32_t nthings_total, uint32_t sh_things,
-              uint32_t* err) {
+              const ThingDev* __restrict__ things, const double* __restrict__ gpix, double* G, uint32_t nthings_total,
+              uint32_t sh_things, uint32_t* err) {
     extern __shared__ double sh[];   // [4 * sh_things] + [6]
     const unsigned long long base = (unsigned long long)blockIdx.x * kAdjPathsPerBlock;
     const uint32_t j0 = adj_job_of(jobs, nj, base);
@@ -279,10 +308,10 @@ __global__ void __launch_bounds__(kAdjThreads, 4)
         if (path >= total) break;
         const uint32_t jx = adj_job_of(jobs, nj, path);
         if (jx == j0) {
-            my_err |= adjoint_path(jobs, nj, path, geo, things, sink, gsky);
+            my_err |= adjoint_path(jobs, nj, path, geo, things, gpix, sink, gsky);
         } else {   // a block that straddles two jobs: sky terms of the later job go straight to G
             double gs[6] = {0, 0, 0, 0, 0, 0};
-            my_err |= adjoint_path(jobs, nj, path, geo, things, sink, gs);
+            my_err |= adjoint_path(jobs, nj, path, geo, things, gpix, sink, gs);
             for (int k = 0; k < 6; ++k)
                 if (gs[k] != 0.0) atomicAdd(G + 4 * size_t(nthings_total) + 6 * size_t(jx) + k, gs[k]);
         }
@@ -334,7 +363,7 @@ __global__ void k_adjoint_out(const double* __restrict__ G, uint32_t nthings_tot
 }
 
 struct AdjWorkspace {
-    DevBuf jobs, outs, G, err;
+    DevBuf jobs, outs, G, err, gpix;
     std::vector<AdjJob> jobs_host;
     std::vector<AdjOut> outs_host;
 };
@@ -354,6 +383,7 @@ void adjoint_jobs(const Geometry& g, const std::vector<AdjointJob>& jobs, cudaSt
     ws.jobs_host.resize(nj);
     ws.outs_host.resize(nj);
     unsigned long long total = 0;
+    uint64_t total_pix = 0;
     uint32_t max_things = 0;
     for (uint32_t k = 0; k < nj; ++k) {
         const AdjointJob& a = jobs[k];
@@ -377,13 +407,17 @@ void adjoint_jobs(const Geometry& g, const std::vector<AdjointJob>& jobs, cudaSt
         d.thing_begin = g.thing_begin[a.seg];
         d.nthings = (a.seg + 1 < g.nsegs ? g.thing_begin[a.seg + 1] : g.nthings) - d.thing_begin;
         d.path_offset = total;
+        d.pix_offset = uint32_t(total_pix);
         d.image = a.image;
         d.grad_image = a.grad_image;
         total += (unsigned long long)d.npix * d.spp;
+        total_pix += d.npix;
         max_things = std::max(max_things, d.nthings);
         ws.outs_host[k] = AdjOut{a.grad_albedo, a.grad_fuzz, a.grad_sky, d.thing_begin, d.nthings};
     }
+    RT_REQUIRE(total_pix < (uint64_t(1) << 31), "too many pixels in one launch (>= 2^31)");
     const size_t gsize = (4 * size_t(g.nthings) + 6 * size_t(nj)) * sizeof(double);
+    ws.gpix.reserve(std::max<size_t>(1, total_pix) * 3 * sizeof(double));
     ws.jobs.reserve(nj * sizeof(AdjJob));
     ws.outs.reserve(nj * sizeof(AdjOut));
     ws.G.reserve(gsize);
@@ -395,10 +429,13 @@ void adjoint_jobs(const Geometry& g, const std::vector<AdjointJob>& jobs, cudaSt
     const uint32_t sh_things = std::min(max_things, kAdjShThings);
     const size_t shmem = (4 * size_t(sh_things) + 6) * sizeof(double);
     if (total) {
+        k_adjoint_pixel_g<<<unsigned((total_pix + 255) / 256), 256, 0, s>>>(ws.jobs.as<AdjJob>(), nj,
+                                                                           uint32_t(total_pix), ws.gpix.as<double>());
+        RT_CHECK_LAUNCH();
         const unsigned grid = unsigned((total + kAdjPathsPerBlock - 1) / kAdjPathsPerBlock);
         k_adjoint<<<grid, kAdjThreads, shmem, s>>>(ws.jobs.as<AdjJob>(), nj, total, g.view(),
-                                                   g.things_dev.as<ThingDev>(), ws.G.as<double>(), g.nthings,
-                                                   sh_things, ws.err.as<uint32_t>());
+                                                   g.things_dev.as<ThingDev>(), ws.gpix.as<double>(),
+                                                   ws.G.as<double>(), g.nthings, sh_things, ws.err.as<uint32_t>());
         RT_CHECK_LAUNCH();
     }
     const unsigned gx = std::max(1u, std::min(64u, (max_things + 255) / 256));

@@ -1,8 +1,9 @@
 """GPU: the adjoint path-replay launch.
 
 Checked three ways: against the FP64 CPU adjoint of the oracle on the same
-image and loss gradient (every path's terms are computed with the same double
-operations, so only the summation order differs); against central finite
+image and loss gradient (albedo and sky terms are computed with the same double
+operations, so only the summation order differs, 1e-9 relative; the fuzz
+tangent runs in binary32 on the GPU, 2e-4 relative); against central finite
 differences of GPU renders with common random numbers (h = 1e-3) for albedo
 and sky colours, through a torch.autograd.Function that wraps the forward
 launch and the adjoint; and batch against single-scene launches.
@@ -63,10 +64,10 @@ def test_adjoint_matches_fp64_oracle(product, oracle, cuda, level, spp, depth):
     g_dev = torch.from_numpy(G.reshape(-1)).cuda()
     got = _adjoint(R, torch, sc, cam, params, img, g_dev)
     ref = wd.adjoint(oracle_camera(O, cam), W, H, spp, depth, seed, I, G, ambient=AMB, white=WHT)
-    _close(got["albedo"], ref["albedo"])
+    _close(got["albedo"], ref["albedo"])   # same FP64 terms, summation order differs
     _close(got["sky"], ref["sky"])
     if np.abs(ref["fuzz"]).max() > 0:
-        _close(got["fuzz"], ref["fuzz"])
+        _close(got["fuzz"], ref["fuzz"], rel=2e-4)   # the fuzz tangent runs in binary32 on the GPU
     # glass has no albedo gradient, only metals have a fuzz gradient
     types = np.array([wd.optics()["types"][k] for k in range(wd.nthings)])
     assert np.all(got["albedo"][types == 2] == 0)
