@@ -120,6 +120,23 @@ rt_status rt_scene_destroy(rt_scene scene);
 rt_status rt_scene_add_mesh(rt_scene scene, const rt_float3* vces, unsigned int nv,
                             const rt_uint3* ices, unsigned int ni, unsigned int* mesh_id);
 
+/* Object(file) + Scene::add per mesh (optx/object.cxx:23-106,
+ * optx/rtwo.cxx:138-145): reads a Wavefront OBJ file on the host; every shape
+ * (`o`/`g` group with faces) becomes one mesh of the scene.  Only `v` and `f`
+ * records are used (face vertices `i`, `i/t`, `i//n`, `i/t/n`, negative
+ * indices relative); faces of more than three vertices are split into fans.
+ * A shape's mesh holds the vertices its faces reference in order of first
+ * reference.  mesh_ids (cap entries, may be NULL) receives the new mesh ids,
+ * n_meshes their count.  RT_ERR_INVALID_ARG for unreadable files, malformed
+ * records and out-of-range indices (with file:line in the message). */
+rt_status rt_scene_add_obj(rt_scene scene, const char* path, unsigned int* mesh_ids, unsigned int cap,
+                           unsigned int* n_meshes);
+/* The same parser alone (host memory, no device use): the number of shapes,
+ * and for shape `shape` its vertex and triangle counts and arrays (any
+ * pointer may be NULL; with all four NULL only nshapes is filled). */
+rt_status rt_obj_parse(const char* path, unsigned int shape, rt_float3* vces, unsigned int* nv,
+                       rt_uint3* ices, unsigned int* ni, unsigned int* nshapes);
+
 /* Sphere(radius, ndiv) (optx/sphere.cxx:17-106) + Scene::add: tessellates a
  * regular tetrahedron ndiv times on the GPU (4*4^ndiv triangles, vertices
  * deduplicated in first-seen order) and adds the mesh.  ndiv <= 10. */

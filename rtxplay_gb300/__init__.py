@@ -96,6 +96,8 @@ SIGNATURES = {
     "rt_scene_destroy": [_P],
     "rt_scene_add_mesh": [_P, _P, _U, _P, _U, _PU],
     "rt_scene_add_sphere_mesh": [_P, _F, _U, _PU],
+    "rt_scene_add_obj": [_P, ctypes.c_char_p, _PU, _U, _PU],
+    "rt_obj_parse": [ctypes.c_char_p, _U, _P, _PU, _P, _PU, _PU],
     "rt_scene_get_mesh": [_P, _U, _P, _PU, _P, _PU],
     "rt_scene_add_thing": [_P, ctypes.POINTER(Optics), _U, _P, _PU],
     "rt_scene_add_analytic_sphere": [_P, float3, _F, ctypes.POINTER(Optics), _PU],
@@ -196,6 +198,21 @@ def optics(otype, albedo=(0, 0, 0), fuzz=0.0, index=0.0):
     return Optics(int(otype), f3(albedo), float(fuzz), float(index))
 
 
+def obj_parse(path):
+    """Host-side OBJ parse: a list of (vertices [n, 3] float32, triangles [m, 3] uint32) per shape."""
+    n = ctypes.c_uint()
+    check(lib().rt_obj_parse(path.encode(), 0, None, None, None, None, ctypes.byref(n)))
+    out = []
+    for k in range(n.value):
+        nv, ni = ctypes.c_uint(), ctypes.c_uint()
+        check(lib().rt_obj_parse(path.encode(), k, None, ctypes.byref(nv), None, ctypes.byref(ni), None))
+        v = np.zeros((nv.value, 3), np.float32)
+        i = np.zeros((ni.value, 3), np.uint32)
+        check(lib().rt_obj_parse(path.encode(), k, _ptr(v), None, _ptr(i), None, None))
+        out.append((v, i))
+    return out
+
+
 def rtow_spheres(rng_kind=RT_RECIPE_GLIBC, seed=1, half_extent=11):
     """The final-scene sphere list (host code, no GPU needed)."""
     n = ctypes.c_uint()
@@ -236,6 +253,15 @@ class Scene:
         mid = ctypes.c_uint()
         check(lib().rt_scene_add_mesh(self.h, _ptr(v), len(v), _ptr(i), len(i), ctypes.byref(mid)))
         return mid.value
+
+    def add_obj(self, path):
+        """Object(file): every shape of a Wavefront OBJ file as a mesh; returns the mesh ids."""
+        n = ctypes.c_uint()
+        check(lib().rt_obj_parse(path.encode(), 0, None, None, None, None, ctypes.byref(n)))
+        ids = (ctypes.c_uint * max(1, n.value))()
+        got = ctypes.c_uint()
+        check(lib().rt_scene_add_obj(self.h, path.encode(), ids, n.value, ctypes.byref(got)))
+        return [ids[k] for k in range(got.value)]
 
     def add_sphere_mesh(self, radius, ndiv):
         mid = ctypes.c_uint()
