@@ -59,6 +59,9 @@ def parse():
     p.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     p.add_argument("--batch-scenes", type=int, default=256, help="scenes of the batched leg (0: skip it)")
     p.add_argument("--no-adjoint", action="store_true", help="skip the adjoint/forward leg")
+    p.add_argument("--inverse-scenes", type=int, default=64, help="scenes of the inverse-rendering leg (0: skip)")
+    p.add_argument("--inverse-iters", type=int, default=10,
+                   help="Adam iterations of the inverse-rendering leg, batched and serial each")
     return p.parse_args()
 
 
@@ -352,6 +355,24 @@ def adjoint_leg(R, torch, sptr, stream, steps):
             "timing": "CUDA events around one rt_launch_ex and one rt_adjoint_launch, median of the timed steps"}
 
 
+def inverse_leg(torch, nscenes, iters):
+    """Batched inverse rendering: nscenes final-scene variants (half-extent
+    U{3..8}, level 4, 256x256, 16 spp, depth 8) optimised from albedo 0.5
+    towards their recipe albedos with Adam (lr 1e-2), batched launches against
+    scene-by-scene launches, same number of iterations."""
+    from rtxplay_gb300 import inverse
+    specs = inverse.inverse_specs(nscenes, seed=7, level=4, size=256, spp=16, depth=8)
+    e0, eb, lb, tb = inverse.run(torch, specs, iters, batched=True)
+    _, es, ls, ts = inverse.run(torch, specs, iters, batched=False)
+    return {"workload": f"{nscenes} final-scene variants, half-extent U{{3..8}}, level 4, 256x256, 16 spp, depth 8; "
+                        "albedos from 0.5 towards the recipe's, Adam lr 1e-2, L2 loss of the clamped image",
+            "iterations": iters, "batched_s": tb, "serial_s": ts, "speedup": ts / tb,
+            "batched_ms_per_iter": tb / iters * 1e3, "serial_ms_per_iter": ts / iters * 1e3,
+            "albedo_error_start": e0, "albedo_error_batched": eb, "albedo_error_serial": es,
+            "loss_batched": lb, "loss_serial": ls,
+            "timing": "host wall clock around the iterations (device synchronised on both ends)"}
+
+
 def main():
     args = parse()
     world, rank, local = dist_setup()
@@ -480,6 +501,10 @@ def main():
     if rank == 0 and world == 1 and not args.no_adjoint:
         adjoint = adjoint_leg(R, torch, sptr, stream, max(3, args.steps))
 
+    inverse_res = None
+    if rank == 0 and world == 1 and args.inverse_scenes > 0:
+        inverse_res = inverse_leg(torch, args.inverse_scenes, args.inverse_iters)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_oracle_run(args, args.cpu_seconds)
@@ -523,7 +548,7 @@ def main():
                 "rays_per_step": total_rays / args.steps / world,
                 "gpu_launches": launches,
                 "clocks": clk, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "batched": batched,
-                "adjoint": adjoint}
+                "adjoint": adjoint, "inverse": inverse_res}
         print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()

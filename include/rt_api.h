@@ -292,6 +292,27 @@ rt_status rt_batch_set_adjoint(rt_batch b, unsigned int index, const rt_float3* 
                                double* grad_albedo, double* grad_fuzz, double* grad_sky);
 rt_status rt_batch_adjoint(rt_batch b, void* stream);
 
+/* Device-side albedos (no reference counterpart): every thing's albedo from
+ * a device array of 3 floats per thing (a batch: all scenes' things in the
+ * order they were added), on `stream`, without a refit and without touching
+ * the host-side optics; a later rt_scene_set_optics of the scene re-uploads
+ * every thing's host-side optics. */
+rt_status rt_scene_set_albedos(rt_scene scene, const float* albedo, void* stream);
+rt_status rt_batch_set_albedos(rt_batch b, const float* albedo, void* stream);
+
+/* Inverse-rendering helpers (device pointers, asynchronous on `stream`):
+ * rt_l2_loss_grad writes grad = 2 (clamp(image, 0, 1) - target) for n pixels
+ * and adds sum (clamp(image) - target)^2 to *loss (a device double; NULL:
+ * not computed).  rt_adam_step is Adam (Kingma and Ba 2015) on n float
+ * parameters with a double gradient: m = b1 m + (1 - b1) g, v = b2 v +
+ * (1 - b2) g^2, theta -= lr (m / (1 - b1^step)) / (sqrt(v / (1 - b2^step)) +
+ * eps), then theta is clamped to [lo, hi]; step counts from 1. */
+rt_status rt_l2_loss_grad(const rt_float3* image, const rt_float3* target, rt_float3* grad_image,
+                          unsigned int n, double* loss, void* stream);
+rt_status rt_adam_step(float* theta, const double* grad, float* m, float* v, unsigned int n, float lr,
+                       float beta1, float beta2, float eps, unsigned int step, float lo, float hi,
+                       void* stream);
+
 /* ------------------------------------------------------------- adjoint */
 /* Gradients of an image loss (no counterpart in the reference): given the
  * rendered image `image` of this scene, camera and params (rawRGB of a

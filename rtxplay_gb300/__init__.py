@@ -138,6 +138,10 @@ SIGNATURES = {
     "rt_batch_set_adjoint": [_P, _U, _P, _P, _P, _P],
     "rt_batch_adjoint": [_P, _P],
     "rt_adjoint_launch": [_P, ctypes.POINTER(Camera), ctypes.POINTER(LaunchParams), _P, _P, _P, _P, _P, _P],
+    "rt_scene_set_albedos": [_P, _P, _P],
+    "rt_batch_set_albedos": [_P, _P, _P],
+    "rt_l2_loss_grad": [_P, _P, _P, _U, _P, _P],
+    "rt_adam_step": [_P, _P, _P, _P, _U, _F, _F, _F, _F, _U, _F, _F, _P],
 }
 
 _lib = None
@@ -313,6 +317,10 @@ class Scene:
             self.set_layout(layout)
         check(lib().rt_scene_build(self.h, morton_bits, stream))
 
+    def set_albedos(self, albedo, stream=None):
+        """rt_scene_set_albedos from a device pointer (3 floats per thing)."""
+        check(lib().rt_scene_set_albedos(self.h, albedo, stream))
+
     def adjoint(self, cam, params, image, grad_image, grad_albedo, grad_fuzz, grad_sky, stream=None):
         """rt_adjoint_launch; every buffer argument is a device pointer (int) or None."""
         check(lib().rt_adjoint_launch(self.h, ctypes.byref(cam), ctypes.byref(params), image, grad_image,
@@ -428,12 +436,26 @@ class Batch:
     def adjoint(self, stream=None):
         check(lib().rt_batch_adjoint(self.h, stream))
 
+    def set_albedos(self, albedo, stream=None):
+        """rt_batch_set_albedos from a device pointer (3 floats per thing, scenes in order)."""
+        check(lib().rt_batch_set_albedos(self.h, albedo, stream))
+
     def info(self):
         n, p = ctypes.c_uint(), ctypes.c_uint()
         ms = ctypes.c_float()
         b = ctypes.c_ulonglong()
         check(lib().rt_batch_info(self.h, ctypes.byref(n), ctypes.byref(p), ctypes.byref(ms), ctypes.byref(b)))
         return dict(n_scenes=n.value, n_prims=p.value, build_ms=ms.value, device_bytes=b.value)
+
+
+def l2_loss_grad(image, target, grad_image, n, loss=None, stream=None):
+    """rt_l2_loss_grad on device pointers (loss: device double pointer or None)."""
+    check(lib().rt_l2_loss_grad(image, target, grad_image, n, loss, stream))
+
+
+def adam_step(theta, grad, m, v, n, step, lr=1e-2, beta1=0.9, beta2=0.999, eps=1e-8, lo=0.0, hi=1.0, stream=None):
+    """rt_adam_step on device pointers."""
+    check(lib().rt_adam_step(theta, grad, m, v, n, lr, beta1, beta2, eps, step, lo, hi, stream))
 
 
 def render(scene, cam, params, guides=False):

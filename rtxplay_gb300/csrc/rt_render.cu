@@ -1090,6 +1090,14 @@ rt_status rt_batch_launch(rt_batch b, void* stream, rt_launch_stats* stats) {
     });
 }
 
+rt_status rt_batch_set_albedos(rt_batch b, const float* albedo, void* stream) {
+    return guarded([&] {
+        Batch* B = batch_from(b);
+        if (!B->built) throw Error(RT_ERR_NOT_BUILT, "batch not built (call rt_batch_build)");
+        set_albedos_device(B->geo, B->scenes, albedo, as_stream(stream));
+    });
+}
+
 rt_status rt_batch_set_adjoint(rt_batch b, unsigned int index, const rt_float3* grad_image, double* grad_albedo,
                                double* grad_fuzz, double* grad_sky) {
     return guarded([&] {

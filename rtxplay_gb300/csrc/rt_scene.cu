@@ -552,6 +552,18 @@ __global__ void k_refit(const float4* __restrict__ prims, uint32_t n, float4* no
     }
 }
 
+// Albedos of all things from a device array (3 floats per thing), for
+// optimisers that keep their parameters on the device.
+__global__ void k_set_albedos(ThingDev* __restrict__ things, const float* __restrict__ albedo, uint32_t n) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    float4 a = things[t].albedo_type;
+    a.x = albedo[3 * size_t(t)];
+    a.y = albedo[3 * size_t(t) + 1];
+    a.z = albedo[3 * size_t(t) + 2];
+    things[t].albedo_type = a;
+}
+
 __global__ void k_lbvh_snapshot_codes32(const uint32_t* __restrict__ c, uint32_t n, unsigned long long* __restrict__ o) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) o[i] = c[i];
@@ -968,6 +980,14 @@ void refit_geometry(Geometry& g, const std::vector<Scene*>& scenes, cudaStream_t
     cudaEventDestroy(e1);
 }
 
+void set_albedos_device(Geometry& g, const std::vector<Scene*>& scenes, const float* albedo, cudaStream_t s) {
+    RT_REQUIRE(albedo != nullptr, "albedo is NULL");
+    sync_optics(g, scenes, s);   // pending host-side optics first, so they cannot overwrite these later
+    if (g.nthings == 0) return;
+    k_set_albedos<<<grid_for(g.nthings), kThreads, 0, s>>>(g.things_dev.as<ThingDev>(), albedo, g.nthings);
+    RT_CHECK_LAUNCH();
+}
+
 void sync_optics(Geometry& g, const std::vector<Scene*>& scenes, cudaStream_t s) {
     RT_REQUIRE(scenes.size() == g.optics_seen.size(), "scene list differs from the built geometry");
     bool stale = false;
@@ -1225,6 +1245,14 @@ rt_status rt_scene_set_layout(rt_scene scene, int layout) {
         Scene* sc = scene_from(scene);
         if (sc->layout != layout) sc->topology_dirty = true;
         sc->layout = layout;
+    });
+}
+
+rt_status rt_scene_set_albedos(rt_scene scene, const float* albedo, void* stream) {
+    return guarded([&] {
+        Scene* sc = scene_from(scene);
+        if (!sc->built || sc->topology_dirty) throw Error(RT_ERR_NOT_BUILT, "scene not built (call rt_scene_build)");
+        set_albedos_device(sc->geo, {sc}, albedo, as_stream(stream));
     });
 }
 

@@ -104,6 +104,10 @@ void refit_geometry(Geometry& g, const std::vector<Scene*>& scenes, cudaStream_t
 // Re-uploads the per-thing optics of `g` when any scene's optics changed
 // since they were last uploaded (optics need no refit).
 void sync_optics(Geometry& g, const std::vector<Scene*>& scenes, cudaStream_t s);
+// Writes the albedos of all things of `g` from a device array (3 floats per
+// thing, in thing order) on stream `s`; the scenes' host-side optics are not
+// changed, and a later host-side optics change re-uploads every thing's optics.
+void set_albedos_device(Geometry& g, const std::vector<Scene*>& scenes, const float* albedo, cudaStream_t s);
 
 struct Scene {
     int layout = RT_LAYOUT_AUTO;  // requested layout of the next build
