@@ -72,7 +72,9 @@ struct JobDev {              // one render job on the device
 
 struct WaveState {
     uint32_t count[2];       // rays in queue 0 / 1
-    uint32_t fetch[2];       // next ray of queue 0 / 1 handed to a persistent traversal lane
+    uint32_t front[2];       // continuing rays, slots [0, front) of queue 0 / 1
+    uint32_t back[2];        // fresh camera rays, slots [cap - back, cap) of queue 0 / 1
+    uint32_t cap;            // queue capacity
     uint32_t cur;            // queue of the current wave
     uint32_t iter;           // waves run
     uint32_t max_iter;       // exact upper bound of the waves
@@ -131,11 +133,22 @@ __device__ __forceinline__ void make_camera_ray(const JobDev& j, uint32_t pid, f
     camera_ray(j.cam, pixel % j.W, pixel / j.W, j.W, j.H, s, o, d);
 }
 
-__global__ void k_init_state(WaveState* st, uint32_t n0, unsigned long long total, uint32_t max_iter) {
+// Queue slot of the i-th ray of a wave: continuing rays first, then the fresh
+// camera rays from the back of the queue (kept apart so that the pixel-
+// coherent primary rays share warps with each other, not with bounces).
+__device__ __forceinline__ uint32_t wave_slot(const WaveState* st, uint32_t cur, uint32_t i) {
+    const uint32_t f = st->front[cur];
+    return i < f ? i : st->cap - st->back[cur] + (i - f);
+}
+
+__global__ void k_init_state(WaveState* st, uint32_t n0, unsigned long long total, uint32_t max_iter, uint32_t cap) {
     st->count[0] = n0;
     st->count[1] = 0;
-    st->fetch[0] = 0;
-    st->fetch[1] = 0;
+    st->front[0] = n0;
+    st->front[1] = 0;
+    st->back[0] = 0;
+    st->back[1] = 0;
+    st->cap = cap;
     st->cur = 0;
     st->iter = 0;
     st->max_iter = max_iter;
@@ -177,13 +190,18 @@ __global__ void __launch_bounds__(kThreads)
     k_extend(Queues qs, float4* __restrict__ hits, uint32_t* __restrict__ hthing, WaveState* st,
              const JobDev* __restrict__ jobs, GeoView g) {
     const uint32_t cur = *((volatile uint32_t*)&st->cur);
-    if (blockIdx.x == 0 && threadIdx.x == 0) st->count[cur ^ 1] = 0;   // the next queue starts empty
+    if (blockIdx.x == 0 && threadIdx.x == 0) {   // the next queue starts empty
+        st->count[cur ^ 1] = 0;
+        st->front[cur ^ 1] = 0;
+        st->back[cur ^ 1] = 0;
+    }
     const uint32_t n = *((volatile uint32_t*)&st->count[cur]);
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t nvis = 0, ntest = 0;
     if (i < n) {
         const Queue Q = pick(qs, cur);
-        const float4 o4 = Q.ori[i], d4 = Q.dir[i];
+        const uint32_t q = wave_slot(st, cur, i);
+        const float4 o4 = Q.ori[q], d4 = Q.dir[q];
         const int root = jobs[__float_as_uint(d4.w) >> 8].root;
         const HitRec h = closest_hit<kCount, kInst>(g, root, xyz(o4), xyz(d4), nvis, ntest);
         // hit reference: top-level record (>= 0), miss (-1), or an instanced
@@ -221,8 +239,8 @@ __global__ void __launch_bounds__(kThreads, 4)
             const FlatDesc* __restrict__ desc, const ThingDev* __restrict__ things, Acc acc, int any_guides) {
     // per-warp counts, turned into block-exclusive offsets by thread 0, and the
     // block's bases from one global atomic per block (not one per warp)
-    __shared__ uint32_t s_warp[kThreads / 32];
-    __shared__ unsigned long long s_base;
+    __shared__ uint32_t s_warp[kThreads / 32], s_warp2[kThreads / 32];
+    __shared__ unsigned long long s_base, s_base2;
     const uint32_t cur = *((volatile uint32_t*)&st->cur);
     const uint32_t n = *((volatile uint32_t*)&st->count[cur]);
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -236,7 +254,8 @@ __global__ void __launch_bounds__(kThreads, 4)
     float3 gN{}, gA{};
     uint32_t pid = 0, bounce = 0, jx = 0;
     if (active) {
-        const float4 o4 = Q.ori[i], d4 = Q.dir[i], t4 = Q.thr[i], h4 = hits[i];
+        const uint32_t q = wave_slot(st, cur, i);
+        const float4 o4 = Q.ori[q], d4 = Q.dir[q], t4 = Q.thr[q], h4 = hits[i];
         pid = __float_as_uint(o4.w);
         const uint32_t tag = __float_as_uint(d4.w);
         jx = tag >> 8;
@@ -245,8 +264,8 @@ __global__ void __launch_bounds__(kThreads, 4)
         const float3 o = xyz(o4), d = xyz(d4);
         float3 thr = xyz(t4);
         if (any_guides) {
-            gN = xyz(Q.gn[i]);
-            gA = xyz(Q.ga[i]);
+            gN = xyz(Q.gn[q]);
+            gA = xyz(Q.ga[q]);
         }
         const int ref = __float_as_int(h4.w);
         float3 color = mk(0.f, 0.f, 0.f);
@@ -328,24 +347,32 @@ __global__ void __launch_bounds__(kThreads, 4)
     }
     if (cont) bounce += 1;
     const bool push = cont || fresh;
-    const uint32_t pm = __ballot_sync(0xFFFFFFFFu, push);
+    // continuing rays fill the next queue from the front, fresh rays from the back
+    const uint32_t pc = __ballot_sync(0xFFFFFFFFu, cont), pf = __ballot_sync(0xFFFFFFFFu, fresh);
     __syncthreads();   // every warp has read its regeneration offset
-    if (lane == 0) s_warp[warp] = __popc(pm);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t tot = 0;
-        for (uint32_t w = 0; w < kThreads / 32; ++w) {
-            const uint32_t c = s_warp[w];
-            s_warp[w] = tot;
-            tot += c;
-        }
-        s_base = tot ? (unsigned long long)atomicAdd(&st->count[cur ^ 1], tot) : 0ull;
+    if (lane == 0) {
+        s_warp[warp] = __popc(pc);
+        s_warp2[warp] = __popc(pf);
     }
     __syncthreads();
-    if (pm) {
-        const uint32_t base = uint32_t(s_base) + s_warp[warp];
+    if (threadIdx.x == 0) {
+        uint32_t tc = 0, tf = 0;
+        for (uint32_t w = 0; w < kThreads / 32; ++w) {
+            const uint32_t c = s_warp[w], f = s_warp2[w];
+            s_warp[w] = tc;
+            s_warp2[w] = tf;
+            tc += c;
+            tf += f;
+        }
+        s_base = tc ? (unsigned long long)atomicAdd(&st->front[cur ^ 1], tc) : 0ull;
+        s_base2 = tf ? (unsigned long long)atomicAdd(&st->back[cur ^ 1], tf) : 0ull;
+    }
+    __syncthreads();
+    if (pc | pf) {
         if (push) {
-            const uint32_t slot = base + __popc(pm & ((1u << lane) - 1u));
+            const uint32_t lt = (1u << lane) - 1u;
+            const uint32_t slot = cont ? uint32_t(s_base) + s_warp[warp] + __popc(pc & lt)
+                                       : st->cap - 1u - (uint32_t(s_base2) + s_warp2[warp] + __popc(pf & lt));
             N.ori[slot] = make_float4(no.x, no.y, no.z, __uint_as_float(pid));
             N.dir[slot] = make_float4(nd.x, nd.y, nd.z, __uint_as_float((jx << 8) | bounce));
             N.thr[slot] = make_float4(nthr.x, nthr.y, nthr.z, 0.f);
@@ -365,6 +392,7 @@ __global__ void k_wave_ctrl(WaveState* st, cudaGraphConditionalHandle handle, in
     if (st->count[cur] != 0) st->iter += 1;   // a wave ran (the host loop may run empty ones)
     const uint32_t next = cur ^ 1u;
     st->cur = next;
+    st->count[next] = st->front[next] + st->back[next];
     bool more = st->count[next] != 0;
     if (more && st->iter >= st->max_iter) {
         st->err |= 2u;
@@ -723,7 +751,7 @@ void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s
     RT_CUDA(cudaMemsetAsync(ws.acc.p, 0, size_t(total_pix) * 28, s));
     if (any_guides) RT_CUDA(cudaMemsetAsync(ws.acc_gd.p, 0, size_t(total_pix) * 48, s));
     const uint32_t n0 = W;
-    k_init_state<<<1, 1, 0, s>>>(L.st, n0, total_paths, uint32_t(max_iter64));
+    k_init_state<<<1, 1, 0, s>>>(L.st, n0, total_paths, uint32_t(max_iter64), W);
     k_generate<<<grid_for(n0), kThreads, 0, s>>>(L.jobs, nj, L.qs.q[0], n0, any_guides);
     RT_CHECK_LAUNCH();
     uint32_t launches = 2;
