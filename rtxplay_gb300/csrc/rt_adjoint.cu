@@ -182,7 +182,7 @@ __device__ uint32_t adjoint_path(const AdjJob* __restrict__ jobs, uint32_t nj, u
     const uint32_t jx = adj_job_of(jobs, nj, path);
     const AdjJob& j = jobs[jx];
     const uint32_t pid = uint32_t(path - j.path_offset);
-    const uint32_t pix = pid % j.npix, smp = pid / j.npix;
+    const uint32_t pix = pid / j.spp, smp = pid % j.spp;   // pixel-major, as the forward wavefront
     double g[3];
     {
         const double* gp = gpix + 3 * (size_t(j.pix_offset) + pix);
