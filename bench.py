@@ -72,6 +72,17 @@ def dist_setup():
     return world, rank, local
 
 
+def combine_replicas(dist, seconds, rays, device):
+    """Replicas (one independent frame per rank): the job's time is the
+    slowest rank's, its rays the sum over ranks.  Returns (seconds, rays)."""
+    import torch
+    t = torch.tensor([float(seconds)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    r = torch.tensor([float(rays)], dtype=torch.float64, device=device)
+    dist.all_reduce(r)
+    return float(t.item()), float(r.item())
+
+
 def load_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -443,12 +454,7 @@ def main():
     torch.cuda.synchronize()
     clk = clocks.stop()
     if dist:
-        t = torch.tensor([elapsed_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
-        r = torch.tensor([float(rays)], device="cuda", dtype=torch.float64)
-        dist.all_reduce(r)
-        total_rays = float(r.item())
+        elapsed_ms, total_rays = combine_replicas(dist, elapsed_ms, rays, "cuda")
     else:
         total_rays = float(rays)
     value = total_rays / (elapsed_ms * 1e-3) / 1e6
@@ -488,10 +494,8 @@ def main():
         e2e = {"value": e2e_rays / dt / 1e6, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h)}
         if dist:
-            t = torch.tensor([dt, float(e2e_rays)], device="cuda", dtype=torch.float64)
-            dist.all_reduce(t[0:1], op=dist.ReduceOp.MAX)
-            dist.all_reduce(t[1:2])
-            e2e["value"] = float(t[1].item()) / float(t[0].item()) / 1e6
+            dt_all, rays_all = combine_replicas(dist, dt, e2e_rays, "cuda")
+            e2e["value"] = rays_all / dt_all / 1e6
 
     batched = None
     if rank == 0 and world == 1 and args.batch_scenes > 0:
