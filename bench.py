@@ -92,13 +92,14 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
-LAYOUTS = {"auto": 0, "flat": 1, "instanced": 2, "grouped": 3}
+LAYOUTS = {"auto": 0, "flat": 1, "instanced": 2, "grouped": 3, "sah": 4}
 
 
 def profile_dram_bytes_per_ray(layout):
     """DRAM bytes per ray of k_extend from the committed ncu summary of the
     layout (one capture of full-wave launches), or None."""
-    name = {1: "k_extend_c1.txt", 2: "k_extend_c1_instanced.txt", 3: "k_extend_c1_grouped.txt"}.get(layout, "")
+    name = {1: "k_extend_c1.txt", 2: "k_extend_c1_instanced.txt", 3: "k_extend_c1_grouped.txt",
+            4: "k_extend_c1_sah.txt"}.get(layout, "")
     path = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(path):
         return None
@@ -542,7 +543,7 @@ def main():
                 "config": {"workload": f"rtow final scene, level-{args.level} tessellation "
                                        f"({info.n_prims} triangles), {W}x{H}, {args.spp} spp, depth {args.depth}",
                            "parallelism": f"replicas x{world}", "morton_bits": info.morton_bits,
-                           "layout": {1: "flat", 2: "instanced", 3: "grouped"}.get(info.layout, str(info.layout)),
+                           "layout": {1: "flat", 2: "instanced", 3: "grouped", 4: "sah"}.get(info.layout, str(info.layout)),
                            "top_records": info.n_top_records, "bottom_records": info.n_bottom_records,
                            "wave_loop": "CUDA graph (conditional WHILE node)" if os.environ.get("RTX_GRAPH", "1") != "0"
                            else "host-driven",

@@ -196,12 +196,17 @@ rt_status rt_scene_set_optics(rt_scene scene, unsigned int thing_id, const rt_op
  *     LBVH per mesh, a top-level LBVH over instance records, analytic spheres
  *     and the triangles of things that cannot be instanced (non-diagonal
  *     transforms, meshes under 16 triangles); memory-lean, more work per step.
+ *   SAH: the flat world-space hierarchy built top-down by binned
+ *     surface-area-heuristic splits (32 bins per axis) down to clusters of at
+ *     most 256 primitives, each cluster an LBVH over 30-bit Morton codes
+ *     inside its own bounds; fewest node visits per ray, slowest build.
  * Hits, ids and images do not depend on the layout (tested bit for bit). */
 typedef enum {
     RT_LAYOUT_AUTO = 0,
     RT_LAYOUT_FLAT = 1,
     RT_LAYOUT_INSTANCED = 2,
-    RT_LAYOUT_GROUPED = 3
+    RT_LAYOUT_GROUPED = 3,
+    RT_LAYOUT_SAH = 4
 } rt_layout;
 rt_status rt_scene_set_layout(rt_scene scene, int layout);
 
@@ -222,7 +227,7 @@ typedef struct {
     unsigned long long device_bytes;
     float build_ms;   /* last rt_scene_build, CUDA events */
     float refit_ms;   /* last rt_scene_update */
-    unsigned int layout;          /* resolved layout: FLAT, GROUPED or INSTANCED */
+    unsigned int layout;          /* resolved layout: FLAT, GROUPED, SAH or INSTANCED */
     unsigned int n_instances;     /* instanced things */
     unsigned int n_top_records;   /* top-level LBVH leaves */
     unsigned int n_bottom_records;/* bottom-level triangles (all instanced meshes) */

@@ -1121,7 +1121,7 @@ rt_status rt_batch_add(rt_batch b, rt_scene scene, const rt_camera* cam, const r
 
 rt_status rt_batch_set_layout(rt_batch b, int layout) {
     return guarded([&] {
-        RT_REQUIRE(layout >= RT_LAYOUT_AUTO && layout <= RT_LAYOUT_GROUPED, "unknown layout");
+        RT_REQUIRE(layout >= RT_LAYOUT_AUTO && layout <= RT_LAYOUT_SAH, "unknown layout");
         Batch* B = batch_from(b);
         if (B->layout != layout) B->built = false;
         B->layout = layout;

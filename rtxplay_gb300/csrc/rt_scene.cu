@@ -7,12 +7,14 @@
 // a 48-byte optics record per thing.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <numeric>
 #include <vector>
 
 #include "rt_scene.h"
+#include "rt_lbvh.cuh"
 
 namespace rt {
 namespace {
@@ -199,31 +201,6 @@ __global__ void k_flatten_top(const FlatDesc* __restrict__ desc, uint32_t nthing
 }
 
 // ------------------------------------------------------------------- LBVH
-struct Box3 {
-    float3 lo, hi;
-};
-
-__device__ __forceinline__ Box3 prim_box(const float4* __restrict__ rec) {
-    const float4 a = rec[0], b = rec[1], c = rec[2];
-    if (__float_as_uint(c.w) == kPrimInstance) return Box3{xyz(a), xyz(b)};
-    if (__float_as_uint(c.w) == kPrimTriangle) {
-        return Box3{mk(fminf(fminf(a.x, b.x), c.x), fminf(fminf(a.y, b.y), c.y), fminf(fminf(a.z, b.z), c.z)),
-                    mk(fmaxf(fmaxf(a.x, b.x), c.x), fmaxf(fmaxf(a.y, b.y), c.y), fmaxf(fmaxf(a.z, b.z), c.z))};
-    }
-    const float r = b.x;
-    return Box3{mk(a.x - r, a.y - r, a.z - r), mk(a.x + r, a.y + r, a.z + r)};
-}
-
-__device__ __forceinline__ float3 centroid(const Box3& b) { return mul(0.5f, add(b.lo, b.hi)); }
-
-__device__ __forceinline__ uint32_t ford(float f) {   // float -> order-preserving u32
-    const uint32_t b = __float_as_uint(f);
-    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
-}
-__device__ __forceinline__ float fdeord(uint32_t o) {
-    return __uint_as_float((o & 0x80000000u) ? (o & 0x7FFFFFFFu) : ~o);
-}
-
 __global__ void k_init_bounds(uint32_t* b, uint32_t nsegs) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= 6 * nsegs) return;
@@ -270,29 +247,6 @@ __global__ void k_centroid_bounds(const float4* __restrict__ prims, const uint32
     }
 }
 
-__device__ __forceinline__ uint32_t expand10(uint32_t x) {
-    x = (x * 0x00010001u) & 0xFF0000FFu;
-    x = (x * 0x00000101u) & 0x0F00F00Fu;
-    x = (x * 0x00000011u) & 0xC30C30C3u;
-    x = (x * 0x00000005u) & 0x49249249u;
-    return x;
-}
-__device__ __forceinline__ unsigned long long expand20(unsigned long long x) {
-    x &= 0xFFFFFull;
-    x = (x | x << 32) & 0x001F00000000FFFFull;
-    x = (x | x << 16) & 0x001F0000FF0000FFull;
-    x = (x | x << 8) & 0x100F00F00F00F00Full;
-    x = (x | x << 4) & 0x10C30C30C30C30C3ull;
-    x = (x | x << 2) & 0x1249249249249249ull;
-    return x;
-}
-__device__ __forceinline__ float quantf(float c, float lo, float ext, float cells) {
-    const float f = ext > 0.f ? (c - lo) / ext : 0.f;
-    const float q = f * cells;
-    const float top = cells - 1.f;
-    return q < 0.f ? 0.f : (q > top ? top : q);
-}
-
 template <class K>
 __global__ void k_morton(const float4* __restrict__ prims, const uint32_t* __restrict__ prim_seg, uint32_t n,
                          const uint32_t* __restrict__ bounds, K* __restrict__ codes, uint32_t* __restrict__ ids) {
@@ -315,15 +269,6 @@ __global__ void k_morton(const float4* __restrict__ prims, const uint32_t* __res
         codes[i] = K((expand20(qx) << 2) | (expand20(qy) << 1) | expand20(qz));
     }
     ids[i] = i;
-}
-
-__device__ __forceinline__ uint32_t seg_of(const SegDev* __restrict__ segs, uint32_t nsegs, uint32_t pos) {
-    uint32_t lo = 0, hi = nsegs;
-    while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (segs[mid].prim_begin <= pos) lo = mid; else hi = mid;
-    }
-    return lo;
 }
 
 // Things-grouped hierarchy (a flat, world-space LBVH with the shape of a
@@ -429,62 +374,6 @@ __global__ void k_permute(const K* __restrict__ codes_in, const uint32_t* __rest
     if (i >= n) return;
     codes_out[i] = codes_in[perm[i]];
     ids_out[i] = ids_in[perm[i]];
-}
-
-// Karras 2012 over one segment's sorted codes (local indices, so a segment's
-// hierarchy is the one a standalone build of that scene gives); equal keys
-// fall back to the index bits, 64 + clz(i ^ j).
-template <class K>
-__device__ __forceinline__ int kdelta(const K* __restrict__ k, int n, int i, int j) {
-    if (j < 0 || j >= n) return -1;
-    const unsigned long long a = (unsigned long long)k[i], b = (unsigned long long)k[j];
-    if (a != b) return __clzll((long long)(a ^ b));
-    return 64 + __clz(i ^ j);
-}
-
-// One thread per node slot.  Slot P + i (i < n - 1) of a segment starting at
-// P with n primitives is its internal node i; a one-primitive segment puts its
-// leaf in both child slots of node P (marked for the refit by parent -2).
-template <class K>
-__global__ void k_karras(const K* __restrict__ codes, const SegDev* __restrict__ segs, uint32_t nsegs, uint32_t ntot,
-                         float4* __restrict__ nodes, int* __restrict__ parent_leaf, int* __restrict__ parent_int) {
-    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
-    if (slot >= ntot) return;
-    const SegDev sg = segs[seg_of(segs, nsegs, slot)];
-    const int n = int(sg.prim_count);
-    const int i = int(slot - sg.prim_begin);
-    const int P = int(sg.prim_begin);
-    if (n == 1) {
-        nodes[4 * size_t(P) + 3] = make_float4(__int_as_float(~P), __int_as_float(~P), 0.f, 0.f);
-        parent_leaf[P] = -2;
-        parent_int[P] = -1;
-        return;
-    }
-    if (i >= n - 1) return;   // the spare slot of the segment
-    const K* k = codes + P;
-    const int d = (kdelta(k, n, i, i + 1) - kdelta(k, n, i, i - 1)) >= 0 ? 1 : -1;
-    const int dmin = kdelta(k, n, i, i - d);
-    int lmax = 2;
-    while (kdelta(k, n, i, i + lmax * d) > dmin) lmax <<= 1;
-    int l = 0;
-    for (int t = lmax >> 1; t >= 1; t >>= 1)
-        if (kdelta(k, n, i, i + (l + t) * d) > dmin) l += t;
-    const int j = i + l * d;
-    const int dnode = kdelta(k, n, i, j);
-    int s = 0;
-    int t = l;
-    do {
-        t = (t + 1) >> 1;
-        if (kdelta(k, n, i, i + (s + t) * d) > dnode) s += t;
-    } while (t > 1);
-    const int gamma = i + s * d + (d < 0 ? -1 : 0);
-    const int lo = min(i, j), hi = max(i, j);
-    const int left = (lo == gamma) ? ~(P + gamma) : P + gamma;
-    const int right = (hi == gamma + 1) ? ~(P + gamma + 1) : P + gamma + 1;
-    nodes[4 * size_t(P + i) + 3] = make_float4(__int_as_float(left), __int_as_float(right), 0.f, 0.f);
-    if (left < 0) parent_leaf[~left] = P + i; else parent_int[left] = P + i;
-    if (right < 0) parent_leaf[~right] = P + i; else parent_int[right] = P + i;
-    if (i == 0) parent_int[P] = -1;
 }
 
 __global__ void k_gather_prims(const float4* __restrict__ flat, const uint32_t* __restrict__ ids, uint32_t n,
@@ -817,14 +706,26 @@ void build_topology(Lbvh& L, cudaStream_t s) {
     RT_CHECK_LAUNCH();
 }
 
+// Largest cluster of the binned-SAH layout: kSahClusterMax, or RTX_SAH_CLUSTER
+// (tests use small clusters to get deep split trees from small scenes).
+uint32_t sah_cluster_max() {
+    const char* v = std::getenv("RTX_SAH_CLUSTER");
+    if (!v || !*v) return kSahClusterMax;
+    const unsigned long x = std::strtoul(v, nullptr, 10);
+    return x >= 1 && x <= (1u << 20) ? uint32_t(x) : kSahClusterMax;
+}
+
 // Morton codes (or things-grouped keys, for top-level records whose a.w is
 // the thing), sort, hierarchy and refit of an LBVH whose records are in
 // prims_flat.
 void build_lbvh(Lbvh& L, int morton_bits, cudaStream_t s, const FlatDesc* desc = nullptr,
-                const std::vector<FlatDesc>* desc_host = nullptr, const std::vector<uint32_t>* thing_begin = nullptr) {
+                const std::vector<FlatDesc>* desc_host = nullptr, const std::vector<uint32_t>* thing_begin = nullptr,
+                bool sah = false) {
     L.morton_bits = morton_bits;
     const uint32_t nthings = desc_host ? uint32_t(desc_host->size()) : 0u;
-    L.grouped = desc != nullptr && nthings > 0 && L.nprims > 0;
+    L.sah = sah && L.nprims > 0;
+    L.grouped = !L.sah && desc != nullptr && nthings > 0 && L.nprims > 0;
+    L.nclusters = L.sah_levels = 0;
     L.nthings = nthings;
     L.roots.clear();
     if (L.grouped) {
@@ -865,7 +766,9 @@ void build_lbvh(Lbvh& L, int morton_bits, cudaStream_t s, const FlatDesc* desc =
                                                         L.nsegs > 1 ? L.prim_seg.as<uint32_t>() : nullptr, n,
                                                         L.bounds.as<uint32_t>(), 0);
     RT_CHECK_LAUNCH();
-    if (L.grouped) {
+    if (L.sah) {
+        build_sah_topology(L, sah_cluster_max(), s);
+    } else if (L.grouped) {
         const uint32_t T = nthings;
         L.tbounds.reserve(size_t(T) * 6 * sizeof(uint32_t));
         L.tcodes.reserve(size_t(T) * 8 * 2);
@@ -923,7 +826,7 @@ void build_lbvh(Lbvh& L, int morton_bits, cudaStream_t s, const FlatDesc* desc =
 
 void build_geometry(Geometry& g, const std::vector<Scene*>& scenes, int morton_bits, int layout, cudaStream_t s) {
     RT_REQUIRE(morton_bits == 0 || morton_bits == 30 || morton_bits == 60, "morton_bits must be 0, 30 or 60");
-    RT_REQUIRE(layout >= RT_LAYOUT_AUTO && layout <= RT_LAYOUT_GROUPED, "unknown layout");
+    RT_REQUIRE(layout >= RT_LAYOUT_AUTO && layout <= RT_LAYOUT_SAH, "unknown layout");
     RT_REQUIRE(!scenes.empty(), "no scenes to build");
     g.morton_bits = morton_bits == 0 ? 60 : morton_bits;
     g.layout_req = layout;
@@ -934,17 +837,18 @@ void build_geometry(Geometry& g, const std::vector<Scene*>& scenes, int morton_b
     const Plan P = make_plan(scenes, layout);
     upload_plan(g, P, scenes.size(), s);
     g.layout = P.ninstances ? RT_LAYOUT_INSTANCED
-                            : (layout == RT_LAYOUT_AUTO || layout == RT_LAYOUT_GROUPED) ? RT_LAYOUT_GROUPED
-                                                                                       : RT_LAYOUT_FLAT;
+               : layout == RT_LAYOUT_SAH ? RT_LAYOUT_SAH
+               : (layout == RT_LAYOUT_AUTO || layout == RT_LAYOUT_GROUPED) ? RT_LAYOUT_GROUPED
+                                                                           : RT_LAYOUT_FLAT;
     g.optics_seen.assign(scenes.size(), 0);
     for (size_t si = 0; si < scenes.size(); ++si) g.optics_seen[si] = scenes[si]->optics_version;
     g.misc.reserve(256);
     flatten_bottom(g, P, s);
     build_lbvh(g.blas, g.morton_bits, s);   // object space, before the instance boxes are taken
     flatten_top(g, s);
-    const bool grouped = (layout == RT_LAYOUT_AUTO || layout == RT_LAYOUT_GROUPED) && P.ninstances == 0;
+    const bool grouped = g.layout == RT_LAYOUT_GROUPED;
     build_lbvh(g.top, g.morton_bits, s, grouped ? g.desc.as<FlatDesc>() : nullptr, grouped ? &g.desc_host : nullptr,
-               &g.thing_begin);
+               &g.thing_begin, g.layout == RT_LAYOUT_SAH);
     RT_CUDA(cudaEventRecord(e1, s));
     RT_CUDA(cudaEventSynchronize(e1));
     RT_CUDA(cudaEventElapsedTime(&g.build_ms, e0, e1));
@@ -1007,7 +911,8 @@ void sync_optics(Geometry& g, const std::vector<Scene*>& scenes, cudaStream_t s)
 
 size_t Lbvh::device_bytes() const {
     return segs.bytes + prim_seg.bytes + prims_flat.bytes + prims.bytes + nodes.bytes + codes.bytes + ids.bytes +
-           parents.bytes + flags.bytes + bounds.bytes + sort_tmp.bytes + seg_tmp.bytes;
+           parents.bytes + flags.bytes + bounds.bytes + sort_tmp.bytes + seg_tmp.bytes + tbounds.bytes + tcodes.bytes +
+           tids.bytes + tsegs.bytes + scene_things.bytes + tseg.bytes + ttmp.bytes + sah_tmp.bytes;
 }
 
 size_t Geometry::device_bytes() const {
@@ -1241,7 +1146,7 @@ rt_status rt_scene_set_optics(rt_scene scene, unsigned int thing_id, const rt_op
 
 rt_status rt_scene_set_layout(rt_scene scene, int layout) {
     return guarded([&] {
-        RT_REQUIRE(layout >= RT_LAYOUT_AUTO && layout <= RT_LAYOUT_GROUPED, "unknown layout");
+        RT_REQUIRE(layout >= RT_LAYOUT_AUTO && layout <= RT_LAYOUT_SAH, "unknown layout");
         Scene* sc = scene_from(scene);
         if (sc->layout != layout) sc->topology_dirty = true;
         sc->layout = layout;

@@ -47,14 +47,17 @@ struct Lbvh {
     // things-grouped hierarchy: per-thing centroid bounds, thing codes and order,
     // per-thing record ranges, per-scene thing ranges, thing -> scene, scratch
     DevBuf tbounds, tcodes, tids, tsegs, scene_things, tseg, ttmp;
+    DevBuf sah_tmp;         // binned-SAH builder scratch
     uint32_t nprims = 0, nsegs = 0, nthings = 0;
+    uint32_t nclusters = 0, sah_levels = 0;   // binned-SAH hierarchies
     int morton_bits = 60;
     int grouped = 0;
+    int sah = 0;
     std::vector<SegDev> seg_host;
-    std::vector<int> roots;   // per segment, grouped hierarchies only
+    std::vector<int> roots;   // per segment, grouped and binned-SAH hierarchies
     size_t device_bytes() const;
     int root(uint32_t seg) const {
-        if (grouped) return roots[seg];
+        if (grouped || sah) return roots[seg];
         return seg_host[seg].prim_count ? int(seg_host[seg].prim_begin) : -1;
     }
 };
@@ -98,6 +101,12 @@ struct Geometry {
 // a Karras hierarchy emitted per segment and refit bottom-up.  Synchronous on
 // `s`.
 void build_geometry(Geometry& g, const std::vector<Scene*>& scenes, int morton_bits, int layout, cudaStream_t s);
+
+// Binned-SAH topology of an LBVH whose records are in prims_flat and whose
+// segment centroid bounds are in `bounds` (rt_sah.cu): leaf order (codes,
+// ids), node children, parents and per-segment roots; the refit follows.
+constexpr uint32_t kSahClusterMax = 256;
+void build_sah_topology(Lbvh& L, uint32_t cluster_max, cudaStream_t s);
 // Re-flattens the top level with the scenes' current transforms and refits it
 // (a full build when a thing changed between instanced and flattened).
 void refit_geometry(Geometry& g, const std::vector<Scene*>& scenes, cudaStream_t s);

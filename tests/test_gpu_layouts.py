@@ -3,9 +3,9 @@
 A scene mixing analytic spheres, diagonally transformed mesh things
 (instanced: one object-space LBVH per mesh under a top level), a negative
 scale (instanced, box bounds swap), rotated things and a small mesh (both
-flattened to world space) is rendered with RT_LAYOUT_FLAT, RT_LAYOUT_INSTANCED
-and RT_LAYOUT_AUTO; every image, ray count and first hit must be identical
-and equal to the oracle's (which always uses one flat LBVH).
+flattened to world space) is rendered with RT_LAYOUT_FLAT, RT_LAYOUT_INSTANCED,
+RT_LAYOUT_AUTO and RT_LAYOUT_SAH; every image, ray count and first hit must be
+identical and equal to the oracle's (which always uses one flat LBVH).
 """
 import numpy as np
 import pytest
@@ -76,7 +76,9 @@ def test_layout_info(product, oracle, cuda):
     flat, _ = _build_pair(R, O, R.RT_LAYOUT_FLAT)
     inst, _ = _build_pair(R, O, R.RT_LAYOUT_INSTANCED)
     auto, _ = _build_pair(R, O, R.RT_LAYOUT_AUTO)
-    fi, ii, ai = flat.info(), inst.info(), auto.info()
+    sah, _ = _build_pair(R, O, R.RT_LAYOUT_SAH)
+    fi, ii, ai, si = flat.info(), inst.info(), auto.info(), sah.info()
+    assert si.layout == R.RT_LAYOUT_SAH and si.n_top_records == fi.n_top_records and si.n_instances == 0
     assert fi.layout == R.RT_LAYOUT_FLAT and fi.n_instances == 0 and fi.n_bottom_records == 0
     assert ii.layout == R.RT_LAYOUT_INSTANCED and ai.layout == R.RT_LAYOUT_GROUPED
     assert fi.n_prims == ii.n_prims == ai.n_prims == fi.n_top_records == ai.n_top_records
@@ -91,7 +93,7 @@ def test_layouts_render_identically_and_match_oracle(product, oracle, cuda, w, h
     cam = R.camera_set((0, 2.5, 9), (0, 0.3, 0), (0, 1, 0), 40, w / h, 0.05, 9.0)
     params = R.launch_params(w, h, spp, depth=depth, seed=31, flags=R.RT_FLAG_GUIDES)
     outs = []
-    for layout in (R.RT_LAYOUT_FLAT, R.RT_LAYOUT_INSTANCED, R.RT_LAYOUT_AUTO):
+    for layout in (R.RT_LAYOUT_FLAT, R.RT_LAYOUT_INSTANCED, R.RT_LAYOUT_AUTO, R.RT_LAYOUT_SAH):
         sc, wd = _build_pair(R, O, layout)
         outs.append(R.render(sc, cam, params, guides=True))
     ref = wd.render(oracle_camera(O, cam), w, h, spp, depth, 31)
@@ -108,7 +110,7 @@ def test_layouts_first_hit_and_fp64_distance(product, oracle, cuda):
     w, h = 160, 120
     cam = R.camera_set((0, 2.5, 9), (0, 0.3, 0), (0, 1, 0), 40, w / h, 0.0, 9.0)
     params = R.launch_params(w, h, 1, seed=5)
-    for layout in (R.RT_LAYOUT_FLAT, R.RT_LAYOUT_INSTANCED, R.RT_LAYOUT_GROUPED):
+    for layout in (R.RT_LAYOUT_FLAT, R.RT_LAYOUT_INSTANCED, R.RT_LAYOUT_GROUPED, R.RT_LAYOUT_SAH):
         sc, wd = _build_pair(R, O, layout)
         g = device_first_hit(R, cuda, sc, cam, params)
         c = wd.first_hit(oracle_camera(O, cam), w, h, 5, fp64=True)
@@ -156,7 +158,7 @@ def test_flat_and_instanced_batches_agree(product, cuda):
     from _helpers import dptr
     specs = [(3, 3, 48, 32, 2, 16, 5), (2, 2, 32, 32, 3, 8, 6), (None, 4, 40, 24, 2, 16, 7)]
     imgs = {}
-    for layout in (R.RT_LAYOUT_FLAT, R.RT_LAYOUT_INSTANCED, R.RT_LAYOUT_GROUPED):
+    for layout in (R.RT_LAYOUT_FLAT, R.RT_LAYOUT_INSTANCED, R.RT_LAYOUT_GROUPED, R.RT_LAYOUT_SAH):
         batch = R.Batch()
         bufs = []
         for level, he, w, h, spp, depth, seed in specs:
@@ -171,7 +173,7 @@ def test_flat_and_instanced_batches_agree(product, cuda):
         batch.launch()
         torch.cuda.synchronize()
         imgs[layout] = [(a.cpu().numpy(), b.cpu().numpy()) for a, b in bufs]
-    for other in (R.RT_LAYOUT_INSTANCED, R.RT_LAYOUT_GROUPED):
+    for other in (R.RT_LAYOUT_INSTANCED, R.RT_LAYOUT_GROUPED, R.RT_LAYOUT_SAH):
         for (a, b), (c, d) in zip(imgs[R.RT_LAYOUT_FLAT], imgs[other]):
             assert np.array_equal(a.view(np.uint32), c.view(np.uint32))
             assert np.array_equal(b, d)

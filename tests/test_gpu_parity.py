@@ -76,7 +76,7 @@ def test_lbvh_bit_exact_vs_oracle_twin(product, oracle, cuda, bits, level, layou
     assert np.array_equal(a["boxes"].view(np.uint32), b["boxes"].view(np.uint32))
 
 
-@pytest.mark.parametrize("layout", [1, 2, 3])
+@pytest.mark.parametrize("layout", [1, 2, 3, 4])
 def test_lbvh_topology_is_a_binary_tree(product, cuda, layout):
     sc = product.rtow_scene(3, layout=layout)
     t = sc.lbvh()
@@ -99,7 +99,7 @@ def test_lbvh_topology_is_a_binary_tree(product, cuda, layout):
 
 
 # ------------------------------------------------------------------- first hit
-@pytest.mark.parametrize("layout", [1, 2, 3])
+@pytest.mark.parametrize("layout", [1, 2, 3, 4])
 @pytest.mark.parametrize("level,w,h", [(None, 192, 108), (2, 192, 108), (3, 320, 180)])
 def test_first_hit_bit_exact_vs_oracle(product, oracle, cuda, level, w, h, layout):
     R, O = product, oracle
@@ -115,7 +115,7 @@ def test_first_hit_bit_exact_vs_oracle(product, oracle, cuda, level, w, h, layou
     assert (g["prim"] >= 0).mean() > 0.5
 
 
-@pytest.mark.parametrize("layout", [1, 2, 3])
+@pytest.mark.parametrize("layout", [1, 2, 3, 4])
 def test_first_hit_equals_brute_force(product, oracle, cuda, layout):
     R, O = product, oracle
     sc, wd = rtow_pair(R, O, 1, half_extent=4, layout=layout)
@@ -127,7 +127,7 @@ def test_first_hit_equals_brute_force(product, oracle, cuda, layout):
     assert np.array_equal(g["t"].view(np.uint32), c["t"].view(np.uint32))
 
 
-@pytest.mark.parametrize("layout", [1, 2, 3])
+@pytest.mark.parametrize("layout", [1, 2, 3, 4])
 def test_first_hit_t_within_1e5_of_fp64(product, oracle, cuda, layout):
     R, O = product, oracle
     sc, wd = rtow_pair(R, O, 3, layout=layout)
@@ -159,7 +159,7 @@ def test_picker_matches_first_hit(product, oracle, cuda):
 
 
 # ----------------------------------------------------------------------- render
-@pytest.mark.parametrize("layout", [1, 2, 3])
+@pytest.mark.parametrize("layout", [1, 2, 3, 4])
 @pytest.mark.parametrize("level,w,h,spp,depth", [(None, 64, 36, 4, 50), (2, 64, 36, 3, 50), (3, 48, 32, 2, 8),
                                                  (2, 40, 30, 5, 1)])
 def test_render_bit_exact_vs_oracle(product, oracle, cuda, level, w, h, spp, depth, layout):
@@ -210,7 +210,7 @@ def test_postproc_vs_oracle(product, oracle, cuda):
 
 
 # -------------------------------------------------------------- update / refit
-@pytest.mark.parametrize("layout", [1, 2, 3])
+@pytest.mark.parametrize("layout", [1, 2, 3, 4])
 def test_update_refit_after_transform_edit(product, oracle, cuda, layout):
     R, O = product, oracle
     sc, wd = rtow_pair(R, O, 2, layout=layout)
