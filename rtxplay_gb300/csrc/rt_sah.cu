@@ -6,17 +6,20 @@
 // every node of the level is binned (32 bins per axis over its centroid
 // bounds), the split of least surface-area cost is taken (Wald 2007) and the
 // node's records are partitioned stably; nodes of at most `cluster_max`
-// records become clusters.  Each cluster then gets a Karras 2012 hierarchy over 30-bit
-// Morton codes inside its own centroid bounds (keys cluster << 30 | code), and
-// the split nodes above the clusters are stitched into the spare node slot of
-// each cluster: a split whose left part ends at record position p lives in
-// slot p - 1, the last slot of the cluster ending there, which that cluster's
-// own n - 1 internal nodes leave free.
+// records become clusters.  Each cluster then gets a Karras 2012 hierarchy
+// over 30-bit Morton codes inside its own centroid bounds (keys cluster << 30
+// | code), and the split nodes above the clusters are stitched into the spare
+// node slot of each cluster: a split whose left part ends at record position
+// p lives in slot p - 1, the last slot of the cluster ending there, which that
+// cluster's own n - 1 internal nodes leave free.
 //
-// Everything is a function of the records alone (child allocation order does
-// not reach the result: slots follow from positions), so a rebuild gives the
-// same tree.  The host reads two counters per level; no kernel waits on
-// another block.
+// A level holds big nodes (more than kSahChunk records: binned by many
+// blocks, split by one warp, partitioned by many blocks with offsets from a
+// scan), block nodes (binned, split and partitioned by one block in one
+// launch) and warp nodes (the same by one warp, at most kWarpNode records).  Everything is a function of the records alone (allocation
+// order does not reach the result: slots follow from positions), so a rebuild
+// gives the same tree.  The host reads the counters once or twice per level;
+// no kernel waits on another block.
 #include <algorithm>
 #include <vector>
 
@@ -26,16 +29,20 @@ namespace rt {
 namespace {
 
 constexpr int kSahBins = 32;
-constexpr uint32_t kSahChunk = 2048;   // records per binning / partition block
+constexpr uint32_t kSahChunk = 2048;   // records per block; larger nodes are big nodes
 constexpr int kSahThreads = 256;
 constexpr int kSahMaxLevels = 64;      // deeper levels split at the median position
 constexpr int kBinWords = 7;           // count, box lo xyz, box hi xyz (orderable u32)
+constexpr uint32_t kBinTotal = 3 * kSahBins * kBinWords;
 
 // A record on its way down: box and record id.
 struct SahRec {
     float4 lo_id;   // box lo, record id (bits)
     float4 hi;      // box hi
 };
+
+constexpr int kBig = 0, kBlock = 1, kWarp = 2, kCluster = 3;
+constexpr uint32_t kWarpNode = 256;   // nodes of at most this many records: one warp each
 
 // A node of the current level.
 struct SahNode {
@@ -44,11 +51,12 @@ struct SahNode {
     uint32_t side;     // which child of the parent
     uint32_t seg;      // segment (scene) of the records
     uint32_t cb[6];    // centroid bounds, orderable u32 (lo xyz, hi xyz)
-    uint32_t chunk0;   // first chunk of the node in the level's chunk table
+    uint32_t chunk0;   // big nodes: first chunk in the level's chunk table
     int axis;          // chosen split: axis (-1: median position), bin, left count
     int bin;
     uint32_t nleft;
-    int child[2];      // >= 0: node of the next level; < 0: ~cluster
+    int child[2];      // index in the next level's list of its kind, or the cluster
+    int ckind[2];      // kBig, kBlock, kWarp or kCluster
 };
 
 struct SahCluster {
@@ -65,7 +73,20 @@ struct SahSplit {
 };
 
 struct SahCounters {
-    uint32_t nnext, ncl, nsplit, nchunks, err;
+    uint32_t nbig[2], nblock[2], nwarp[2];   // node lists, by level parity
+    uint32_t ncl, nsplit, nchunks, err;
+};
+
+// Where the children of a level's nodes go.
+struct SahOut {
+    SahNode* big;
+    SahNode* block;
+    SahNode* warp;
+    SahCluster* clusters;
+    SahSplit* splits;
+    SahCounters* ctr;
+    uint32_t nx;            // parity of the next level
+    uint32_t cluster_max;
 };
 
 __device__ __forceinline__ uint32_t sah_bin(float c, float lo, float scale) {
@@ -83,6 +104,13 @@ __device__ __forceinline__ void sah_frame(const uint32_t* cb, float lo[3], float
     }
 }
 
+__device__ __forceinline__ void empty_bins(uint32_t* b, uint32_t first, uint32_t step) {
+    for (uint32_t w = first; w < kBinTotal; w += step) {
+        const uint32_t k = w % kBinWords;
+        b[w] = (k >= 1 && k <= 3) ? 0xFFFFFFFFu : 0u;
+    }
+}
+
 __device__ __forceinline__ uint32_t node_of_chunk(const SahNode* __restrict__ nodes, uint32_t nact, uint32_t c) {
     uint32_t lo = 0, hi = nact;
     while (hi - lo > 1) {
@@ -90,6 +118,40 @@ __device__ __forceinline__ uint32_t node_of_chunk(const SahNode* __restrict__ no
         if (nodes[mid].chunk0 <= c) lo = mid; else hi = mid;
     }
     return lo;
+}
+
+__device__ __forceinline__ float3 rec_centroid(const SahRec& r) {
+    return mk(0.5f * (r.lo_id.x + r.hi.x), 0.5f * (r.lo_id.y + r.hi.y), 0.5f * (r.lo_id.z + r.hi.z));
+}
+
+// Adds one batch of records (one per lane, `valid`) to shared bins: lanes of
+// a warp in one bin reduce first, their leader updates shared memory.  Every
+// lane of the warp must call it.
+__device__ __forceinline__ void bin_records(uint32_t* sb, const SahRec& r, bool valid, const float lo[3],
+                                            const float scale[3], uint32_t lane) {
+    const float3 c = rec_centroid(r);
+    const float cc[3] = {c.x, c.y, c.z};
+    const uint32_t box[6] = {ford(r.lo_id.x), ford(r.lo_id.y), ford(r.lo_id.z), ford(r.hi.x), ford(r.hi.y),
+                             ford(r.hi.z)};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const uint32_t bin = valid ? sah_bin(cc[a], lo[a], scale[a]) : 0xFFFFu;
+        const uint32_t g = __match_any_sync(0xFFFFFFFFu, bin);
+        if (valid) {
+            const uint32_t m0 = __reduce_min_sync(g, box[0]);
+            const uint32_t m1 = __reduce_min_sync(g, box[1]);
+            const uint32_t m2 = __reduce_min_sync(g, box[2]);
+            const uint32_t x0 = __reduce_max_sync(g, box[3]);
+            const uint32_t x1 = __reduce_max_sync(g, box[4]);
+            const uint32_t x2 = __reduce_max_sync(g, box[5]);
+            if (lane == uint32_t(__ffs(g) - 1)) {
+                uint32_t* s = sb + (a * kSahBins + bin) * kBinWords;
+                atomicAdd(&s[0], uint32_t(__popc(g)));
+                atomicMin(&s[1], m0); atomicMin(&s[2], m1); atomicMin(&s[3], m2);
+                atomicMax(&s[4], x0); atomicMax(&s[5], x1); atomicMax(&s[6], x2);
+            }
+        }
+    }
 }
 
 __global__ void k_sah_records(const float4* __restrict__ prims, uint32_t n, SahRec* __restrict__ recs,
@@ -108,42 +170,34 @@ __global__ void k_sah_nchunks(const SahNode* __restrict__ nodes, uint32_t nact, 
     nch[i] = (nodes[i].count + kSahChunk - 1) / kSahChunk;
 }
 
-// chunk0 of every node from the scanned chunk counts; the total to the counters;
-// the node's bins emptied.
+// chunk0 of every big node from the scanned chunk counts, the total to the
+// counters, the nodes' bins emptied.
 __global__ void k_sah_prepare(SahNode* __restrict__ nodes, uint32_t nact, const uint32_t* __restrict__ chunk0,
                               SahCounters* __restrict__ ctr, uint32_t* __restrict__ bins) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < nact) {
         nodes[i].chunk0 = chunk0[i];
-        if (i == nact - 1) {
-            ctr->nchunks = chunk0[i] + (nodes[i].count + kSahChunk - 1) / kSahChunk;
-            ctr->nnext = 0;
-        }
+        if (i == nact - 1) ctr->nchunks = chunk0[i] + (nodes[i].count + kSahChunk - 1) / kSahChunk;
     }
-    const size_t words = size_t(nact) * 3 * kSahBins * kBinWords;
+    const size_t words = size_t(nact) * kBinTotal;
     for (size_t w = i; w < words; w += size_t(gridDim.x) * blockDim.x) {
         const uint32_t k = uint32_t(w % kBinWords);
         bins[w] = (k >= 1 && k <= 3) ? 0xFFFFFFFFu : 0u;
     }
 }
 
-// One block per chunk of a node: per-axis bins of the chunk in shared memory
-// (lanes of a warp that fall into one bin reduce first, their leader updates
-// shared memory), then added to the node's bins; the chunk's bin counts are
-// kept for the partition offsets.
+// Big nodes, one block per chunk: the chunk's bins in shared memory, added to
+// the node's bins; the chunk's bin counts kept for the partition offsets.
 __global__ void __launch_bounds__(kSahThreads)
     k_sah_bin(const SahRec* __restrict__ recs, const SahNode* __restrict__ nodes, uint32_t nact,
               uint32_t* __restrict__ bins, uint32_t* __restrict__ chunk_counts) {
-    __shared__ uint32_t sb[3 * kSahBins * kBinWords];
+    __shared__ uint32_t sb[kBinTotal];
     const uint32_t c = blockIdx.x;
     const uint32_t ni = node_of_chunk(nodes, nact, c);
     const SahNode& nd = nodes[ni];
     const uint32_t b = nd.start + (c - nd.chunk0) * kSahChunk;
     const uint32_t e = min(b + kSahChunk, nd.start + nd.count);
-    for (uint32_t w = threadIdx.x; w < 3 * kSahBins * kBinWords; w += blockDim.x) {
-        const uint32_t k = w % kBinWords;
-        sb[w] = (k >= 1 && k <= 3) ? 0xFFFFFFFFu : 0u;
-    }
+    empty_bins(sb, threadIdx.x, blockDim.x);
     float lo[3], scale[3];
     sah_frame(nd.cb, lo, scale);
     __syncthreads();
@@ -153,28 +207,7 @@ __global__ void __launch_bounds__(kSahThreads)
         const bool valid = p < e;
         SahRec r{};
         if (valid) r = recs[p];
-        const float cc[3] = {0.5f * (r.lo_id.x + r.hi.x), 0.5f * (r.lo_id.y + r.hi.y), 0.5f * (r.lo_id.z + r.hi.z)};
-        const uint32_t box[6] = {ford(r.lo_id.x), ford(r.lo_id.y), ford(r.lo_id.z),
-                                 ford(r.hi.x), ford(r.hi.y), ford(r.hi.z)};
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            const uint32_t bin = valid ? sah_bin(cc[a], lo[a], scale[a]) : 0xFFFFu;
-            const uint32_t g = __match_any_sync(0xFFFFFFFFu, bin);
-            if (valid) {
-                const uint32_t m0 = __reduce_min_sync(g, box[0]);
-                const uint32_t m1 = __reduce_min_sync(g, box[1]);
-                const uint32_t m2 = __reduce_min_sync(g, box[2]);
-                const uint32_t x0 = __reduce_max_sync(g, box[3]);
-                const uint32_t x1 = __reduce_max_sync(g, box[4]);
-                const uint32_t x2 = __reduce_max_sync(g, box[5]);
-                if (lane == uint32_t(__ffs(g) - 1)) {
-                    uint32_t* s = sb + (a * kSahBins + bin) * kBinWords;
-                    atomicAdd(&s[0], uint32_t(__popc(g)));
-                    atomicMin(&s[1], m0); atomicMin(&s[2], m1); atomicMin(&s[3], m2);
-                    atomicMax(&s[4], x0); atomicMax(&s[5], x1); atomicMax(&s[6], x2);
-                }
-            }
-        }
+        bin_records(sb, r, valid, lo, scale, lane);
     }
     __syncthreads();
     for (uint32_t t = threadIdx.x; t < 3 * kSahBins; t += blockDim.x) {
@@ -194,186 +227,197 @@ __device__ __forceinline__ float box_area(float3 lo, float3 hi) {
     return 2.f * (dx * dy + dy * dz + dz * dx);
 }
 
-// One warp per node: the least-cost split over 3 x 31 bin borders (ties: the
-// lower axis, then the lower border), the median position where no border
-// separates records or the level cap is reached; children allocated, the
-// split node recorded and linked to its parent, the chunks' left offsets.
+// Least-cost split of one node from its bins (3 axes x 32 bins x kBinWords,
+// one warp, lane = bin): the border of least surface-area cost over 3 x 31
+// borders (ties: the lower axis, then the lower border); axis stays -1 where
+// no border separates records.
+__device__ __forceinline__ void best_split(const uint32_t* nb, uint32_t lane, int& axis, int& bin, uint32_t& nleft) {
+    float best = INFINITY;
+    for (int a = 0; a < 3; ++a) {
+        const uint32_t* g = nb + (a * kSahBins + lane) * kBinWords;
+        uint32_t cnt = g[0];
+        float3 blo = cnt ? mk(fdeord(g[1]), fdeord(g[2]), fdeord(g[3])) : mk(INFINITY, INFINITY, INFINITY);
+        float3 bhi = cnt ? mk(fdeord(g[4]), fdeord(g[5]), fdeord(g[6])) : mk(-INFINITY, -INFINITY, -INFINITY);
+        // prefix (bins 0..lane) and suffix (bins lane..31)
+        uint32_t pc = cnt, sc = cnt;
+        float3 plo = blo, phi = bhi, slo = blo, shi = bhi;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t uc = __shfl_up_sync(0xFFFFFFFFu, pc, o);
+            const float3 ulo = mk(__shfl_up_sync(0xFFFFFFFFu, plo.x, o), __shfl_up_sync(0xFFFFFFFFu, plo.y, o),
+                                  __shfl_up_sync(0xFFFFFFFFu, plo.z, o));
+            const float3 uhi = mk(__shfl_up_sync(0xFFFFFFFFu, phi.x, o), __shfl_up_sync(0xFFFFFFFFu, phi.y, o),
+                                  __shfl_up_sync(0xFFFFFFFFu, phi.z, o));
+            const uint32_t dc = __shfl_down_sync(0xFFFFFFFFu, sc, o);
+            const float3 dlo = mk(__shfl_down_sync(0xFFFFFFFFu, slo.x, o),
+                                  __shfl_down_sync(0xFFFFFFFFu, slo.y, o),
+                                  __shfl_down_sync(0xFFFFFFFFu, slo.z, o));
+            const float3 dhi = mk(__shfl_down_sync(0xFFFFFFFFu, shi.x, o),
+                                  __shfl_down_sync(0xFFFFFFFFu, shi.y, o),
+                                  __shfl_down_sync(0xFFFFFFFFu, shi.z, o));
+            if (lane >= uint32_t(o)) {
+                pc += uc;
+                plo = mk(fminf(plo.x, ulo.x), fminf(plo.y, ulo.y), fminf(plo.z, ulo.z));
+                phi = mk(fmaxf(phi.x, uhi.x), fmaxf(phi.y, uhi.y), fmaxf(phi.z, uhi.z));
+            }
+            if (lane + o < 32) {
+                sc += dc;
+                slo = mk(fminf(slo.x, dlo.x), fminf(slo.y, dlo.y), fminf(slo.z, dlo.z));
+                shi = mk(fmaxf(shi.x, dhi.x), fmaxf(shi.y, dhi.y), fmaxf(shi.z, dhi.z));
+            }
+        }
+        // border lane + 1: left = bins 0..lane (own prefix), right = bins lane+1..31
+        const uint32_t rc = __shfl_down_sync(0xFFFFFFFFu, sc, 1);
+        const float3 rlo = mk(__shfl_down_sync(0xFFFFFFFFu, slo.x, 1), __shfl_down_sync(0xFFFFFFFFu, slo.y, 1),
+                              __shfl_down_sync(0xFFFFFFFFu, slo.z, 1));
+        const float3 rhi = mk(__shfl_down_sync(0xFFFFFFFFu, shi.x, 1), __shfl_down_sync(0xFFFFFFFFu, shi.y, 1),
+                              __shfl_down_sync(0xFFFFFFFFu, shi.z, 1));
+        float cost = INFINITY;
+        if (lane < 31 && pc > 0 && rc > 0) cost = box_area(plo, phi) * float(pc) + box_area(rlo, rhi) * float(rc);
+        // warp argmin (cost, lane)
+        float bc = cost;
+        uint32_t bl = lane;
+        for (int o = 16; o > 0; o >>= 1) {
+            const float oc = __shfl_xor_sync(0xFFFFFFFFu, bc, o);
+            const uint32_t ol = __shfl_xor_sync(0xFFFFFFFFu, bl, o);
+            if (oc < bc || (oc == bc && ol < bl)) { bc = oc; bl = ol; }
+        }
+        const uint32_t bpc = __shfl_sync(0xFFFFFFFFu, pc, bl);
+        if (bc < best) {
+            best = bc;
+            axis = a;
+            bin = int(bl) + 1;
+            nleft = bpc;
+        }
+    }
+}
+
+// Records the split of node nd (left part nleft records) and allocates its
+// children: nodes of the next level (big, block or warp node by size) or
+// clusters, each with empty centroid bounds; links the split to its parent.
+// One thread.
+__device__ void emit_split(SahNode& nd, uint32_t nleft, const SahOut& out) {
+    const uint32_t sid = atomicAdd(&out.ctr->nsplit, 1u);
+    SahSplit sp;
+    sp.start = nd.start;
+    sp.split = nd.start + nleft;
+    sp.end = nd.start + nd.count;
+    sp.child[0] = sp.child[1] = -1;
+    sp.parent = nd.parent;
+    sp.seg = nd.seg;
+    for (int k = 0; k < 2; ++k) {
+        const uint32_t cs = k ? nd.start + nleft : nd.start;
+        const uint32_t cn = k ? nd.count - nleft : nleft;
+        if (cn > out.cluster_max) {
+            const int kind = cn > kSahChunk ? kBig : cn > kWarpNode ? kBlock : kWarp;
+            uint32_t* cnt = kind == kBig ? &out.ctr->nbig[out.nx] : kind == kBlock ? &out.ctr->nblock[out.nx]
+                                                                                   : &out.ctr->nwarp[out.nx];
+            const uint32_t id = atomicAdd(cnt, 1u);
+            SahNode ch;
+            ch.start = cs;
+            ch.count = cn;
+            ch.parent = int(sid);
+            ch.side = uint32_t(k);
+            ch.seg = nd.seg;
+            ch.cb[0] = ch.cb[1] = ch.cb[2] = 0xFFFFFFFFu;
+            ch.cb[3] = ch.cb[4] = ch.cb[5] = 0u;
+            ch.chunk0 = 0;
+            ch.axis = -1;
+            ch.bin = 0;
+            ch.nleft = 0;
+            ch.child[0] = ch.child[1] = 0;
+            ch.ckind[0] = ch.ckind[1] = kCluster;
+            (kind == kBig ? out.big : kind == kBlock ? out.block : out.warp)[id] = ch;
+            nd.child[k] = int(id);
+            nd.ckind[k] = kind;
+        } else {
+            const uint32_t id = atomicAdd(&out.ctr->ncl, 1u);
+            SahCluster cl;
+            cl.start = cs;
+            cl.count = cn;
+            cl.cb[0] = cl.cb[1] = cl.cb[2] = 0xFFFFFFFFu;
+            cl.cb[3] = cl.cb[4] = cl.cb[5] = 0u;
+            out.clusters[id] = cl;
+            nd.child[k] = int(id);
+            nd.ckind[k] = kCluster;
+        }
+    }
+    out.splits[sid] = sp;
+    if (nd.parent >= 0) out.splits[nd.parent].child[nd.side] = int(sid);
+    nd.nleft = nleft;
+}
+
+__device__ __forceinline__ uint32_t* child_cb(const SahNode& nd, int k, const SahOut& out) {
+    const int id = nd.child[k];
+    const int kind = nd.ckind[k];
+    return kind == kBig ? out.big[id].cb : kind == kBlock ? out.block[id].cb : kind == kWarp ? out.warp[id].cb
+                                                                                           : out.clusters[id].cb;
+}
+
+// Big nodes, one warp each: the split (best_split, or the median position
+// where no border separates records or the level cap is reached), children
+// allocated.
 __global__ void k_sah_split(SahNode* __restrict__ nodes, uint32_t nact, const uint32_t* __restrict__ bins,
-                            const uint32_t* __restrict__ chunk_counts, uint32_t* __restrict__ chunk_left,
-                            SahNode* __restrict__ next, SahCluster* __restrict__ clusters,
-                            SahSplit* __restrict__ splits, SahCounters* __restrict__ ctr, uint32_t cluster_max,
-                            int median_only) {
+                            SahOut out, int median_only) {
     const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t lane = threadIdx.x & 31u;
     if (w >= nact) return;
     SahNode nd = nodes[w];
-    float best = INFINITY;
     int axis = -1, bin = 0;
     uint32_t nleft = nd.count / 2;
-    if (!median_only) {
-        for (int a = 0; a < 3; ++a) {
-            const uint32_t* g = bins + (size_t(w) * 3 * kSahBins + a * kSahBins + lane) * kBinWords;
-            uint32_t cnt = g[0];
-            float3 blo = cnt ? mk(fdeord(g[1]), fdeord(g[2]), fdeord(g[3])) : mk(INFINITY, INFINITY, INFINITY);
-            float3 bhi = cnt ? mk(fdeord(g[4]), fdeord(g[5]), fdeord(g[6])) : mk(-INFINITY, -INFINITY, -INFINITY);
-            // prefix (bins 0..lane) and suffix (bins lane..31)
-            uint32_t pc = cnt, sc = cnt;
-            float3 plo = blo, phi = bhi, slo = blo, shi = bhi;
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t uc = __shfl_up_sync(0xFFFFFFFFu, pc, o);
-                const float3 ulo = mk(__shfl_up_sync(0xFFFFFFFFu, plo.x, o), __shfl_up_sync(0xFFFFFFFFu, plo.y, o),
-                                      __shfl_up_sync(0xFFFFFFFFu, plo.z, o));
-                const float3 uhi = mk(__shfl_up_sync(0xFFFFFFFFu, phi.x, o), __shfl_up_sync(0xFFFFFFFFu, phi.y, o),
-                                      __shfl_up_sync(0xFFFFFFFFu, phi.z, o));
-                const uint32_t dc = __shfl_down_sync(0xFFFFFFFFu, sc, o);
-                const float3 dlo = mk(__shfl_down_sync(0xFFFFFFFFu, slo.x, o),
-                                      __shfl_down_sync(0xFFFFFFFFu, slo.y, o),
-                                      __shfl_down_sync(0xFFFFFFFFu, slo.z, o));
-                const float3 dhi = mk(__shfl_down_sync(0xFFFFFFFFu, shi.x, o),
-                                      __shfl_down_sync(0xFFFFFFFFu, shi.y, o),
-                                      __shfl_down_sync(0xFFFFFFFFu, shi.z, o));
-                if (lane >= uint32_t(o)) {
-                    pc += uc;
-                    plo = mk(fminf(plo.x, ulo.x), fminf(plo.y, ulo.y), fminf(plo.z, ulo.z));
-                    phi = mk(fmaxf(phi.x, uhi.x), fmaxf(phi.y, uhi.y), fmaxf(phi.z, uhi.z));
-                }
-                if (lane + o < 32) {
-                    sc += dc;
-                    slo = mk(fminf(slo.x, dlo.x), fminf(slo.y, dlo.y), fminf(slo.z, dlo.z));
-                    shi = mk(fmaxf(shi.x, dhi.x), fmaxf(shi.y, dhi.y), fmaxf(shi.z, dhi.z));
-                }
-            }
-            // border lane + 1: left = bins 0..lane (own prefix), right = bins lane+1..31
-            const uint32_t rc = __shfl_down_sync(0xFFFFFFFFu, sc, 1);
-            const float3 rlo = mk(__shfl_down_sync(0xFFFFFFFFu, slo.x, 1), __shfl_down_sync(0xFFFFFFFFu, slo.y, 1),
-                                  __shfl_down_sync(0xFFFFFFFFu, slo.z, 1));
-            const float3 rhi = mk(__shfl_down_sync(0xFFFFFFFFu, shi.x, 1), __shfl_down_sync(0xFFFFFFFFu, shi.y, 1),
-                                  __shfl_down_sync(0xFFFFFFFFu, shi.z, 1));
-            float cost = INFINITY;
-            if (lane < 31 && pc > 0 && rc > 0) cost = box_area(plo, phi) * float(pc) + box_area(rlo, rhi) * float(rc);
-            // warp argmin (cost, lane)
-            float bc = cost;
-            uint32_t bl = lane;
-            for (int o = 16; o > 0; o >>= 1) {
-                const float oc = __shfl_xor_sync(0xFFFFFFFFu, bc, o);
-                const uint32_t ol = __shfl_xor_sync(0xFFFFFFFFu, bl, o);
-                if (oc < bc || (oc == bc && ol < bl)) { bc = oc; bl = ol; }
-            }
-            const uint32_t bpc = __shfl_sync(0xFFFFFFFFu, pc, bl);
-            if (bc < best) {
-                best = bc;
-                axis = a;
-                bin = int(bl) + 1;
-                nleft = bpc;
-            }
-        }
-    }
-    const uint32_t nch = (nd.count + kSahChunk - 1) / kSahChunk;
+    if (!median_only) best_split(bins + size_t(w) * kBinTotal, lane, axis, bin, nleft);
     if (lane == 0) {
-        const uint32_t sid = atomicAdd(&ctr->nsplit, 1u);
-        SahSplit sp;
-        sp.start = nd.start;
-        sp.split = nd.start + nleft;
-        sp.end = nd.start + nd.count;
-        sp.child[0] = sp.child[1] = -1;
-        sp.parent = nd.parent;
-        sp.seg = nd.seg;
-        for (int k = 0; k < 2; ++k) {
-            const uint32_t cs = k ? nd.start + nleft : nd.start;
-            const uint32_t cn = k ? nd.count - nleft : nleft;
-            if (cn > cluster_max) {
-                const uint32_t id = atomicAdd(&ctr->nnext, 1u);
-                SahNode ch;
-                ch.start = cs;
-                ch.count = cn;
-                ch.parent = int(sid);
-                ch.side = uint32_t(k);
-                ch.seg = nd.seg;
-                ch.cb[0] = ch.cb[1] = ch.cb[2] = 0xFFFFFFFFu;
-                ch.cb[3] = ch.cb[4] = ch.cb[5] = 0u;
-                ch.chunk0 = 0;
-                ch.axis = -1;
-                ch.bin = 0;
-                ch.nleft = 0;
-                ch.child[0] = ch.child[1] = 0;
-                next[id] = ch;
-                nd.child[k] = int(id);
-            } else {
-                const uint32_t id = atomicAdd(&ctr->ncl, 1u);
-                SahCluster cl;
-                cl.start = cs;
-                cl.count = cn;
-                cl.cb[0] = cl.cb[1] = cl.cb[2] = 0xFFFFFFFFu;
-                cl.cb[3] = cl.cb[4] = cl.cb[5] = 0u;
-                clusters[id] = cl;
-                nd.child[k] = ~int(id);
-            }
-        }
-        splits[sid] = sp;
-        if (nd.parent >= 0) splits[nd.parent].child[nd.side] = int(sid);
+        emit_split(nd, nleft, out);
         nd.axis = axis;
         nd.bin = bin;
-        nd.nleft = nleft;
         nodes[w] = nd;
-    }
-    // left records before each chunk of the node (stable partition offsets)
-    uint32_t run = 0;
-    for (uint32_t c0 = 0; c0 < nch; c0 += 32) {
-        const uint32_t ci = c0 + lane;
-        uint32_t l = 0;
-        if (ci < nch) {
-            if (axis >= 0) {
-                const uint32_t* cc = chunk_counts + size_t(nd.chunk0 + ci) * 3 * kSahBins + axis * kSahBins;
-                for (int k = 0; k < bin; ++k) l += cc[k];
-            } else {
-                const uint32_t first = ci * kSahChunk;
-                const uint32_t len = min(kSahChunk, nd.count - first);
-                l = nleft > first ? min(nleft - first, len) : 0u;
-            }
-        }
-        uint32_t x = l;   // inclusive warp scan
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
-            if (lane >= uint32_t(o)) x += y;
-        }
-        if (ci < nch) chunk_left[nd.chunk0 + ci] = run + x - l;
-        run += __shfl_sync(0xFFFFFFFFu, x, 31);
     }
 }
 
-// One block per chunk: stable partition of the chunk's records into the two
-// children (block-wide ranks from warp ballots), records of a cluster child
-// also to their final position in out_ids; centroid bounds of both children
-// accumulated.
-__global__ void __launch_bounds__(kSahThreads)
-    k_sah_partition(const SahRec* __restrict__ recs, SahRec* __restrict__ out, const SahNode* __restrict__ nodes,
-                    uint32_t nact, const uint32_t* __restrict__ chunk_left, SahNode* __restrict__ next,
-                    SahCluster* __restrict__ clusters, uint32_t* __restrict__ out_ids, SahCounters* __restrict__ ctr) {
-    __shared__ uint32_t s_warp[kSahThreads / 32];
-    __shared__ uint32_t s_cb[12];
-    const uint32_t c = blockIdx.x;
-    const uint32_t ni = node_of_chunk(nodes, nact, c);
-    const SahNode& nd = nodes[ni];
-    const uint32_t b = nd.start + (c - nd.chunk0) * kSahChunk;
-    const uint32_t e = min(b + kSahChunk, nd.start + nd.count);
-    const uint32_t left_base = chunk_left[c];
-    const uint32_t before = b - nd.start;   // records of the node before this chunk
+// Left records of every chunk of the big nodes (one thread per chunk); an
+// exclusive scan over all chunks minus its value at the node's first chunk
+// gives the left records before a chunk inside its node.
+__global__ void k_sah_chunk_left(const SahNode* __restrict__ nodes, uint32_t nact, uint32_t nchunks,
+                                 const uint32_t* __restrict__ chunk_counts, uint32_t* __restrict__ chunk_left) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nchunks) return;
+    const SahNode& nd = nodes[node_of_chunk(nodes, nact, c)];
+    uint32_t l = 0;
+    if (nd.axis >= 0) {
+        const uint32_t* cc = chunk_counts + size_t(c) * 3 * kSahBins + nd.axis * kSahBins;
+        for (int k = 0; k < nd.bin; ++k) l += cc[k];
+    } else {
+        const uint32_t first = (c - nd.chunk0) * kSahChunk;
+        const uint32_t len = min(kSahChunk, nd.count - first);
+        l = nd.nleft > first ? min(nd.nleft - first, len) : 0u;
+    }
+    chunk_left[c] = l;
+}
+
+// Stable partition of records [b, e) of node nd (a chunk, or a whole
+// block node) into its children: block-wide ranks from warp ballots;
+// `left_base` left records of the node precede b.  Records go to `out_rec`
+// (child node) or, as ids, to out_ids (cluster); the children's centroid
+// bounds are reduced into s_cb (12 orderable u32, lo xyz hi xyz per child).
+__device__ __forceinline__ void partition_records(const SahRec* __restrict__ recs, SahRec* __restrict__ out_rec,
+                                                  uint32_t* __restrict__ out_ids, const SahNode& nd, uint32_t b,
+                                                  uint32_t e, uint32_t left_base, const float lo[3],
+                                                  const float scale[3], uint32_t* s_warp, uint32_t* s_cb,
+                                                  SahCounters* ctr) {
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t before = b - nd.start;   // records of the node before b
     const int axis = nd.axis;
     const uint32_t bin = uint32_t(nd.bin), nleft = nd.nleft;
-    float lo[3], scale[3];
-    sah_frame(nd.cb, lo, scale);
-    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    if (threadIdx.x < 12) s_cb[threadIdx.x] = (threadIdx.x % 6) < 3 ? 0xFFFFFFFFu : 0u;
-    uint32_t acc[12];   // child 0 lo xyz, hi xyz, child 1 lo xyz, hi xyz
+    uint32_t acc[12];
 #pragma unroll
     for (int k = 0; k < 12; ++k) acc[k] = (k % 6) < 3 ? 0xFFFFFFFFu : 0u;
-    uint32_t run = 0;   // left records of this chunk in earlier rounds
+    uint32_t run = 0;   // left records of [b, e) in earlier rounds
     for (uint32_t base = b; base < e; base += blockDim.x) {
         const uint32_t p = base + threadIdx.x;
         const bool valid = p < e;
         SahRec r{};
         if (valid) r = recs[p];
-        const float cc[3] = {0.5f * (r.lo_id.x + r.hi.x), 0.5f * (r.lo_id.y + r.hi.y), 0.5f * (r.lo_id.z + r.hi.z)};
+        const float3 c3 = rec_centroid(r);
+        const float cc[3] = {c3.x, c3.y, c3.z};
         bool left = false;
         if (valid) left = axis >= 0 ? sah_bin(cc[axis], lo[axis], scale[axis]) < bin : (p - nd.start) < nleft;
         const uint32_t ballot = __ballot_sync(0xFFFFFFFFu, left);
@@ -386,17 +430,16 @@ __global__ void __launch_bounds__(kSahThreads)
             total += v;
         }
         if (valid) {
-            const uint32_t lbefore = run + woff + __popc(ballot & ((1u << lane) - 1u));   // lefts before p in chunk
-            const uint32_t pos_in_chunk = p - b;
+            const uint32_t lbefore = run + woff + __popc(ballot & ((1u << lane) - 1u));   // lefts before p in [b, e)
             const uint32_t dest = left ? nd.start + left_base + lbefore
-                                       : nd.start + nleft + (before - left_base) + (pos_in_chunk - lbefore);
-            const int ch = nd.child[left ? 0 : 1];
-            // the binning and this pass bin identically, so dest stays inside the
+                                       : nd.start + nleft + (before - left_base) + (p - b - lbefore);
+            const int kind = nd.ckind[left ? 0 : 1];
+            // binning and partition bin identically, so dest stays inside the
             // child; the check only guards the writes
             const uint32_t cb = left ? nd.start : nd.start + nleft;
             const uint32_t ce = left ? nd.start + nleft : nd.start + nd.count;
             if (dest < cb || dest >= ce) atomicOr(&ctr->err, 1u);
-            else if (ch >= 0) out[dest] = r;
+            else if (kind != kCluster) out_rec[dest] = r;
             else out_ids[dest] = __float_as_uint(r.lo_id.w);
             const int o = left ? 0 : 6;
 #pragma unroll
@@ -416,16 +459,157 @@ __global__ void __launch_bounds__(kSahThreads)
             if ((k % 6) < 3) atomicMin(&s_cb[k], v); else atomicMax(&s_cb[k], v);
         }
     }
+}
+
+// Big nodes, one block per chunk: partition with offsets from the scan;
+// children's centroid bounds by global atomics (many chunks per node).
+__global__ void __launch_bounds__(kSahThreads)
+    k_sah_partition(const SahRec* __restrict__ recs, SahRec* __restrict__ out_rec, const SahNode* __restrict__ nodes,
+                    uint32_t nact, const uint32_t* __restrict__ chunk_scan, uint32_t* __restrict__ out_ids, SahOut out) {
+    __shared__ uint32_t s_warp[kSahThreads / 32];
+    __shared__ uint32_t s_cb[12];
+    const uint32_t c = blockIdx.x;
+    const uint32_t ni = node_of_chunk(nodes, nact, c);
+    const SahNode& nd = nodes[ni];
+    const uint32_t b = nd.start + (c - nd.chunk0) * kSahChunk;
+    const uint32_t e = min(b + kSahChunk, nd.start + nd.count);
+    float lo[3], scale[3];
+    sah_frame(nd.cb, lo, scale);
+    if (threadIdx.x < 12) s_cb[threadIdx.x] = (threadIdx.x % 6) < 3 ? 0xFFFFFFFFu : 0u;
+    __syncthreads();
+    partition_records(recs, out_rec, out_ids, nd, b, e, chunk_scan[c] - chunk_scan[nd.chunk0], lo, scale, s_warp,
+                      s_cb, out.ctr);
     __syncthreads();
     if (threadIdx.x < 12) {
         const uint32_t k = threadIdx.x;
-        const int ch = nd.child[k / 6];
         const uint32_t v = s_cb[k];
-        const bool empty = (k % 6) < 3 ? v == 0xFFFFFFFFu : v == 0u;
-        if (!empty) {
-            uint32_t* dst = ch >= 0 ? next[ch].cb : clusters[~ch].cb;
+        if ((k % 6) < 3 ? v != 0xFFFFFFFFu : v != 0u) {
+            uint32_t* dst = child_cb(nd, int(k / 6), out);
             if ((k % 6) < 3) atomicMin(&dst[k % 6], v); else atomicMax(&dst[k % 6], v);
         }
+    }
+}
+
+// Block nodes (kWarpNode < records <= kSahChunk), one block each: bins in
+// shared memory, the split by warp 0, the partition; the children's centroid
+// bounds are final when the block ends (no other block touches them).
+__global__ void __launch_bounds__(kSahThreads)
+    k_sah_node(const SahRec* __restrict__ recs, SahRec* __restrict__ out_rec, const SahNode* __restrict__ nodes,
+               uint32_t* __restrict__ out_ids, SahOut out, int median_only) {
+    __shared__ uint32_t sb[kBinTotal];
+    __shared__ uint32_t s_warp[kSahThreads / 32];
+    __shared__ uint32_t s_cb[12];
+    __shared__ SahNode s_nd;
+    SahNode nd = nodes[blockIdx.x];
+    const uint32_t b = nd.start, e = nd.start + nd.count;
+    const uint32_t lane = threadIdx.x & 31u;
+    float lo[3], scale[3];
+    sah_frame(nd.cb, lo, scale);
+    if (!median_only) {
+        empty_bins(sb, threadIdx.x, blockDim.x);
+        __syncthreads();
+        for (uint32_t base = b; base < e; base += blockDim.x) {
+            const uint32_t p = base + threadIdx.x;
+            const bool valid = p < e;
+            SahRec r{};
+            if (valid) r = recs[p];
+            bin_records(sb, r, valid, lo, scale, lane);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x < 32) {
+        int axis = -1, bin = 0;
+        uint32_t nleft = nd.count / 2;
+        if (!median_only) best_split(sb, lane, axis, bin, nleft);
+        if (lane == 0) {
+            emit_split(nd, nleft, out);
+            nd.axis = axis;
+            nd.bin = bin;
+            s_nd = nd;
+        }
+    }
+    if (threadIdx.x < 12) s_cb[threadIdx.x] = (threadIdx.x % 6) < 3 ? 0xFFFFFFFFu : 0u;
+    __syncthreads();
+    nd = s_nd;
+    partition_records(recs, out_rec, out_ids, nd, b, e, 0u, lo, scale, s_warp, s_cb, out.ctr);
+    __syncthreads();
+    if (threadIdx.x < 12) {
+        const uint32_t k = threadIdx.x;
+        child_cb(nd, int(k / 6), out)[k % 6] = s_cb[k];
+    }
+}
+
+// Warp nodes (cluster_max < records <= kWarpNode), one warp each: the same
+// steps as a block node with warp-private bins and warp ballots.
+__global__ void __launch_bounds__(kSahThreads)
+    k_sah_warp(const SahRec* __restrict__ recs, SahRec* __restrict__ out_rec, const SahNode* __restrict__ nodes,
+               uint32_t nw, uint32_t* __restrict__ out_ids, SahOut out, int median_only) {
+    __shared__ uint32_t sbins[kSahThreads / 32][kBinTotal];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t w = blockIdx.x * (kSahThreads / 32) + warp;
+    if (w >= nw) return;   // whole warps
+    uint32_t* sb = sbins[warp];
+    SahNode nd = nodes[w];
+    const uint32_t b = nd.start, e = nd.start + nd.count;
+    float lo[3], scale[3];
+    sah_frame(nd.cb, lo, scale);
+    int axis = -1, bin = 0;
+    uint32_t nleft = nd.count / 2;
+    if (!median_only) {
+        empty_bins(sb, lane, 32);
+        __syncwarp();
+        for (uint32_t base = b; base < e; base += 32) {
+            const uint32_t p = base + lane;
+            const bool valid = p < e;
+            SahRec r{};
+            if (valid) r = recs[p];
+            bin_records(sb, r, valid, lo, scale, lane);
+        }
+        __syncwarp();
+        best_split(sb, lane, axis, bin, nleft);
+    }
+    if (lane == 0) emit_split(nd, nleft, out);
+    nd.child[0] = __shfl_sync(0xFFFFFFFFu, nd.child[0], 0);
+    nd.child[1] = __shfl_sync(0xFFFFFFFFu, nd.child[1], 0);
+    nd.ckind[0] = __shfl_sync(0xFFFFFFFFu, nd.ckind[0], 0);
+    nd.ckind[1] = __shfl_sync(0xFFFFFFFFu, nd.ckind[1], 0);
+    uint32_t acc[12];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) acc[k] = (k % 6) < 3 ? 0xFFFFFFFFu : 0u;
+    uint32_t run = 0;
+    for (uint32_t base = b; base < e; base += 32) {
+        const uint32_t p = base + lane;
+        const bool valid = p < e;
+        SahRec r{};
+        if (valid) r = recs[p];
+        const float3 c3 = rec_centroid(r);
+        const float cc[3] = {c3.x, c3.y, c3.z};
+        bool left = false;
+        if (valid) left = axis >= 0 ? sah_bin(cc[axis], lo[axis], scale[axis]) < uint32_t(bin) : (p - b) < nleft;
+        const uint32_t ballot = __ballot_sync(0xFFFFFFFFu, left);
+        if (valid) {
+            const uint32_t lb = run + __popc(ballot & ((1u << lane) - 1u));
+            const uint32_t dest = left ? b + lb : b + nleft + (p - b - lb);
+            const int kind = nd.ckind[left ? 0 : 1];
+            const uint32_t cb = left ? b : b + nleft;
+            const uint32_t ce = left ? b + nleft : e;
+            if (dest < cb || dest >= ce) atomicOr(&out.ctr->err, 1u);
+            else if (kind != kCluster) out_rec[dest] = r;
+            else out_ids[dest] = __float_as_uint(r.lo_id.w);
+            const int o = left ? 0 : 6;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                const uint32_t v = ford(cc[a]);
+                acc[o + a] = min(acc[o + a], v);
+                acc[o + 3 + a] = max(acc[o + 3 + a], v);
+            }
+        }
+        run += __popc(ballot);
+    }
+#pragma unroll
+    for (int k = 0; k < 12; ++k) {
+        const uint32_t v = (k % 6) < 3 ? __reduce_min_sync(0xFFFFFFFFu, acc[k]) : __reduce_max_sync(0xFFFFFFFFu, acc[k]);
+        if (lane == uint32_t(k)) child_cb(nd, k / 6, out)[k % 6] = v;
     }
 }
 
@@ -517,7 +701,7 @@ void build_sah_topology(Lbvh& L, uint32_t cluster_max, cudaStream_t s) {
     std::vector<uint32_t> sb(6 * size_t(ns));
     RT_CUDA(cudaMemcpyAsync(sb.data(), L.bounds.p, sb.size() * 4, cudaMemcpyDeviceToHost, s));
     RT_CUDA(cudaStreamSynchronize(s));
-    std::vector<SahNode> seed;
+    std::vector<SahNode> seed_big, seed_block, seed_warp;
     std::vector<SahCluster> seed_cl;
     L.roots.assign(ns, -1);
     for (uint32_t g = 0; g < ns; ++g) {
@@ -530,7 +714,8 @@ void build_sah_topology(Lbvh& L, uint32_t cluster_max, cudaStream_t s) {
             nd.parent = -1;
             nd.seg = g;
             for (int k = 0; k < 6; ++k) nd.cb[k] = sb[6 * g + k];
-            seed.push_back(nd);
+            nd.ckind[0] = nd.ckind[1] = kCluster;
+            (sg.prim_count > kSahChunk ? seed_big : sg.prim_count > kWarpNode ? seed_block : seed_warp).push_back(nd);
         } else {
             SahCluster cl{};
             cl.start = sg.prim_begin;
@@ -540,17 +725,18 @@ void build_sah_topology(Lbvh& L, uint32_t cluster_max, cudaStream_t s) {
             L.roots[g] = int(sg.prim_begin);   // a single cluster: its Karras root (or its only record)
         }
     }
-    // scratch: records x2, node lists x2, bins, chunk tables, clusters, splits
-    // per level at most n / (cluster_max + 1) nodes are split (disjoint
-    // ranges above the cluster size); over all levels there are fewer splits
-    // and clusters than records
+    // scratch: records x2, big, block and warp node lists x2, bins, chunk
+    // tables, clusters, splits.  A level holds at most n / (cluster_max + 1)
+    // nodes (disjoint ranges above the cluster size) and n / kSahChunk big
+    // ones; over all levels there are fewer splits and clusters than records.
     const size_t max_nodes = size_t(n) / (cluster_max + 1) + ns + 1;
-    const size_t max_chunks = size_t(n) / kSahChunk + max_nodes + 1;
+    const size_t max_big = size_t(n) / kSahChunk + ns + 1;
+    const size_t max_chunks = size_t(n) / kSahChunk + max_big + 1;
     const size_t max_cl = size_t(n) + 1;
     const size_t max_split = size_t(n) + 1;
     SahRec* rec[2];
-    SahNode* nodes[2];
-    uint32_t *bins, *chunk_counts, *nch, *chunk0, *chunk_left, *out_ids, *ckeys, *cvals, *tcb;
+    SahNode *big[2], *block[2], *warp[2];
+    uint32_t *bins, *chunk_counts, *nch, *chunk0, *chunk_left, *chunk_scan, *out_ids, *ckeys, *cvals, *tcb;
     SahCluster* clusters;
     SahSplit* splits;
     SegDev* tsegs;
@@ -560,13 +746,18 @@ void build_sah_topology(Lbvh& L, uint32_t cluster_max, cudaStream_t s) {
         char* const p0 = p;
         rec[0] = carve<SahRec>(p, n);
         rec[1] = carve<SahRec>(p, n);
-        nodes[0] = carve<SahNode>(p, max_nodes);
-        nodes[1] = carve<SahNode>(p, max_nodes);
-        bins = carve<uint32_t>(p, max_nodes * 3 * kSahBins * kBinWords);
+        big[0] = carve<SahNode>(p, max_big);
+        big[1] = carve<SahNode>(p, max_big);
+        block[0] = carve<SahNode>(p, max_nodes);
+        block[1] = carve<SahNode>(p, max_nodes);
+        warp[0] = carve<SahNode>(p, max_nodes);
+        warp[1] = carve<SahNode>(p, max_nodes);
+        bins = carve<uint32_t>(p, max_big * kBinTotal);
         chunk_counts = carve<uint32_t>(p, max_chunks * 3 * kSahBins);
         nch = carve<uint32_t>(p, max_chunks);
         chunk0 = carve<uint32_t>(p, max_chunks);
         chunk_left = carve<uint32_t>(p, max_chunks);
+        chunk_scan = carve<uint32_t>(p, max_chunks);
         clusters = carve<SahCluster>(p, max_cl);
         splits = carve<SahSplit>(p, max_split);
         out_ids = carve<uint32_t>(p, n);
@@ -581,10 +772,20 @@ void build_sah_topology(Lbvh& L, uint32_t cluster_max, cudaStream_t s) {
     L.sah_tmp.reserve(layout(reinterpret_cast<char*>(uintptr_t(256))));
     layout(L.sah_tmp.as<char>());
 
-    SahCounters c0{0u, uint32_t(seed_cl.size()), 0u, 0u, 0u};
+    SahCounters c0{};
+    c0.nbig[0] = uint32_t(seed_big.size());
+    c0.nblock[0] = uint32_t(seed_block.size());
+    c0.nwarp[0] = uint32_t(seed_warp.size());
+    c0.ncl = uint32_t(seed_cl.size());
     RT_CUDA(cudaMemcpyAsync(ctr, &c0, sizeof c0, cudaMemcpyHostToDevice, s));
-    if (!seed.empty())
-        RT_CUDA(cudaMemcpyAsync(nodes[0], seed.data(), seed.size() * sizeof(SahNode), cudaMemcpyHostToDevice, s));
+    if (!seed_big.empty())
+        RT_CUDA(cudaMemcpyAsync(big[0], seed_big.data(), seed_big.size() * sizeof(SahNode), cudaMemcpyHostToDevice, s));
+    if (!seed_block.empty())
+        RT_CUDA(cudaMemcpyAsync(block[0], seed_block.data(), seed_block.size() * sizeof(SahNode),
+                                cudaMemcpyHostToDevice, s));
+    if (!seed_warp.empty())
+        RT_CUDA(cudaMemcpyAsync(warp[0], seed_warp.data(), seed_warp.size() * sizeof(SahNode), cudaMemcpyHostToDevice,
+                                s));
     if (!seed_cl.empty())
         RT_CUDA(cudaMemcpyAsync(clusters, seed_cl.data(), seed_cl.size() * sizeof(SahCluster), cudaMemcpyHostToDevice,
                                 s));
@@ -592,40 +793,64 @@ void build_sah_topology(Lbvh& L, uint32_t cluster_max, cudaStream_t s) {
     k_sah_records<<<(n + kSahThreads - 1) / kSahThreads, kSahThreads, 0, s>>>(L.prims_flat.as<float4>(), n, rec[0],
                                                                                out_ids);
     RT_CHECK_LAUNCH();
-    uint32_t nact = uint32_t(seed.size());
+    uint32_t nb = c0.nbig[0], nbl = c0.nblock[0], nw = c0.nwarp[0];
     int cur = 0, level = 0;
     SahCounters hc{};
-    for (; nact > 0; ++level) {
-        RT_REQUIRE(nact <= max_nodes, "internal: SAH level overflow");
-        k_sah_nchunks<<<(nact + kSahThreads - 1) / kSahThreads, kSahThreads, 0, s>>>(nodes[cur], nact, nch);
-        RT_CHECK_LAUNCH();
-        scan_exclusive_u32(nch, chunk0, nact, L.sort_tmp, s);
-        const uint32_t prep_blocks = std::min<uint32_t>(
-            4096u, uint32_t((size_t(nact) * 3 * kSahBins * kBinWords + kSahThreads - 1) / kSahThreads));
-        k_sah_prepare<<<std::max(prep_blocks, (nact + kSahThreads - 1) / kSahThreads), kSahThreads, 0, s>>>(
-            nodes[cur], nact, chunk0, ctr, bins);
-        RT_CHECK_LAUNCH();
-        RT_CUDA(cudaMemcpyAsync(&hc, ctr, sizeof hc, cudaMemcpyDeviceToHost, s));
-        RT_CUDA(cudaStreamSynchronize(s));
-        const uint32_t nchunks = hc.nchunks;
-        RT_REQUIRE(nchunks <= max_chunks, "internal: SAH chunk overflow");
-        k_sah_bin<<<nchunks, kSahThreads, 0, s>>>(rec[cur], nodes[cur], nact, bins, chunk_counts);
-        RT_CHECK_LAUNCH();
-        k_sah_split<<<(nact * 32 + 127) / 128, 128, 0, s>>>(nodes[cur], nact, bins, chunk_counts, chunk_left,
-                                                            nodes[cur ^ 1], clusters, splits, ctr, cluster_max,
-                                                            level >= kSahMaxLevels ? 1 : 0);
-        RT_CHECK_LAUNCH();
-        k_sah_partition<<<nchunks, kSahThreads, 0, s>>>(rec[cur], rec[cur ^ 1], nodes[cur], nact, chunk_left,
-                                                        nodes[cur ^ 1], clusters, out_ids, ctr);
-        RT_CHECK_LAUNCH();
+    for (; nb + nbl + nw > 0; ++level) {
+        RT_REQUIRE(nb <= max_big && nbl <= max_nodes && nw <= max_nodes, "internal: SAH level overflow");
+        const uint32_t nx = uint32_t(cur ^ 1);
+        RT_CUDA(cudaMemsetAsync(&ctr->nbig[nx], 0, 4, s));
+        RT_CUDA(cudaMemsetAsync(&ctr->nblock[nx], 0, 4, s));
+        RT_CUDA(cudaMemsetAsync(&ctr->nwarp[nx], 0, 4, s));
+        const SahOut out{big[nx], block[nx], warp[nx], clusters, splits, ctr, nx, cluster_max};
+        const int median_only = level >= kSahMaxLevels ? 1 : 0;
+        if (nb) {
+            SahNode* nodes = big[cur];
+            k_sah_nchunks<<<(nb + kSahThreads - 1) / kSahThreads, kSahThreads, 0, s>>>(nodes, nb, nch);
+            RT_CHECK_LAUNCH();
+            scan_exclusive_u32(nch, chunk0, nb, L.sort_tmp, s);
+            const uint32_t prep_blocks =
+                std::min<uint32_t>(4096u, uint32_t((size_t(nb) * kBinTotal + kSahThreads - 1) / kSahThreads));
+            k_sah_prepare<<<std::max(prep_blocks, (nb + kSahThreads - 1) / kSahThreads), kSahThreads, 0, s>>>(
+                nodes, nb, chunk0, ctr, bins);
+            RT_CHECK_LAUNCH();
+            RT_CUDA(cudaMemcpyAsync(&hc, ctr, sizeof hc, cudaMemcpyDeviceToHost, s));
+            RT_CUDA(cudaStreamSynchronize(s));
+            const uint32_t nchunks = hc.nchunks;
+            RT_REQUIRE(nchunks <= max_chunks, "internal: SAH chunk overflow");
+            k_sah_bin<<<nchunks, kSahThreads, 0, s>>>(rec[cur], nodes, nb, bins, chunk_counts);
+            RT_CHECK_LAUNCH();
+            k_sah_split<<<(nb * 32 + 127) / 128, 128, 0, s>>>(nodes, nb, bins, out, median_only);
+            RT_CHECK_LAUNCH();
+            k_sah_chunk_left<<<(nchunks + kSahThreads - 1) / kSahThreads, kSahThreads, 0, s>>>(nodes, nb, nchunks,
+                                                                                             chunk_counts, chunk_left);
+            RT_CHECK_LAUNCH();
+            scan_exclusive_u32(chunk_left, chunk_scan, nchunks, L.sort_tmp, s);
+            k_sah_partition<<<nchunks, kSahThreads, 0, s>>>(rec[cur], rec[nx], nodes, nb, chunk_scan, out_ids, out);
+            RT_CHECK_LAUNCH();
+        }
+        if (nbl) {
+            k_sah_node<<<nbl, kSahThreads, 0, s>>>(rec[cur], rec[nx], block[cur], out_ids, out, median_only);
+            RT_CHECK_LAUNCH();
+        }
+        if (nw) {
+            const uint32_t wpb = kSahThreads / 32;
+            k_sah_warp<<<(nw + wpb - 1) / wpb, kSahThreads, 0, s>>>(rec[cur], rec[nx], warp[cur], nw, out_ids, out,
+                                                                   median_only);
+            RT_CHECK_LAUNCH();
+        }
         RT_CUDA(cudaMemcpyAsync(&hc, ctr, sizeof hc, cudaMemcpyDeviceToHost, s));
         RT_CUDA(cudaStreamSynchronize(s));
         if (hc.err) throw Error(RT_ERR_INTERNAL, "SAH build: partition and binning disagree");
-        nact = hc.nnext;
+        nb = hc.nbig[nx];
+        nbl = hc.nblock[nx];
+        nw = hc.nwarp[nx];
         cur ^= 1;
     }
-    RT_CUDA(cudaMemcpyAsync(&hc, ctr, sizeof hc, cudaMemcpyDeviceToHost, s));
-    RT_CUDA(cudaStreamSynchronize(s));
+    if (level == 0) {   // no node above the cluster size: the seed clusters only
+        RT_CUDA(cudaMemcpyAsync(&hc, ctr, sizeof hc, cudaMemcpyDeviceToHost, s));
+        RT_CUDA(cudaStreamSynchronize(s));
+    }
     const uint32_t ncl = hc.ncl, nsplit = hc.nsplit;
     RT_REQUIRE(ncl <= max_cl && nsplit <= max_split, "internal: SAH cluster overflow");
     // clusters in position order

@@ -50,7 +50,7 @@ def _check_tree(t, tris):
     return roots[0]
 
 
-@pytest.mark.parametrize("cluster", [1, 3, 16, None])
+@pytest.mark.parametrize("cluster", [1, 3, 16, 2048, None])
 def test_sah_tree_structure(product, oracle, cuda, sah_cluster, cluster):
     R, O = product, oracle
     sah_cluster(cluster)
@@ -59,7 +59,7 @@ def test_sah_tree_structure(product, oracle, cuda, sah_cluster, cluster):
     _check_tree(sc.lbvh(), wd.triangles())
 
 
-@pytest.mark.parametrize("cluster", [1, 16, None])
+@pytest.mark.parametrize("cluster", [1, 16, 2048, None])
 def test_sah_hits_and_images_match_oracle(product, oracle, cuda, sah_cluster, cluster):
     R, O = product, oracle
     sah_cluster(cluster)
