@@ -186,7 +186,7 @@ rt_status rt_scene_set_optics(rt_scene scene, unsigned int thing_id, const rt_op
 /* Acceleration-structure layout of the next build.
  *   FLAT: every thing flattened to world-space primitives under one LBVH
  *     over plain Morton codes of the primitive centroids.
- *   GROUPED (AUTO, the default): the same flat world-space LBVH, but its keys
+ *   GROUPED: the same flat world-space LBVH, but its keys
  *     order the things first (a 60-bit code of each thing's centre, ranked)
  *     and a thing's primitives after (a 30-bit code inside the thing's
  *     bounds), so the hierarchy has the shape of a two-level one -- the
@@ -196,10 +196,11 @@ rt_status rt_scene_set_optics(rt_scene scene, unsigned int thing_id, const rt_op
  *     LBVH per mesh, a top-level LBVH over instance records, analytic spheres
  *     and the triangles of things that cannot be instanced (non-diagonal
  *     transforms, meshes under 16 triangles); memory-lean, more work per step.
- *   SAH: the flat world-space hierarchy built top-down by binned
- *     surface-area-heuristic splits (32 bins per axis) down to clusters of at
- *     most 256 primitives, each cluster an LBVH over 30-bit Morton codes
- *     inside its own bounds; fewest node visits per ray, slowest build.
+ *   SAH (AUTO, the default): the flat world-space hierarchy built top-down
+ *     by binned surface-area-heuristic splits (32 bins per axis) down to
+ *     clusters of at most 16 primitives, each cluster an LBVH over 30-bit
+ *     Morton codes inside its own bounds; fewest node visits per ray (C1: 37
+ *     against 46 grouped, 58 flat), build about 4x the LBVH's.
  * Hits, ids and images do not depend on the layout (tested bit for bit). */
 typedef enum {
     RT_LAYOUT_AUTO = 0,

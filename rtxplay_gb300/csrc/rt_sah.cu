@@ -769,8 +769,11 @@ void build_sah_topology(Lbvh& L, uint32_t cluster_max, cudaStream_t s) {
         roots_dev = carve<int>(p, ns);
         return size_t(p - p0);
     };
-    L.sah_tmp.reserve(layout(reinterpret_cast<char*>(uintptr_t(256))));
-    layout(L.sah_tmp.as<char>());
+    // one scratch per host thread, shared by all builds (builds return only
+    // when their kernels are done)
+    static thread_local DevBuf scratch;
+    scratch.reserve(layout(reinterpret_cast<char*>(uintptr_t(256))));
+    layout(scratch.as<char>());
 
     SahCounters c0{};
     c0.nbig[0] = uint32_t(seed_big.size());
@@ -889,6 +892,7 @@ void build_sah_topology(Lbvh& L, uint32_t cluster_max, cudaStream_t s) {
     }
     L.nclusters = ncl;
     L.sah_levels = uint32_t(level);
+    RT_CUDA(cudaStreamSynchronize(s));   // the scratch is free for the next build
 }
 
 }  // namespace rt

@@ -836,10 +836,10 @@ void build_geometry(Geometry& g, const std::vector<Scene*>& scenes, int morton_b
     RT_CUDA(cudaEventRecord(e0, s));
     const Plan P = make_plan(scenes, layout);
     upload_plan(g, P, scenes.size(), s);
-    g.layout = P.ninstances ? RT_LAYOUT_INSTANCED
-               : layout == RT_LAYOUT_SAH ? RT_LAYOUT_SAH
-               : (layout == RT_LAYOUT_AUTO || layout == RT_LAYOUT_GROUPED) ? RT_LAYOUT_GROUPED
-                                                                           : RT_LAYOUT_FLAT;
+    g.layout = P.ninstances                                           ? RT_LAYOUT_INSTANCED
+               : (layout == RT_LAYOUT_AUTO || layout == RT_LAYOUT_SAH) ? RT_LAYOUT_SAH
+               : layout == RT_LAYOUT_GROUPED                          ? RT_LAYOUT_GROUPED
+                                                                      : RT_LAYOUT_FLAT;
     g.optics_seen.assign(scenes.size(), 0);
     for (size_t si = 0; si < scenes.size(); ++si) g.optics_seen[si] = scenes[si]->optics_version;
     g.misc.reserve(256);
@@ -912,7 +912,7 @@ void sync_optics(Geometry& g, const std::vector<Scene*>& scenes, cudaStream_t s)
 size_t Lbvh::device_bytes() const {
     return segs.bytes + prim_seg.bytes + prims_flat.bytes + prims.bytes + nodes.bytes + codes.bytes + ids.bytes +
            parents.bytes + flags.bytes + bounds.bytes + sort_tmp.bytes + seg_tmp.bytes + tbounds.bytes + tcodes.bytes +
-           tids.bytes + tsegs.bytes + scene_things.bytes + tseg.bytes + ttmp.bytes + sah_tmp.bytes;
+           tids.bytes + tsegs.bytes + scene_things.bytes + tseg.bytes + ttmp.bytes;
 }
 
 size_t Geometry::device_bytes() const {

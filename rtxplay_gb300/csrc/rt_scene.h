@@ -47,7 +47,6 @@ struct Lbvh {
     // things-grouped hierarchy: per-thing centroid bounds, thing codes and order,
     // per-thing record ranges, per-scene thing ranges, thing -> scene, scratch
     DevBuf tbounds, tcodes, tids, tsegs, scene_things, tseg, ttmp;
-    DevBuf sah_tmp;         // binned-SAH builder scratch
     uint32_t nprims = 0, nsegs = 0, nthings = 0;
     uint32_t nclusters = 0, sah_levels = 0;   // binned-SAH hierarchies
     int morton_bits = 60;
@@ -105,7 +104,7 @@ void build_geometry(Geometry& g, const std::vector<Scene*>& scenes, int morton_b
 // Binned-SAH topology of an LBVH whose records are in prims_flat and whose
 // segment centroid bounds are in `bounds` (rt_sah.cu): leaf order (codes,
 // ids), node children, parents and per-segment roots; the refit follows.
-constexpr uint32_t kSahClusterMax = 256;
+constexpr uint32_t kSahClusterMax = 16;
 void build_sah_topology(Lbvh& L, uint32_t cluster_max, cudaStream_t s);
 // Re-flattens the top level with the scenes' current transforms and refits it
 // (a full build when a thing changed between instanced and flattened).

@@ -39,9 +39,9 @@ def golden_scene(seed):
 def rtow_pair(R, O, level, rng_kind=0, seed=1, half_extent=11, morton_bits=60, layout=0):
     """The same final scene in the product (GPU, any layout) and in the oracle
     (CPU; flat LBVH, with things-grouped keys when the product's layout is
-    the default or RT_LAYOUT_GROUPED)."""
+    RT_LAYOUT_GROUPED).  Hits and images do not depend on the trees."""
     sc = R.rtow_scene(level, rng_kind, seed, half_extent, morton_bits, layout=layout)
-    w, _ = O.rtow_world(level, rng_kind, seed, half_extent, morton_bits, grouped=layout in (0, 3))
+    w, _ = O.rtow_world(level, rng_kind, seed, half_extent, morton_bits, grouped=layout == 3)
     return sc, w
 
 

@@ -45,27 +45,30 @@ def test_c1_first_hit_ids_bit_exact(product, oracle, cuda, c1):
 
 
 def test_c1_layouts(product, oracle, cuda, c1):
-    """Default (things-grouped) layout and the instanced one at full size:
-    info, and first hits identical to the flat oracle's."""
+    """Default (binned-SAH) layout, the things-grouped and the instanced one
+    at full size: info, and first hits identical to each other's."""
     R, O = product, oracle
     sc, wd = c1
     inf = sc.info()
-    assert inf.layout == R.RT_LAYOUT_GROUPED and inf.n_top_records == 7979008 and inf.n_instances == 0
+    assert inf.layout == R.RT_LAYOUT_SAH and inf.n_top_records == 7979008 and inf.n_instances == 0
     si = R.rtow_scene(6, layout=R.RT_LAYOUT_INSTANCED)
     ii = si.info()
     assert ii.layout == R.RT_LAYOUT_INSTANCED and ii.n_instances == 487 and ii.n_top_records == 487
     assert ii.n_bottom_records == 16384
+    sg = R.rtow_scene(6, layout=R.RT_LAYOUT_GROUPED)
+    assert sg.info().layout == R.RT_LAYOUT_GROUPED
     cam = R.rtow_camera(W, H)
     params = R.launch_params(W, H, 1, seed=99)
-    a = device_first_hit(R, cuda, si, cam, params)
     b = device_first_hit(R, cuda, sc, cam, params)
-    for k in ("prim", "thing", "t", "u", "v"):
-        assert np.array_equal(a[k].view(np.uint32) if a[k].dtype == np.float32 else a[k],
-                              b[k].view(np.uint32) if b[k].dtype == np.float32 else b[k]), k
+    for other in (si, sg):
+        a = device_first_hit(R, cuda, other, cam, params)
+        for k in ("prim", "thing", "t", "u", "v"):
+            assert np.array_equal(a[k].view(np.uint32) if a[k].dtype == np.float32 else a[k],
+                                  b[k].view(np.uint32) if b[k].dtype == np.float32 else b[k]), k
 
 
-def test_c1_grouped_lbvh_matches_twin(product, oracle, cuda, c1):
-    sc, _ = c1
+def test_c1_grouped_lbvh_matches_twin(product, oracle, cuda):
+    sc = product.rtow_scene(6, layout=product.RT_LAYOUT_GROUPED)
     wg, _ = oracle.rtow_world(6, grouped=True)
     a, b = sc.lbvh(), wg.lbvh()
     for k in ("codes", "ids", "left", "right"):

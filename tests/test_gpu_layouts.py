@@ -80,7 +80,7 @@ def test_layout_info(product, oracle, cuda):
     fi, ii, ai, si = flat.info(), inst.info(), auto.info(), sah.info()
     assert si.layout == R.RT_LAYOUT_SAH and si.n_top_records == fi.n_top_records and si.n_instances == 0
     assert fi.layout == R.RT_LAYOUT_FLAT and fi.n_instances == 0 and fi.n_bottom_records == 0
-    assert ii.layout == R.RT_LAYOUT_INSTANCED and ai.layout == R.RT_LAYOUT_GROUPED
+    assert ii.layout == R.RT_LAYOUT_INSTANCED and ai.layout == R.RT_LAYOUT_SAH
     assert fi.n_prims == ii.n_prims == ai.n_prims == fi.n_top_records == ai.n_top_records
     assert ai.n_instances == 0 and ai.n_bottom_records == 0
     assert ii.n_instances == 11                           # diagonal things; the rotated ones are flattened
