@@ -460,6 +460,8 @@ __device__ __forceinline__ bool trav_step(Trav& s, int* stack, const GeoView& g,
     }
     // h0: c0 hit; h1: c1 hit too (c0 nearer).  Primitive leaves are tested
     // now; what stays hit is descended (an internal node, or an instance).
+    // (One loop over both leaves, so that lanes with a near and lanes with a
+    // far leaf share the test's code, measured 2 % slower on C1.)
     if (bottom) {
         if (h0 && c0 < 0) { trav_leaf_bottom<kCount>(s, g, ~c0, ntest); h0 = false; }
         if (h1 && c1 < 0) { trav_leaf_bottom<kCount>(s, g, ~c1, ntest); h1 = false; }
