@@ -237,7 +237,11 @@ __device__ __forceinline__ unsigned long long fx_q(float x) {
 }
 
 // Four resident blocks per SM (64 registers): more warps in flight for the
-// latency-bound gathers.
+// latency-bound gathers.  Measured without gain on C1 (64 spp, within 0.3 %):
+// one block-wide aggregation round for the three counters instead of two
+// (2 barriers instead of 5), and the hit's thing id written by k_extend so its
+// optics load beside the primitive record (k_extend then needs 51 registers,
+// 4 % slower overall unless held to 48).
 __global__ void __launch_bounds__(kThreads, 4)
     k_shade(Queues qs, const float4* __restrict__ hits, const uint32_t* __restrict__ hthing, WaveState* st,
             const JobDev* __restrict__ jobs, uint32_t nj, const float4* __restrict__ tprims,
