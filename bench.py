@@ -95,16 +95,17 @@ def load_peaks():
 LAYOUTS = {"auto": 0, "flat": 1, "instanced": 2, "grouped": 3, "sah": 4}
 
 
-def profile_dram_bytes_per_ray(layout):
-    """DRAM bytes per ray of k_extend from the committed ncu summary of the
-    layout (one capture of full-wave launches), or None."""
+def profile_bytes_per_ray(layout, key="dram_bytes_per_ray"):
+    """DRAM (or, with key "lts_bytes_per_ray", L2) bytes per ray of k_extend
+    from the committed ncu summary of the layout (one capture of full-wave
+    launches), or None."""
     name = {1: "k_extend_c1.txt", 2: "k_extend_c1_instanced.txt", 3: "k_extend_c1_grouped.txt",
             4: "k_extend_c1_sah.txt"}.get(layout, "")
     path = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(path):
         return None
     with open(path) as f:
-        m = re.search(r"^dram_bytes_per_ray:\s*([0-9.eE+]+)", f.read(), re.M)
+        m = re.search(r"^" + key + r":\s*([0-9.eE+]+)", f.read(), re.M)
     return float(m.group(1)) if m else None
 
 
@@ -519,15 +520,17 @@ def main():
     per_launch_ms = rst.extend_ms / ext_launches
     rays_per_launch = rst.rays / ext_launches
     achieved = bytes_per_ray * rays_per_launch / (per_launch_ms * 1e-3) / 1e9 if per_launch_ms > 0 else None
-    dram_per_ray = profile_dram_bytes_per_ray(info.layout)
+    dram_per_ray = profile_bytes_per_ray(info.layout)
+    l2_per_ray = profile_bytes_per_ray(info.layout, "lts_bytes_per_ray")
     traffic = dram_per_ray * rays_per_launch if dram_per_ray else None
     frame_ms = elapsed_ms / args.steps
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": (achieved / peak) if achieved else None,
                 "traffic": traffic,
-                "traffic_note": "ncu dram bytes of full-wave launches (profiles/k_extend_c1.txt), "
-                                "per ray, times the rays of a mean launch",
-                "kernel": "k_extend (LBVH traversal + ray/triangle tests)",
+                "l2_traffic": l2_per_ray * rays_per_launch if l2_per_ray else None,
+                "traffic_note": "ncu dram__bytes (l2_traffic: lts__t_sectors x 32 B) of full-wave launches "
+                                "(profiles/k_extend_c1_<layout>.txt), per ray, times the rays of a mean launch",
+                "kernel": "k_extend (hierarchy traversal + ray/triangle tests)",
                 "timing": "CUDA events around every k_extend launch of one frame of the same workload "
                           "rendered right after the timed steps",
                 "peak_source": f"{peak_src} hbm_gbs",
