@@ -74,7 +74,7 @@ struct SahSplit {
 
 struct SahCounters {
     uint32_t nbig[2], nblock[2], nwarp[2];   // node lists, by level parity
-    uint32_t ncl, nsplit, nchunks, err;
+    uint32_t ncl, nchunks, err;
 };
 
 // Where the children of a level's nodes go.
@@ -291,12 +291,22 @@ __device__ __forceinline__ void best_split(const uint32_t* nb, uint32_t lane, in
     }
 }
 
-// Records the split of node nd (left part nleft records) and allocates its
-// children: nodes of the next level (big, block or warp node by size) or
-// clusters, each with empty centroid bounds; links the split to its parent.
-// One thread.
-__device__ void emit_split(SahNode& nd, uint32_t nleft, const SahOut& out) {
-    const uint32_t sid = atomicAdd(&out.ctr->nsplit, 1u);
+__device__ __forceinline__ int child_kind(uint32_t count, uint32_t cluster_max) {
+    return count <= cluster_max ? kCluster : count > kSahChunk ? kBig : count > kWarpNode ? kBlock : kWarp;
+}
+
+__device__ __forceinline__ uint32_t* kind_counter(int kind, const SahOut& out) {
+    return kind == kBig ? &out.ctr->nbig[out.nx] : kind == kBlock ? &out.ctr->nblock[out.nx]
+                         : kind == kWarp ? &out.ctr->nwarp[out.nx] : &out.ctr->ncl;
+}
+
+// Records split `sid` of node nd (left part nleft records) and its children,
+// whose kinds and list indices the caller allocated: nodes of the next level
+// or clusters, each with empty centroid bounds; links the split to its
+// parent.  Split ids are positions in the level's node order, so they need
+// no counter.  One thread.
+__device__ void emit_split(SahNode& nd, uint32_t nleft, uint32_t sid, const int kind[2], const uint32_t id[2],
+                           const SahOut& out) {
     SahSplit sp;
     sp.start = nd.start;
     sp.split = nd.start + nleft;
@@ -307,11 +317,7 @@ __device__ void emit_split(SahNode& nd, uint32_t nleft, const SahOut& out) {
     for (int k = 0; k < 2; ++k) {
         const uint32_t cs = k ? nd.start + nleft : nd.start;
         const uint32_t cn = k ? nd.count - nleft : nleft;
-        if (cn > out.cluster_max) {
-            const int kind = cn > kSahChunk ? kBig : cn > kWarpNode ? kBlock : kWarp;
-            uint32_t* cnt = kind == kBig ? &out.ctr->nbig[out.nx] : kind == kBlock ? &out.ctr->nblock[out.nx]
-                                                                                   : &out.ctr->nwarp[out.nx];
-            const uint32_t id = atomicAdd(cnt, 1u);
+        if (kind[k] != kCluster) {
             SahNode ch;
             ch.start = cs;
             ch.count = cn;
@@ -326,24 +332,31 @@ __device__ void emit_split(SahNode& nd, uint32_t nleft, const SahOut& out) {
             ch.nleft = 0;
             ch.child[0] = ch.child[1] = 0;
             ch.ckind[0] = ch.ckind[1] = kCluster;
-            (kind == kBig ? out.big : kind == kBlock ? out.block : out.warp)[id] = ch;
-            nd.child[k] = int(id);
-            nd.ckind[k] = kind;
+            (kind[k] == kBig ? out.big : kind[k] == kBlock ? out.block : out.warp)[id[k]] = ch;
         } else {
-            const uint32_t id = atomicAdd(&out.ctr->ncl, 1u);
             SahCluster cl;
             cl.start = cs;
             cl.count = cn;
             cl.cb[0] = cl.cb[1] = cl.cb[2] = 0xFFFFFFFFu;
             cl.cb[3] = cl.cb[4] = cl.cb[5] = 0u;
-            out.clusters[id] = cl;
-            nd.child[k] = int(id);
-            nd.ckind[k] = kCluster;
+            out.clusters[id[k]] = cl;
         }
+        nd.child[k] = int(id[k]);
+        nd.ckind[k] = kind[k];
     }
     out.splits[sid] = sp;
     if (nd.parent >= 0) out.splits[nd.parent].child[nd.side] = int(sid);
-    nd.nleft = nleft;
+}
+
+// emit_split with the children allocated one by one (one thread).
+__device__ void emit_split_alloc(SahNode& nd, uint32_t nleft, uint32_t sid, const SahOut& out) {
+    int kind[2];
+    uint32_t id[2];
+    for (int k = 0; k < 2; ++k) {
+        kind[k] = child_kind(k ? nd.count - nleft : nleft, out.cluster_max);
+        id[k] = atomicAdd(kind_counter(kind[k], out), 1u);
+    }
+    emit_split(nd, nleft, sid, kind, id, out);
 }
 
 __device__ __forceinline__ uint32_t* child_cb(const SahNode& nd, int k, const SahOut& out) {
@@ -357,7 +370,7 @@ __device__ __forceinline__ uint32_t* child_cb(const SahNode& nd, int k, const Sa
 // where no border separates records or the level cap is reached), children
 // allocated.
 __global__ void k_sah_split(SahNode* __restrict__ nodes, uint32_t nact, const uint32_t* __restrict__ bins,
-                            SahOut out, int median_only) {
+                            SahOut out, uint32_t sid0, int median_only) {
     const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t lane = threadIdx.x & 31u;
     if (w >= nact) return;
@@ -366,9 +379,10 @@ __global__ void k_sah_split(SahNode* __restrict__ nodes, uint32_t nact, const ui
     uint32_t nleft = nd.count / 2;
     if (!median_only) best_split(bins + size_t(w) * kBinTotal, lane, axis, bin, nleft);
     if (lane == 0) {
-        emit_split(nd, nleft, out);
+        emit_split_alloc(nd, nleft, sid0 + w, out);
         nd.axis = axis;
         nd.bin = bin;
+        nd.nleft = nleft;
         nodes[w] = nd;
     }
 }
@@ -495,7 +509,7 @@ __global__ void __launch_bounds__(kSahThreads)
 // bounds are final when the block ends (no other block touches them).
 __global__ void __launch_bounds__(kSahThreads)
     k_sah_node(const SahRec* __restrict__ recs, SahRec* __restrict__ out_rec, const SahNode* __restrict__ nodes,
-               uint32_t* __restrict__ out_ids, SahOut out, int median_only) {
+               uint32_t* __restrict__ out_ids, SahOut out, uint32_t sid0, int median_only) {
     __shared__ uint32_t sb[kBinTotal];
     __shared__ uint32_t s_warp[kSahThreads / 32];
     __shared__ uint32_t s_cb[12];
@@ -522,9 +536,10 @@ __global__ void __launch_bounds__(kSahThreads)
         uint32_t nleft = nd.count / 2;
         if (!median_only) best_split(sb, lane, axis, bin, nleft);
         if (lane == 0) {
-            emit_split(nd, nleft, out);
+            emit_split_alloc(nd, nleft, sid0 + blockIdx.x, out);
             nd.axis = axis;
             nd.bin = bin;
+            nd.nleft = nleft;
             s_nd = nd;
         }
     }
@@ -543,19 +558,21 @@ __global__ void __launch_bounds__(kSahThreads)
 // steps as a block node with warp-private bins and warp ballots.
 __global__ void __launch_bounds__(kSahThreads)
     k_sah_warp(const SahRec* __restrict__ recs, SahRec* __restrict__ out_rec, const SahNode* __restrict__ nodes,
-               uint32_t nw, uint32_t* __restrict__ out_ids, SahOut out, int median_only) {
+               uint32_t nw, uint32_t* __restrict__ out_ids, SahOut out, uint32_t sid0, int median_only) {
     __shared__ uint32_t sbins[kSahThreads / 32][kBinTotal];
+    __shared__ uint32_t s_cnt[4], s_base[4];   // the block's children per kind, and their first index
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const uint32_t w = blockIdx.x * (kSahThreads / 32) + warp;
-    if (w >= nw) return;   // whole warps
+    const bool live = w < nw;   // whole warps; every warp reaches the barriers
+    if (threadIdx.x < 4) s_cnt[threadIdx.x] = 0;
     uint32_t* sb = sbins[warp];
-    SahNode nd = nodes[w];
-    const uint32_t b = nd.start, e = nd.start + nd.count;
+    SahNode nd = nodes[live ? w : 0];
+    const uint32_t b = nd.start, e = live ? nd.start + nd.count : nd.start;
     float lo[3], scale[3];
     sah_frame(nd.cb, lo, scale);
     int axis = -1, bin = 0;
     uint32_t nleft = nd.count / 2;
-    if (!median_only) {
+    if (live && !median_only) {
         empty_bins(sb, lane, 32);
         __syncwarp();
         for (uint32_t base = b; base < e; base += 32) {
@@ -568,7 +585,24 @@ __global__ void __launch_bounds__(kSahThreads)
         __syncwarp();
         best_split(sb, lane, axis, bin, nleft);
     }
-    if (lane == 0) emit_split(nd, nleft, out);
+    // children: counted per block, one global atomic per kind and block
+    int kind[2] = {kCluster, kCluster};
+    uint32_t local[2] = {0u, 0u};
+    __syncthreads();   // s_cnt is cleared
+    if (live && lane == 0) {
+        for (int k = 0; k < 2; ++k) {
+            kind[k] = child_kind(k ? nd.count - nleft : nleft, out.cluster_max);
+            local[k] = atomicAdd(&s_cnt[kind[k]], 1u);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 4 && s_cnt[threadIdx.x]) s_base[threadIdx.x] = atomicAdd(kind_counter(threadIdx.x, out), s_cnt[threadIdx.x]);
+    __syncthreads();
+    if (!live) return;
+    if (lane == 0) {
+        const uint32_t id[2] = {s_base[kind[0]] + local[0], s_base[kind[1]] + local[1]};
+        emit_split(nd, nleft, sid0 + w, kind, id, out);
+    }
     nd.child[0] = __shfl_sync(0xFFFFFFFFu, nd.child[0], 0);
     nd.child[1] = __shfl_sync(0xFFFFFFFFu, nd.child[1], 0);
     nd.ckind[0] = __shfl_sync(0xFFFFFFFFu, nd.ckind[0], 0);
@@ -797,6 +831,7 @@ void build_sah_topology(Lbvh& L, uint32_t cluster_max, cudaStream_t s) {
                                                                                out_ids);
     RT_CHECK_LAUNCH();
     uint32_t nb = c0.nbig[0], nbl = c0.nblock[0], nw = c0.nwarp[0];
+    uint32_t nsplit = 0;   // one split per node of every level, ids in level order
     int cur = 0, level = 0;
     SahCounters hc{};
     for (; nb + nbl + nw > 0; ++level) {
@@ -823,7 +858,7 @@ void build_sah_topology(Lbvh& L, uint32_t cluster_max, cudaStream_t s) {
             RT_REQUIRE(nchunks <= max_chunks, "internal: SAH chunk overflow");
             k_sah_bin<<<nchunks, kSahThreads, 0, s>>>(rec[cur], nodes, nb, bins, chunk_counts);
             RT_CHECK_LAUNCH();
-            k_sah_split<<<(nb * 32 + 127) / 128, 128, 0, s>>>(nodes, nb, bins, out, median_only);
+            k_sah_split<<<(nb * 32 + 127) / 128, 128, 0, s>>>(nodes, nb, bins, out, nsplit, median_only);
             RT_CHECK_LAUNCH();
             k_sah_chunk_left<<<(nchunks + kSahThreads - 1) / kSahThreads, kSahThreads, 0, s>>>(nodes, nb, nchunks,
                                                                                              chunk_counts, chunk_left);
@@ -833,18 +868,20 @@ void build_sah_topology(Lbvh& L, uint32_t cluster_max, cudaStream_t s) {
             RT_CHECK_LAUNCH();
         }
         if (nbl) {
-            k_sah_node<<<nbl, kSahThreads, 0, s>>>(rec[cur], rec[nx], block[cur], out_ids, out, median_only);
+            k_sah_node<<<nbl, kSahThreads, 0, s>>>(rec[cur], rec[nx], block[cur], out_ids, out, nsplit + nb,
+                                                   median_only);
             RT_CHECK_LAUNCH();
         }
         if (nw) {
             const uint32_t wpb = kSahThreads / 32;
             k_sah_warp<<<(nw + wpb - 1) / wpb, kSahThreads, 0, s>>>(rec[cur], rec[nx], warp[cur], nw, out_ids, out,
-                                                                   median_only);
+                                                                   nsplit + nb + nbl, median_only);
             RT_CHECK_LAUNCH();
         }
         RT_CUDA(cudaMemcpyAsync(&hc, ctr, sizeof hc, cudaMemcpyDeviceToHost, s));
         RT_CUDA(cudaStreamSynchronize(s));
         if (hc.err) throw Error(RT_ERR_INTERNAL, "SAH build: partition and binning disagree");
+        nsplit += nb + nbl + nw;
         nb = hc.nbig[nx];
         nbl = hc.nblock[nx];
         nw = hc.nwarp[nx];
@@ -854,7 +891,7 @@ void build_sah_topology(Lbvh& L, uint32_t cluster_max, cudaStream_t s) {
         RT_CUDA(cudaMemcpyAsync(&hc, ctr, sizeof hc, cudaMemcpyDeviceToHost, s));
         RT_CUDA(cudaStreamSynchronize(s));
     }
-    const uint32_t ncl = hc.ncl, nsplit = hc.nsplit;
+    const uint32_t ncl = hc.ncl;
     RT_REQUIRE(ncl <= max_cl && nsplit <= max_split, "internal: SAH cluster overflow");
     // clusters in position order
     k_sah_cluster_keys<<<(ncl + kSahThreads - 1) / kSahThreads, kSahThreads, 0, s>>>(clusters, ncl, ckeys, cvals);

@@ -208,11 +208,17 @@ __global__ void k_init_bounds(uint32_t* b, uint32_t nsegs) {
 }
 
 // Centroid bounds per segment: a warp whose primitives share one segment
-// reduces in registers and issues six atomics; a mixed warp (segment border)
-// issues them per lane.
-__global__ void k_centroid_bounds(const float4* __restrict__ prims, const uint32_t* __restrict__ prim_seg,
-                                  uint32_t n, uint32_t* __restrict__ bounds, int by_thing) {
+// reduces in registers; the warps of a block that share a segment merge in
+// shared memory and issue six atomics per block; a mixed warp (segment
+// border) issues them per lane.
+__global__ void __launch_bounds__(kThreads)
+    k_centroid_bounds(const float4* __restrict__ prims, const uint32_t* __restrict__ prim_seg, uint32_t n,
+                      uint32_t* __restrict__ bounds, int by_thing) {
+    __shared__ uint32_t s_v[kThreads / 32][6];
+    __shared__ uint32_t s_seg[kThreads / 32];
+    __shared__ int s_uni[kThreads / 32];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t warp = threadIdx.x >> 5;
     const bool valid = i < n;
     uint32_t v[6] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u};
     uint32_t seg = 0;
@@ -224,9 +230,8 @@ __global__ void k_centroid_bounds(const float4* __restrict__ prims, const uint32
         seg = by_thing ? __float_as_uint(prims[3 * size_t(i)].w) : (prim_seg ? prim_seg[i] : 0u);
     }
     const uint32_t vmask = __ballot_sync(0xFFFFFFFFu, valid);
-    if (!vmask) return;
-    const uint32_t seg0 = __shfl_sync(0xFFFFFFFFu, seg, __ffs(vmask) - 1);
-    const bool uniform = __all_sync(0xFFFFFFFFu, !valid || seg == seg0);
+    const uint32_t seg0 = vmask ? __shfl_sync(0xFFFFFFFFu, seg, __ffs(vmask) - 1) : 0u;
+    const bool uniform = vmask && __all_sync(0xFFFFFFFFu, !valid || seg == seg0);
     if (uniform) {
         for (int o = 16; o > 0; o >>= 1) {
 #pragma unroll
@@ -235,15 +240,36 @@ __global__ void k_centroid_bounds(const float4* __restrict__ prims, const uint32
                 v[k] = k < 3 ? min(v[k], w) : max(v[k], w);
             }
         }
-        if ((threadIdx.x & 31u) == 0) {
-            uint32_t* b = bounds + 6 * seg0;
-            atomicMin(&b[0], v[0]); atomicMin(&b[1], v[1]); atomicMin(&b[2], v[2]);
-            atomicMax(&b[3], v[3]); atomicMax(&b[4], v[4]); atomicMax(&b[5], v[5]);
-        }
     } else if (valid) {
         uint32_t* b = bounds + 6 * seg;
         atomicMin(&b[0], v[0]); atomicMin(&b[1], v[1]); atomicMin(&b[2], v[2]);
         atomicMax(&b[3], v[3]); atomicMax(&b[4], v[4]); atomicMax(&b[5], v[5]);
+    }
+    if ((threadIdx.x & 31u) == 0) {
+        s_uni[warp] = uniform ? 1 : 0;
+        s_seg[warp] = seg0;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) s_v[warp][k] = v[k];
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {   // thread k merges value k over runs of warps with one segment
+        const uint32_t k = threadIdx.x;
+        uint32_t cur = 0xFFFFFFFFu, acc = 0;
+        for (uint32_t w = 0; w <= kThreads / 32; ++w) {
+            const bool end = w == kThreads / 32;
+            if (!end && !s_uni[w]) continue;
+            if (end || s_seg[w] != cur) {
+                if (cur != 0xFFFFFFFFu) {
+                    if (k < 3) atomicMin(&bounds[6 * size_t(cur) + k], acc);
+                    else atomicMax(&bounds[6 * size_t(cur) + k], acc);
+                }
+                if (end) break;
+                cur = s_seg[w];
+                acc = s_v[w][k];
+            } else {
+                acc = k < 3 ? min(acc, s_v[w][k]) : max(acc, s_v[w][k]);
+            }
+        }
     }
 }
 
