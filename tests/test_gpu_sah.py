@@ -132,3 +132,85 @@ def test_sah_batch_segments(product, cuda, sah_cluster, cluster):
     for (raw, rpp), ref in zip(bufs, singles):
         assert np.array_equal(raw.cpu().numpy().view(np.uint32), ref["rawRGB"].reshape(-1).view(np.uint32))
         assert np.array_equal(rpp.cpu().numpy(), ref["rpp"].reshape(-1))
+
+
+def _pair_from(R, O, meshes, things, spheres):
+    """Product scene (SAH) and oracle world from (vces, ices) meshes,
+    (mesh index, transform) things and (centre, radius) analytic spheres."""
+    sc, wd = R.Scene(), O.World()
+    opt = (0, (0.6, 0.5, 0.4), 0.0, 0.0)
+    ro = R.optics(opt[0], opt[1], opt[2], opt[3])
+    mids, oids = [], []
+    for v, i in meshes:
+        mids.append(sc.add_mesh(v, i))
+        oids.append(wd.add_mesh(np.ascontiguousarray(v, np.float32), np.ascontiguousarray(i, np.uint32)))
+    for m, T in things:
+        T = np.asarray(T, np.float32)
+        sc.add_thing(ro, mids[m], T)
+        wd.add_thing(opt[0], np.asarray(opt[1], np.float32), opt[2], opt[3], oids[m], T)
+    for c, r in spheres:
+        sc.add_analytic_sphere(c, r, ro)
+        wd.add_sphere(opt[0], np.asarray(opt[1], np.float32), opt[2], opt[3], np.asarray(c, np.float32), float(r))
+    sc.build(layout=R.RT_LAYOUT_SAH)
+    wd.build(60)
+    return sc, wd
+
+
+def _first_hits_match(R, O, cuda, sc, wd, cam, w, h):
+    g = device_first_hit(R, cuda, sc, cam, R.launch_params(w, h, 1, seed=21))
+    c = wd.first_hit(oracle_camera(O, cam), w, h, 21)
+    assert np.array_equal(g["prim"], c["prim"]) and np.array_equal(g["thing"], c["thing"])
+    assert np.array_equal(g["t"].view(np.uint32), c["t"].view(np.uint32))
+    return g
+
+
+def test_sah_identical_centroids(product, oracle, cuda):
+    """6000 copies of one triangle (one centroid: no border separates them,
+    every split is a median split) beside a small sphere mesh."""
+    R, O = product, oracle
+    tri_v = np.array([[-1, 0, -1], [1, 0, -1], [0, 0, 1]], np.float32)
+    tri_i = np.array([[0, 1, 2]] * 6000, np.uint32)
+    sv, si = O.tessellate(1.0, 3)
+    ident = [1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0]
+    sc, wd = _pair_from(R, O, [(tri_v, tri_i), (sv, si)], [(0, ident), (1, [0.5, 0, 0, 2, 0, 0.5, 0, 0.6, 0, 0, 0.5, 0])],
+                        [])
+    assert sc.info().layout == R.RT_LAYOUT_SAH
+    _check_tree(sc.lbvh(), wd.triangles())
+    cam = R.camera_set((0, 3, 6), (0.5, 0, 0), (0, 1, 0), 40, 1.5, 0.0, 6.0)
+    g = _first_hits_match(R, O, cuda, sc, wd, cam, 96, 64)
+    assert (g["prim"] >= 0).sum() > 0 and (g["prim"] == 5999).any()   # equal t: the larger id wins
+
+
+def test_sah_exponential_spacing_hits_level_cap(product, oracle, cuda, sah_cluster):
+    """Spheres at x = 1.25^k: binned SAH peels them off one or a few per
+    level, past the level cap (64), where the median split takes over."""
+    R, O = product, oracle
+    sah_cluster(2)
+    spheres = [((float(1.25 ** k), 0.0, 0.0), 0.1) for k in range(300)]
+    sc, wd = _pair_from(R, O, [], [], spheres)
+    t = sc.lbvh()
+    n = len(t["ids"])
+    assert n == 300 and np.array_equal(np.sort(t["ids"]), np.arange(n, dtype=np.uint32))
+    kids = np.concatenate([t["left"], t["right"]])
+    assert np.array_equal(np.sort(~kids[kids < 0]), np.arange(n))
+    cam = R.camera_set((0.3, 0.0, 40.0), (0.3, 0.0, 0.0), (0, 1, 0), 30, 1.5, 0.0, 40.0)
+    _first_hits_match(R, O, cuda, sc, wd, cam, 120, 80)
+
+
+def test_sah_update_refits_and_rebuilds(product, oracle, cuda):
+    """Transform edits under the SAH layout: the refit keeps the tree and the
+    hits follow the oracle's rebuilt world."""
+    R, O = product, oracle
+    sc, wd = rtow_pair(R, O, 2, layout=R.RT_LAYOUT_SAH)
+    for tid in (3, 40, 100):
+        st, T = sc.get_transform(tid)
+        T = T.copy()
+        T[3] += 0.4
+        T[11] -= 0.3
+        assert sc.set_transform(tid, T) == R.RT_OK
+        assert wd.set_transform(tid, T) == 0
+    sc.update()
+    wd.build()
+    _check_tree(sc.lbvh(), wd.triangles())
+    cam = R.rtow_camera(160, 96)
+    _first_hits_match(R, O, cuda, sc, wd, cam, 160, 96)
