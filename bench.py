@@ -537,7 +537,12 @@ def main():
                 "bytes_per_ray": bytes_per_ray, "nodes_per_ray": nodes_per_ray, "prims_per_ray": prims_per_ray,
                 "extend_ms_per_launch": per_launch_ms, "extend_launches": int(rst.extend_launches),
                 "shade_ms_per_frame": rst.shade_ms, "extend_ms_per_frame": rst.extend_ms,
-                "extend_share": rst.extend_ms / max(frame_ms, 1e-9), "rays_per_launch": rays_per_launch}
+                "extend_share": rst.extend_ms / max(frame_ms, 1e-9), "rays_per_launch": rays_per_launch,
+                # what actually reaches DRAM and L2 per second at the measured launch time
+                # (profiled bytes per ray x rays per launch / mean launch duration)
+                "dram_gbs": (traffic / (per_launch_ms * 1e-3) / 1e9) if traffic and per_launch_ms > 0 else None,
+                "l2_gbs": (l2_per_ray * rays_per_launch / (per_launch_ms * 1e-3) / 1e9)
+                if l2_per_ray and per_launch_ms > 0 else None}
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": frame_ms, "higher_is_better": True,
