@@ -24,11 +24,13 @@
 //                    move on the fixed surface, sphere normals turn with the
 //                    hit point, reflection / refraction directions are
 //                    differentiated, diffuse directions follow the normal.
-// The albedo and sky terms are computed in double precision in the same
-// operation order as the FP64 CPU restatement of the method
-// (oracle/rt_oracle.cpp, orc_adjoint), so every path's terms agree bit for
-// bit and the totals only differ by summation order; the fuzz tangent runs in
-// binary32 (agreeing with the FP64 restatement to single precision).
+// Each path's terms are binary32 products in the operation order of the FP64
+// CPU restatement of the method (oracle/rt_oracle.cpp, orc_adjoint); a block
+// sums them in binary32 in shared memory and adds its sums to double-precision
+// totals.  GB300's FP64 rate made the all-double form of these terms the
+// adjoint's bound (FP64 pipe 64 % busy); the totals agree with the FP64
+// restatement to single precision.  The fuzz tangent keeps two double-precision
+// steps where grazing geometry cancels digits (see tangent_to_sky).
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -65,7 +67,6 @@ __device__ __forceinline__ D3 operator-(D3 a, D3 b) { return D3{a.x - b.x, a.y -
 __device__ __forceinline__ D3 operator*(double s, D3 a) { return D3{s * a.x, s * a.y, s * a.z}; }
 __device__ __forceinline__ double ddot(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 __device__ __forceinline__ double dlen(D3 a) { return sqrt(ddot(a, a)); }
-__device__ __forceinline__ D3 dmul(D3 a, D3 b) { return D3{a.x * b.x, a.y * b.y, a.z * b.z}; }
 
 // derivative of unit(d) along dd
 __device__ __forceinline__ D3 dunit(D3 d, D3 dd) {
@@ -83,7 +84,7 @@ struct AdjVtx {
     float ratio;     // glass: index ratio
     uint32_t thing;  // global thing (sphere centre / radius for the tangent)
     uint32_t bits;   // type | branch << 2 | front << 3
-    D3 pre;          // product of the albedos before this vertex
+    float3 pre;      // product of the albedos before this vertex
 };
 
 // Forward tangent (dO, dD) of the ray entering vertex m, carried through
@@ -160,37 +161,37 @@ __device__ __forceinline__ uint32_t adj_job_of(const AdjJob* __restrict__ jobs, 
 }
 
 // Gradient sinks of one block: per-thing sums of the block's first job in
-// shared memory (4 doubles per thing: albedo rgb, fuzz), everything else in
-// the global sums G (4 doubles per global thing, then 6 sky values per job).
+// shared memory (4 floats per thing: albedo rgb, fuzz), everything else in
+// the global double sums G (4 per global thing, then 6 sky values per job).
 struct Sink {
-    double* sh;         // shared sums of job j0, or nullptr
+    float* sh;          // shared sums of job j0, or nullptr
     uint32_t j0;
     double* G;
     uint32_t nthings_total;
-    __device__ __forceinline__ void add(uint32_t jx, const AdjJob& j, uint32_t thing, int c, double x) const {
-        if (x == 0.0) return;
+    __device__ __forceinline__ void add(uint32_t jx, const AdjJob& j, uint32_t thing, int c, float x) const {
+        if (x == 0.f) return;
         if (sh && jx == j0) atomicAdd(sh + 4 * (thing - j.thing_begin) + c, x);
-        else atomicAdd(G + 4 * size_t(thing) + c, x);
+        else atomicAdd(G + 4 * size_t(thing) + c, double(x));
     }
 };
 
 // Replays global path `path` and adds its gradient terms.  Returns 1 when the
 // traversal stack overflowed.
 __device__ uint32_t adjoint_path(const AdjJob* __restrict__ jobs, uint32_t nj, unsigned long long path, const GeoView& geo,
-                                 const ThingDev* __restrict__ things, const double* __restrict__ gpix, const Sink& sink,
-                                 double gsky[6]) {
+                                 const ThingDev* __restrict__ things, const float* __restrict__ gpix, const Sink& sink,
+                                 float gsky[6]) {
     const uint32_t jx = adj_job_of(jobs, nj, path);
     const AdjJob& j = jobs[jx];
     const uint32_t pid = uint32_t(path - j.path_offset);
     const uint32_t pix = pid / j.spp, smp = pid % j.spp;   // pixel-major, as the forward wavefront
-    double g[3];
+    float g[3];
     {
-        const double* gp = gpix + 3 * (size_t(j.pix_offset) + pix);
+        const float* gp = gpix + 3 * (size_t(j.pix_offset) + pix);
         g[0] = gp[0];
         g[1] = gp[1];
         g[2] = gp[2];
     }
-    if (g[0] == 0.0 && g[1] == 0.0 && g[2] == 0.0) return 0;
+    if (g[0] == 0.f && g[1] == 0.f && g[2] == 0.f) return 0;
 
     float3 o, d;
     {
@@ -200,7 +201,7 @@ __device__ uint32_t adjoint_path(const AdjJob* __restrict__ jobs, uint32_t nj, u
     AdjVtx V[kAdjMaxDepth - 1];
     uint32_t ne = 0;
     bool miss = false;
-    D3 pre{1, 1, 1};
+    float3 pre = mk(1.f, 1.f, 1.f);
     for (uint32_t k = 0;; ++k) {
         uint32_t nv = 0, nt = 0;
         const HitRec h = closest_hit_any<false>(geo, j.root, o, d, nv, nt);
@@ -225,8 +226,8 @@ __device__ uint32_t adjoint_path(const AdjJob* __restrict__ jobs, uint32_t nj, u
         v.thing = h.thing;
         v.bits = uint32_t(so.type) | (uint32_t(so.branch) << 2) | (uint32_t(so.front) << 3);
         v.pre = pre;
-        const D3 a = so.type == RT_OPTICS_REFRACT ? D3{1, 1, 1} : dd3(xyz(things[v.thing].albedo_type));
-        pre = dmul(pre, a);
+        const float3 a = so.type == RT_OPTICS_REFRACT ? mk(1.f, 1.f, 1.f) : xyz(things[v.thing].albedo_type);
+        pre = mulv(pre, a);
         ++ne;
         if (!so.cont) break;   // absorbed
         o = so.p;
@@ -234,33 +235,33 @@ __device__ uint32_t adjoint_path(const AdjJob* __restrict__ jobs, uint32_t nj, u
     }
     if (!miss) return 0;   // absorbed or depth-limited: black, no gradient
 
-    const D3 u = (1.0 / dlen(dd3(d))) * dd3(d);
-    const double sv = 0.5 * (u.y + 1.0);
-    const double skyc[3] = {(1.0 - sv) * j.white.x + sv * j.ambient.x, (1.0 - sv) * j.white.y + sv * j.ambient.y,
-                            (1.0 - sv) * j.white.z + sv * j.ambient.z};
-    const double th3[3] = {pre.x, pre.y, pre.z};
+    const float3 u = mul(1.f / len(d), d);
+    const float sv = .5f * (u.y + 1.f);
+    const float skyc[3] = {(1.f - sv) * j.white.x + sv * j.ambient.x, (1.f - sv) * j.white.y + sv * j.ambient.y,
+                           (1.f - sv) * j.white.z + sv * j.ambient.z};
+    const float th3[3] = {pre.x, pre.y, pre.z};
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         gsky[c] += g[c] * th3[c] * sv;              // ambient
-        gsky[3 + c] += g[c] * th3[c] * (1.0 - sv);  // white
+        gsky[3 + c] += g[c] * th3[c] * (1.f - sv);  // white
     }
-    D3 suf{1, 1, 1};
+    float3 suf = mk(1.f, 1.f, 1.f);
     for (uint32_t k = ne; k-- > 0;) {
         const AdjVtx& v = V[k];
         const int type = int(v.bits & 3u);
         if (type == RT_OPTICS_REFRACT) continue;   // albedo factor 1: suffix unchanged
-        const D3 o3 = dmul(v.pre, suf);
+        const float3 o3 = mulv(v.pre, suf);
         sink.add(jx, j, v.thing, 0, g[0] * o3.x * skyc[0]);
         sink.add(jx, j, v.thing, 1, g[1] * o3.y * skyc[1]);
         sink.add(jx, j, v.thing, 2, g[2] * o3.z * skyc[2]);
         if (type == RT_OPTICS_REFLECT) {
-            const double duy = tangent_to_sky(V, k + 1, ne, geo.desc, mk(0.f, 0.f, 0.f), v.v, d);
-            const double ds = 0.5 * duy;
-            const D3 dsc{ds * (double(j.ambient.x) - j.white.x), ds * (double(j.ambient.y) - j.white.y),
-                         ds * (double(j.ambient.z) - j.white.z)};
+            const float duy = tangent_to_sky(V, k + 1, ne, geo.desc, mk(0.f, 0.f, 0.f), v.v, d);
+            const float ds = .5f * duy;
+            const float3 dsc = mk(ds * (j.ambient.x - j.white.x), ds * (j.ambient.y - j.white.y),
+                                  ds * (j.ambient.z - j.white.z));
             sink.add(jx, j, v.thing, 3, g[0] * th3[0] * dsc.x + g[1] * th3[1] * dsc.y + g[2] * th3[2] * dsc.z);
         }
-        suf = dmul(suf, dd3(xyz(things[v.thing].albedo_type)));
+        suf = mulv(suf, xyz(things[v.thing].albedo_type));
     }
     return 0;
 }
@@ -268,7 +269,7 @@ __device__ uint32_t adjoint_path(const AdjJob* __restrict__ jobs, uint32_t nj, u
 // Per pixel and channel, the loss gradient each of the pixel's paths carries:
 // g = dL/dI' * [0 < I < 1] / spp (once per pixel instead of once per path).
 __global__ void k_adjoint_pixel_g(const AdjJob* __restrict__ jobs, uint32_t nj, uint32_t total_pix,
-                                  double* __restrict__ gpix) {
+                                  float* __restrict__ gpix) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= total_pix) return;
     uint32_t lo = 0, hi = nj;
@@ -283,7 +284,7 @@ __global__ void k_adjoint_pixel_g(const AdjJob* __restrict__ jobs, uint32_t nj, 
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         const double mask = (Ic[c] > 0.f && Ic[c] < 1.f) ? 1.0 : 0.0;   // clamp to [0, 1]
-        gpix[3 * size_t(p) + c] = double(Gc[c]) * mask / double(j.spp);
+        gpix[3 * size_t(p) + c] = float(double(Gc[c]) * mask / double(j.spp));
     }
 }
 
@@ -291,17 +292,17 @@ __global__ void k_adjoint_pixel_g(const AdjJob* __restrict__ jobs, uint32_t nj, 
 // Four resident blocks per SM cap the registers at 128 per thread.
 __global__ void __launch_bounds__(kAdjThreads, 4)
     k_adjoint(const AdjJob* __restrict__ jobs, uint32_t nj, unsigned long long total, GeoView geo,
-              const ThingDev* __restrict__ things, const double* __restrict__ gpix, double* G, uint32_t nthings_total,
+              const ThingDev* __restrict__ things, const float* __restrict__ gpix, double* G, uint32_t nthings_total,
               uint32_t sh_things, uint32_t* err) {
-    extern __shared__ double sh[];   // [4 * sh_things] + [6]
+    extern __shared__ float sh[];   // [4 * sh_things] + [6]
     const unsigned long long base = (unsigned long long)blockIdx.x * kAdjPathsPerBlock;
     const uint32_t j0 = adj_job_of(jobs, nj, base);
     const bool use_sh = jobs[j0].nthings <= sh_things;
     const uint32_t nsh = use_sh ? 4 * jobs[j0].nthings : 0;
-    for (uint32_t i = threadIdx.x; i < nsh + 6; i += blockDim.x) sh[i] = 0.0;
+    for (uint32_t i = threadIdx.x; i < nsh + 6; i += blockDim.x) sh[i] = 0.f;
     __syncthreads();
     Sink sink{use_sh ? sh : nullptr, j0, G, nthings_total};
-    double gsky[6] = {0, 0, 0, 0, 0, 0};
+    float gsky[6] = {0, 0, 0, 0, 0, 0};
     uint32_t my_err = 0;
     for (uint32_t c = 0; c < kAdjPathsPerThread; ++c) {
         const unsigned long long path = base + c * kAdjThreads + threadIdx.x;
@@ -310,29 +311,29 @@ __global__ void __launch_bounds__(kAdjThreads, 4)
         if (jx == j0) {
             my_err |= adjoint_path(jobs, nj, path, geo, things, gpix, sink, gsky);
         } else {   // a block that straddles two jobs: sky terms of the later job go straight to G
-            double gs[6] = {0, 0, 0, 0, 0, 0};
+            float gs[6] = {0, 0, 0, 0, 0, 0};
             my_err |= adjoint_path(jobs, nj, path, geo, things, gpix, sink, gs);
             for (int k = 0; k < 6; ++k)
-                if (gs[k] != 0.0) atomicAdd(G + 4 * size_t(nthings_total) + 6 * size_t(jx) + k, gs[k]);
+                if (gs[k] != 0.f) atomicAdd(G + 4 * size_t(nthings_total) + 6 * size_t(jx) + k, double(gs[k]));
         }
     }
     if (my_err) atomicOr(err, 1u);
     // sky sums of job j0: warp reduction, then one shared atomic per warp
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
-        double x = gsky[k];
+        float x = gsky[k];
         for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xFFFFFFFFu, x, off);
-        if ((threadIdx.x & 31u) == 0 && x != 0.0) atomicAdd(sh + nsh + k, x);
+        if ((threadIdx.x & 31u) == 0 && x != 0.f) atomicAdd(sh + nsh + k, x);
     }
     __syncthreads();
     const size_t tb = jobs[j0].thing_begin;
     for (uint32_t i = threadIdx.x; i < nsh; i += blockDim.x) {
-        const double x = sh[i];
-        if (x != 0.0) atomicAdd(G + 4 * tb + i, x);
+        const float x = sh[i];
+        if (x != 0.f) atomicAdd(G + 4 * tb + i, double(x));
     }
     if (threadIdx.x < 6) {
-        const double x = sh[nsh + threadIdx.x];
-        if (x != 0.0) atomicAdd(G + 4 * size_t(nthings_total) + 6 * size_t(j0) + threadIdx.x, x);
+        const float x = sh[nsh + threadIdx.x];
+        if (x != 0.f) atomicAdd(G + 4 * size_t(nthings_total) + 6 * size_t(j0) + threadIdx.x, double(x));
     }
 }
 
@@ -417,7 +418,7 @@ void adjoint_jobs(const Geometry& g, const std::vector<AdjointJob>& jobs, cudaSt
     }
     RT_REQUIRE(total_pix < (uint64_t(1) << 31), "too many pixels in one launch (>= 2^31)");
     const size_t gsize = (4 * size_t(g.nthings) + 6 * size_t(nj)) * sizeof(double);
-    ws.gpix.reserve(std::max<size_t>(1, total_pix) * 3 * sizeof(double));
+    ws.gpix.reserve(std::max<size_t>(1, total_pix) * 3 * sizeof(float));
     ws.jobs.reserve(nj * sizeof(AdjJob));
     ws.outs.reserve(nj * sizeof(AdjOut));
     ws.G.reserve(gsize);
@@ -427,14 +428,14 @@ void adjoint_jobs(const Geometry& g, const std::vector<AdjointJob>& jobs, cudaSt
     RT_CUDA(cudaMemsetAsync(ws.G.p, 0, gsize, s));
     RT_CUDA(cudaMemsetAsync(ws.err.p, 0, 4, s));
     const uint32_t sh_things = std::min(max_things, kAdjShThings);
-    const size_t shmem = (4 * size_t(sh_things) + 6) * sizeof(double);
+    const size_t shmem = (4 * size_t(sh_things) + 6) * sizeof(float);
     if (total) {
         k_adjoint_pixel_g<<<unsigned((total_pix + 255) / 256), 256, 0, s>>>(ws.jobs.as<AdjJob>(), nj,
-                                                                           uint32_t(total_pix), ws.gpix.as<double>());
+                                                                           uint32_t(total_pix), ws.gpix.as<float>());
         RT_CHECK_LAUNCH();
         const unsigned grid = unsigned((total + kAdjPathsPerBlock - 1) / kAdjPathsPerBlock);
         k_adjoint<<<grid, kAdjThreads, shmem, s>>>(ws.jobs.as<AdjJob>(), nj, total, g.view(),
-                                                   g.things_dev.as<ThingDev>(), ws.gpix.as<double>(),
+                                                   g.things_dev.as<ThingDev>(), ws.gpix.as<float>(),
                                                    ws.G.as<double>(), g.nthings, sh_things, ws.err.as<uint32_t>());
         RT_CHECK_LAUNCH();
     }

@@ -1,9 +1,10 @@
 """GPU: the adjoint path-replay launch.
 
 Checked three ways: against the FP64 CPU adjoint of the oracle on the same
-image and loss gradient (albedo and sky terms are computed with the same double
-operations, so only the summation order differs, 1e-9 relative; the fuzz
-tangent runs in binary32 on the GPU, 2e-4 relative); against central finite
+image and loss gradient (the GPU forms each path's albedo and sky terms in
+binary32 and sums them in binary32 per block, double across blocks: 1e-5 of
+the largest gradient; the fuzz tangent, binary32 with two double steps: 2e-4);
+against central finite
 differences of GPU renders with common random numbers (h = 1e-3) for albedo
 and sky colours, through a torch.autograd.Function that wraps the forward
 launch and the adjoint; and batch against single-scene launches.
@@ -64,8 +65,8 @@ def test_adjoint_matches_fp64_oracle(product, oracle, cuda, level, spp, depth):
     g_dev = torch.from_numpy(G.reshape(-1)).cuda()
     got = _adjoint(R, torch, sc, cam, params, img, g_dev)
     ref = wd.adjoint(oracle_camera(O, cam), W, H, spp, depth, seed, I, G, ambient=AMB, white=WHT)
-    _close(got["albedo"], ref["albedo"])   # same FP64 terms, summation order differs
-    _close(got["sky"], ref["sky"])
+    _close(got["albedo"], ref["albedo"], rel=1e-5)   # binary32 terms against FP64 ones
+    _close(got["sky"], ref["sky"], rel=1e-5)
     if np.abs(ref["fuzz"]).max() > 0:
         _close(got["fuzz"], ref["fuzz"], rel=2e-4)   # the fuzz tangent runs in binary32 on the GPU
     # glass has no albedo gradient, only metals have a fuzz gradient
@@ -204,10 +205,11 @@ def test_batch_adjoint_equals_single_scene_adjoints(product, cuda):
         img = _render(R, torch, sc, cam, params)
         assert torch.equal(img, raw)
         one = _adjoint(R, torch, sc, cam, params, img, o[0])
-        _close(o[1].cpu().numpy().reshape(-1, 3), one["albedo"])
+        # the same binary32 terms; block sums group the paths differently
+        _close(o[1].cpu().numpy().reshape(-1, 3), one["albedo"], rel=1e-5)
         if np.abs(one["fuzz"]).max() > 0:
-            _close(o[2].cpu().numpy(), one["fuzz"])
-        _close(o[3].cpu().numpy(), one["sky"])
+            _close(o[2].cpu().numpy(), one["fuzz"], rel=1e-5)
+        _close(o[3].cpu().numpy(), one["sky"], rel=1e-5)
 
 
 def test_adjoint_errors(product, cuda):
