@@ -850,6 +850,19 @@ void build_lbvh(Lbvh& L, int morton_bits, cudaStream_t s, const FlatDesc* desc =
 
 }  // namespace
 
+// Bottom-level roots of the instanced things, read from the built bottom
+// level (a binned-SAH hierarchy's root is not its segment's first slot).
+void set_blas_roots(const Lbvh& blas, std::vector<FlatDesc>& desc, std::vector<InstDev>& inst) {
+    for (size_t t = 0; t < desc.size(); ++t) {
+        if (!desc[t].instanced) continue;
+        const int r = blas.root(desc[t].blas_seg);
+        desc[t].blas_root = r;
+        float rootf;
+        std::memcpy(&rootf, &r, 4);
+        inst[t].b.w = rootf;
+    }
+}
+
 void build_geometry(Geometry& g, const std::vector<Scene*>& scenes, int morton_bits, int layout, cudaStream_t s) {
     RT_REQUIRE(morton_bits == 0 || morton_bits == 30 || morton_bits == 60, "morton_bits must be 0, 30 or 60");
     RT_REQUIRE(layout >= RT_LAYOUT_AUTO && layout <= RT_LAYOUT_SAH, "unknown layout");
@@ -870,11 +883,19 @@ void build_geometry(Geometry& g, const std::vector<Scene*>& scenes, int morton_b
     for (size_t si = 0; si < scenes.size(); ++si) g.optics_seen[si] = scenes[si]->optics_version;
     g.misc.reserve(256);
     flatten_bottom(g, P, s);
-    build_lbvh(g.blas, g.morton_bits, s);   // object space, before the instance boxes are taken
+    // object space, before the instance boxes are taken; binned SAH per mesh
+    build_lbvh(g.blas, g.morton_bits, s, nullptr, nullptr, nullptr, g.layout == RT_LAYOUT_INSTANCED);
+    std::vector<InstDev> inst = P.inst;
+    if (P.ninstances) {   // the bottom roots are known now
+        set_blas_roots(g.blas, g.desc_host, inst);
+        RT_CUDA(cudaMemcpyAsync(g.desc.p, g.desc_host.data(), g.desc_host.size() * sizeof(FlatDesc),
+                                cudaMemcpyHostToDevice, s));
+        RT_CUDA(cudaMemcpyAsync(g.inst.p, inst.data(), inst.size() * sizeof(InstDev), cudaMemcpyHostToDevice, s));
+    }
     flatten_top(g, s);
     const bool grouped = g.layout == RT_LAYOUT_GROUPED;
     build_lbvh(g.top, g.morton_bits, s, grouped ? g.desc.as<FlatDesc>() : nullptr, grouped ? &g.desc_host : nullptr,
-               &g.thing_begin, g.layout == RT_LAYOUT_SAH);
+               &g.thing_begin, g.layout == RT_LAYOUT_SAH || g.layout == RT_LAYOUT_INSTANCED);
     RT_CUDA(cudaEventRecord(e1, s));
     RT_CUDA(cudaEventSynchronize(e1));
     RT_CUDA(cudaEventElapsedTime(&g.build_ms, e0, e1));
@@ -897,9 +918,12 @@ void refit_geometry(Geometry& g, const std::vector<Scene*>& scenes, cudaStream_t
     // transforms only reach the descriptors, instance data and the top level;
     // the bottom level is in object space and stays as built
     g.desc_host = P.desc;
-    RT_CUDA(cudaMemcpyAsync(g.desc.p, P.desc.data(), P.desc.size() * sizeof(FlatDesc), cudaMemcpyHostToDevice, s));
+    std::vector<InstDev> inst = P.inst;
+    set_blas_roots(g.blas, g.desc_host, inst);
+    RT_CUDA(cudaMemcpyAsync(g.desc.p, g.desc_host.data(), g.desc_host.size() * sizeof(FlatDesc),
+                            cudaMemcpyHostToDevice, s));
     RT_CUDA(cudaMemcpyAsync(g.things_dev.p, P.td.data(), P.td.size() * sizeof(ThingDev), cudaMemcpyHostToDevice, s));
-    RT_CUDA(cudaMemcpyAsync(g.inst.p, P.inst.data(), P.inst.size() * sizeof(InstDev), cudaMemcpyHostToDevice, s));
+    RT_CUDA(cudaMemcpyAsync(g.inst.p, inst.data(), inst.size() * sizeof(InstDev), cudaMemcpyHostToDevice, s));
     for (size_t si = 0; si < scenes.size(); ++si) g.optics_seen[si] = scenes[si]->optics_version;
     flatten_top(g, s);
     refit(g.top, s);
