@@ -193,9 +193,10 @@ rt_status rt_scene_set_optics(rt_scene scene, unsigned int thing_id, const rt_op
  *     reference's GAS-per-mesh / IAS-over-things split (optx/rtwo.cxx:138-244)
  *     -- at the cost of a flat traversal step.
  *   INSTANCED: the reference's two-level layout itself: one object-space
- *     LBVH per mesh, a top-level LBVH over instance records, analytic spheres
- *     and the triangles of things that cannot be instanced (non-diagonal
- *     transforms, meshes under 16 triangles); memory-lean, more work per step.
+ *     hierarchy per mesh, a top-level one over instance records, analytic
+ *     spheres and the triangles of things that cannot be instanced
+ *     (non-diagonal transforms, meshes under 16 triangles), both levels built
+ *     like SAH below; memory-lean, more work per step.
  *   SAH (AUTO, the default): the flat world-space hierarchy built top-down
  *     by binned surface-area-heuristic splits (32 bins per axis) down to
  *     clusters of at most 16 primitives, each cluster an LBVH over 30-bit
