@@ -79,6 +79,7 @@ struct WaveState {
     uint32_t iter;           // waves run
     uint32_t max_iter;       // exact upper bound of the waves
     uint32_t err;            // 1: traversal stack overflow, 2: wave bound exceeded
+    uint32_t ext_next[2];    // next unclaimed ray of queue 0 / 1 (persistent traversal)
     unsigned long long next_path, total_paths;
     unsigned long long nodes, prims, rays;
 };
@@ -158,6 +159,7 @@ __global__ void k_init_state(WaveState* st, uint32_t n0, unsigned long long tota
     st->iter = 0;
     st->max_iter = max_iter;
     st->err = 0;
+    st->ext_next[0] = st->ext_next[1] = 0;
     st->next_path = n0;
     st->total_paths = total;
     st->nodes = st->prims = st->rays = 0;
@@ -181,12 +183,11 @@ __global__ void __launch_bounds__(kThreads) k_generate(const JobDev* __restrict_
     }
 }
 
-// One thread per queued ray; kInst selects the two-level traversal.  Two
-// alternatives measured slower on C1: persistent lanes refilled with new rays
-// (active lanes per instruction 12.0 -> 16.6 of 32, but 35% more
-// instructions in an issue-bound kernel) and warp-cooperative traversal with
-// parked leaf tests (active lanes 9.6 -> 12.9, 30% more instructions: 803 vs
-// 993 Mrays/s instanced, 64 spp).
+// One thread per queued ray (the counting pass; rendering uses the persistent
+// k_extend_p below); kInst selects the two-level traversal.  Warp-cooperative
+// traversal with parked leaf tests measured slower (active lanes 9.6 -> 12.9,
+// 30 % more instructions: 803 vs 993 Mrays/s instanced, 64 spp); an earlier
+// persistent form that refilled lanes eagerly cost 35 % more instructions.
 // Writing the hit geometry (point, normal, facing) here instead, so shading
 // needs no gather of the primitive, measured slower on C1 (1146 vs 1216
 // Mrays/s, 64 spp): the shading time did not drop and traversal grew.
@@ -224,6 +225,78 @@ __global__ void __launch_bounds__(kThreads)
         if (lane_id() == 0 && (nvis | ntest)) {
             atomicAdd(&st->nodes, (unsigned long long)nvis);
             atomicAdd(&st->prims, (unsigned long long)ntest);
+        }
+    }
+}
+
+// Persistent traversal: a grid that fills the GPU once, each warp claiming
+// rays of the wave from a counter.  A warp claims new rays for its idle lanes
+// whenever at most kRefillBelow of its lanes are still traversing (checked
+// every kStepsPerCheck steps), so lanes whose rays finish early do not wait
+// for the warp's longest ray.  Same hits as k_extend.  Measured on C1 (64
+// spp, binned-SAH layout, 2070 MHz): one thread per ray 2097 Mrays/s;
+// persistent with (threshold, steps) = (16, 8) 2182, (8, 16) 2282, (12, 16)
+// 2283, (16, 32) 2278, (4, 16) 2259, (24, 8) 2114, (28, 8) 2015 -- and
+// 2135 at the 54 registers the kernel takes unbounded (5 blocks per SM at 48
+// registers are worth a few spilled bytes).
+constexpr uint32_t kRefillBelow = 12;
+constexpr int kStepsPerCheck = 16;
+
+template <bool kInst>
+__global__ void __launch_bounds__(kThreads, kInst ? 4 : 5)
+    k_extend_p(Queues qs, float4* __restrict__ hits, uint32_t* __restrict__ hthing, WaveState* st,
+               const JobDev* __restrict__ jobs, GeoView g) {
+    const uint32_t cur = *((volatile uint32_t*)&st->cur);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {   // the next queue starts empty
+        st->count[cur ^ 1] = 0;
+        st->front[cur ^ 1] = 0;
+        st->back[cur ^ 1] = 0;
+    }
+    const uint32_t n = *((volatile uint32_t*)&st->count[cur]);
+    const Queue Q = pick(qs, cur);
+    const uint32_t lane = lane_id();
+    Trav s;
+    int stack[kStackSize];
+    uint32_t i = 0, nvis = 0, ntest = 0;
+    bool busy = false, drained = false;
+    while (true) {
+        uint32_t bm = __ballot_sync(0xFFFFFFFFu, busy);
+        if (!drained && uint32_t(__popc(bm)) <= kRefillBelow) {
+            const uint32_t idle = ~bm;
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(&st->ext_next[cur], uint32_t(__popc(idle)));
+            base = __shfl_sync(0xFFFFFFFFu, base, 0);
+            if (base + uint32_t(__popc(idle)) >= n) drained = true;
+            if (!busy) {
+                i = base + __popc(idle & ((1u << lane) - 1u));
+                if (i < n) {
+                    const uint32_t q = wave_slot(st, cur, i);
+                    const float4 o4 = Q.ori[q], d4 = Q.dir[q];
+                    const int root = jobs[__float_as_uint(d4.w) >> 8].root;
+                    trav_init(s, xyz(o4), xyz(d4), root);
+                    if (root >= 0) busy = true;
+                    else hits[i] = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));   // empty scene: a miss
+                }
+            }
+            bm = __ballot_sync(0xFFFFFFFFu, busy);
+        }
+        if (bm == 0) {
+            if (drained) break;
+            continue;
+        }
+        if (busy) {
+#pragma unroll 1
+            for (int k = 0; k < kStepsPerCheck; ++k) {
+                if (!trav_step<false, kInst>(s, stack, g, nvis, ntest)) {
+                    const HitRec& h = s.h;
+                    const int ref = !h.hit ? -1 : (h.leaf >= 0 ? h.leaf : -2 - int(h.id));
+                    hits[i] = make_float4(h.t, h.u, h.v, __int_as_float(ref));
+                    if (kInst && ref <= -2) hthing[i] = h.thing;
+                    if (h.overflow) atomicOr(&st->err, 1u);
+                    busy = false;
+                    break;
+                }
+            }
         }
     }
 }
@@ -426,6 +499,7 @@ __global__ void k_wave_ctrl(WaveState* st, cudaGraphConditionalHandle handle, in
     const uint32_t next = cur ^ 1u;
     st->cur = next;
     st->count[next] = st->front[next] + st->back[next];
+    st->ext_next[next] = 0;
     bool more = st->count[next] != 0;
     if (more && st->iter >= st->max_iter) {
         st->err |= 2u;
@@ -625,6 +699,7 @@ bool graph_mode() {
 
 struct WaveLaunch {
     ExtendFn ext_fn;
+    unsigned egrid;    // extend grid (persistent: fills the GPU once)
     unsigned qgrid;
     Queues qs;
     float4* hits;      // t, u, v, hit reference
@@ -637,6 +712,13 @@ struct WaveLaunch {
     Acc acc;
     int any_guides;
 };
+
+// Blocks of a persistent extend kernel: resident blocks per SM x SMs.
+unsigned persistent_grid(ExtendFn fn) {
+    int per_sm = 0;
+    RT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, reinterpret_cast<const void*>(fn), kThreads, 0));
+    return unsigned(std::max(1, per_sm) * sm_count());
+}
 
 void build_wave_graph(Workspace& ws, const WaveLaunch& L) {
     WaveGraph& G = ws.graph;
@@ -658,7 +740,7 @@ void build_wave_graph(Workspace& ws, const WaveLaunch& L) {
     cudaGraphNode_t n_ext, n_shade, n_ctrl;
     void* ext_args[] = {&l.qs, &l.hits, &l.hthing, &l.st, &l.jobs, &l.geo};
     kp.func = reinterpret_cast<void*>(l.ext_fn);
-    kp.gridDim = dim3(l.qgrid);
+    kp.gridDim = dim3(l.egrid);
     kp.blockDim = dim3(kThreads);
     kp.kernelParams = ext_args;
     RT_CUDA(cudaGraphAddKernelNode(&n_ext, body, nullptr, 0, &kp));
@@ -761,9 +843,11 @@ void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s
         L.qs.q[b].gn = any_guides ? ws.q[b][3].as<float4>() : nullptr;
         L.qs.q[b].ga = any_guides ? ws.q[b][4].as<float4>() : nullptr;
     }
-    L.ext_fn = g.ninstances ? (count ? k_extend<true, true> : k_extend<false, true>)
-                            : (count ? k_extend<true, false> : k_extend<false, false>);
+    // the counting pass keeps one thread per ray (its counts are per-ray sums)
+    L.ext_fn = g.ninstances ? (count ? k_extend<true, true> : k_extend_p<true>)
+                            : (count ? k_extend<true, false> : k_extend_p<false>);
     L.qgrid = grid_for(W);
+    L.egrid = count ? L.qgrid : persistent_grid(L.ext_fn);
     L.hits = ws.hits.as<float4>();
     L.hthing = ws.hthing.as<uint32_t>();
     L.st = ws.state.as<WaveState>();
@@ -793,6 +877,7 @@ void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s
     if (use_graph) {
         const std::vector<const void*> key = {
             reinterpret_cast<const void*>(L.ext_fn), reinterpret_cast<const void*>(uintptr_t(L.qgrid)),
+            reinterpret_cast<const void*>(uintptr_t(L.egrid)),
             L.qs.q[0].ori, L.qs.q[0].gn, L.qs.q[1].ori, L.qs.q[1].gn, L.hits, L.hthing, L.st, L.jobs,
             reinterpret_cast<const void*>(uintptr_t(nj)), L.geo.tnodes, L.geo.tprims, L.geo.bnodes, L.geo.bprims,
             L.geo.inst, L.geo.desc, L.things, L.acc.col[0], L.acc.gd[0], reinterpret_cast<const void*>(uintptr_t(total_pix)),
@@ -814,7 +899,7 @@ void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s
                     timed.push_back({ev, 0});
                     ev += 2;
                 }
-                RT_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(L.ext_fn), dim3(L.qgrid), dim3(kThreads),
+                RT_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(L.ext_fn), dim3(L.egrid), dim3(kThreads),
                                          ext_args, 0, s));
                 if (stage_timing) {
                     RT_CUDA(cudaEventRecord(ws.event(ev - 1), s));
