@@ -289,7 +289,9 @@ __global__ void k_adjoint_pixel_g(const AdjJob* __restrict__ jobs, uint32_t nj, 
 }
 
 // One block: kAdjPathsPerBlock consecutive global paths, thread-strided.
-// Four resident blocks per SM cap the registers at 128 per thread.
+// Four resident blocks per SM cap the registers at 128 per thread.  Lanes
+// claiming their warp's next path from a shared counter as soon as they finish
+// (instead of the fixed stride) measured 2 % slower (3.60 vs 3.52 ms, C3).
 __global__ void __launch_bounds__(kAdjThreads, 4)
     k_adjoint(const AdjJob* __restrict__ jobs, uint32_t nj, unsigned long long total, GeoView geo,
               const ThingDev* __restrict__ things, const float* __restrict__ gpix, double* G, uint32_t nthings_total,
