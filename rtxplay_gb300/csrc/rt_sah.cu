@@ -73,7 +73,7 @@ struct SahSplit {
 };
 
 struct SahCounters {
-    uint32_t nbig[2], nblock[2], nwarp[2];   // node lists, by level parity
+    uint32_t next[2][3];   // node lists by level parity: big, block, warp nodes
     uint32_t ncl, nchunks, err;
 };
 
@@ -190,9 +190,10 @@ __global__ void k_sah_prepare(SahNode* __restrict__ nodes, uint32_t nact, const 
 // the node's bins; the chunk's bin counts kept for the partition offsets.
 __global__ void __launch_bounds__(kSahThreads)
     k_sah_bin(const SahRec* __restrict__ recs, const SahNode* __restrict__ nodes, uint32_t nact,
-              uint32_t* __restrict__ bins, uint32_t* __restrict__ chunk_counts) {
+              uint32_t* __restrict__ bins, uint32_t* __restrict__ chunk_counts, const SahCounters* ctr) {
     __shared__ uint32_t sb[kBinTotal];
     const uint32_t c = blockIdx.x;
+    if (c >= *((volatile uint32_t*)&ctr->nchunks)) return;   // the grid is an upper bound
     const uint32_t ni = node_of_chunk(nodes, nact, c);
     const SahNode& nd = nodes[ni];
     const uint32_t b = nd.start + (c - nd.chunk0) * kSahChunk;
@@ -296,8 +297,7 @@ __device__ __forceinline__ int child_kind(uint32_t count, uint32_t cluster_max) 
 }
 
 __device__ __forceinline__ uint32_t* kind_counter(int kind, const SahOut& out) {
-    return kind == kBig ? &out.ctr->nbig[out.nx] : kind == kBlock ? &out.ctr->nblock[out.nx]
-                         : kind == kWarp ? &out.ctr->nwarp[out.nx] : &out.ctr->ncl;
+    return kind == kCluster ? &out.ctr->ncl : &out.ctr->next[out.nx][kind];
 }
 
 // Records split `sid` of node nd (left part nleft records) and its children,
@@ -390,10 +390,15 @@ __global__ void k_sah_split(SahNode* __restrict__ nodes, uint32_t nact, const ui
 // Left records of every chunk of the big nodes (one thread per chunk); an
 // exclusive scan over all chunks minus its value at the node's first chunk
 // gives the left records before a chunk inside its node.
-__global__ void k_sah_chunk_left(const SahNode* __restrict__ nodes, uint32_t nact, uint32_t nchunks,
-                                 const uint32_t* __restrict__ chunk_counts, uint32_t* __restrict__ chunk_left) {
+__global__ void k_sah_chunk_left(const SahNode* __restrict__ nodes, uint32_t nact, uint32_t bound,
+                                 const uint32_t* __restrict__ chunk_counts, uint32_t* __restrict__ chunk_left,
+                                 const SahCounters* ctr) {
     const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= nchunks) return;
+    if (c >= bound) return;
+    if (c >= ctr->nchunks) {   // past the level's chunks: zero, so the scan can run over the bound
+        chunk_left[c] = 0;
+        return;
+    }
     const SahNode& nd = nodes[node_of_chunk(nodes, nact, c)];
     uint32_t l = 0;
     if (nd.axis >= 0) {
@@ -483,6 +488,7 @@ __global__ void __launch_bounds__(kSahThreads)
     __shared__ uint32_t s_warp[kSahThreads / 32];
     __shared__ uint32_t s_cb[12];
     const uint32_t c = blockIdx.x;
+    if (c >= *((volatile uint32_t*)&out.ctr->nchunks)) return;   // the grid is an upper bound
     const uint32_t ni = node_of_chunk(nodes, nact, c);
     const SahNode& nd = nodes[ni];
     const uint32_t b = nd.start + (c - nd.chunk0) * kSahChunk;
@@ -810,9 +816,9 @@ void build_sah_topology(Lbvh& L, uint32_t cluster_max, cudaStream_t s) {
     layout(scratch.as<char>());
 
     SahCounters c0{};
-    c0.nbig[0] = uint32_t(seed_big.size());
-    c0.nblock[0] = uint32_t(seed_block.size());
-    c0.nwarp[0] = uint32_t(seed_warp.size());
+    c0.next[0][kBig] = uint32_t(seed_big.size());
+    c0.next[0][kBlock] = uint32_t(seed_block.size());
+    c0.next[0][kWarp] = uint32_t(seed_warp.size());
     c0.ncl = uint32_t(seed_cl.size());
     RT_CUDA(cudaMemcpyAsync(ctr, &c0, sizeof c0, cudaMemcpyHostToDevice, s));
     if (!seed_big.empty())
@@ -830,16 +836,14 @@ void build_sah_topology(Lbvh& L, uint32_t cluster_max, cudaStream_t s) {
     k_sah_records<<<(n + kSahThreads - 1) / kSahThreads, kSahThreads, 0, s>>>(L.prims_flat.as<float4>(), n, rec[0],
                                                                                out_ids);
     RT_CHECK_LAUNCH();
-    uint32_t nb = c0.nbig[0], nbl = c0.nblock[0], nw = c0.nwarp[0];
+    uint32_t nb = c0.next[0][kBig], nbl = c0.next[0][kBlock], nw = c0.next[0][kWarp];
     uint32_t nsplit = 0;   // one split per node of every level, ids in level order
     int cur = 0, level = 0;
     SahCounters hc{};
     for (; nb + nbl + nw > 0; ++level) {
         RT_REQUIRE(nb <= max_big && nbl <= max_nodes && nw <= max_nodes, "internal: SAH level overflow");
         const uint32_t nx = uint32_t(cur ^ 1);
-        RT_CUDA(cudaMemsetAsync(&ctr->nbig[nx], 0, 4, s));
-        RT_CUDA(cudaMemsetAsync(&ctr->nblock[nx], 0, 4, s));
-        RT_CUDA(cudaMemsetAsync(&ctr->nwarp[nx], 0, 4, s));
+        RT_CUDA(cudaMemsetAsync(ctr->next[nx], 0, sizeof(ctr->next[nx]), s));
         const SahOut out{big[nx], block[nx], warp[nx], clusters, splits, ctr, nx, cluster_max};
         const int median_only = level >= kSahMaxLevels ? 1 : 0;
         if (nb) {
@@ -852,19 +856,18 @@ void build_sah_topology(Lbvh& L, uint32_t cluster_max, cudaStream_t s) {
             k_sah_prepare<<<std::max(prep_blocks, (nb + kSahThreads - 1) / kSahThreads), kSahThreads, 0, s>>>(
                 nodes, nb, chunk0, ctr, bins);
             RT_CHECK_LAUNCH();
-            RT_CUDA(cudaMemcpyAsync(&hc, ctr, sizeof hc, cudaMemcpyDeviceToHost, s));
-            RT_CUDA(cudaStreamSynchronize(s));
-            const uint32_t nchunks = hc.nchunks;
-            RT_REQUIRE(nchunks <= max_chunks, "internal: SAH chunk overflow");
-            k_sah_bin<<<nchunks, kSahThreads, 0, s>>>(rec[cur], nodes, nb, bins, chunk_counts);
+            // chunks of the level: at most one per kSahChunk records plus one per node
+            // (the device holds the exact count; surplus blocks return at once)
+            const uint32_t bound = n / kSahChunk + nb + 1;
+            k_sah_bin<<<bound, kSahThreads, 0, s>>>(rec[cur], nodes, nb, bins, chunk_counts, ctr);
             RT_CHECK_LAUNCH();
             k_sah_split<<<(nb * 32 + 127) / 128, 128, 0, s>>>(nodes, nb, bins, out, nsplit, median_only);
             RT_CHECK_LAUNCH();
-            k_sah_chunk_left<<<(nchunks + kSahThreads - 1) / kSahThreads, kSahThreads, 0, s>>>(nodes, nb, nchunks,
-                                                                                             chunk_counts, chunk_left);
+            k_sah_chunk_left<<<(bound + kSahThreads - 1) / kSahThreads, kSahThreads, 0, s>>>(nodes, nb, bound,
+                                                                                           chunk_counts, chunk_left, ctr);
             RT_CHECK_LAUNCH();
-            scan_exclusive_u32(chunk_left, chunk_scan, nchunks, L.sort_tmp, s);
-            k_sah_partition<<<nchunks, kSahThreads, 0, s>>>(rec[cur], rec[nx], nodes, nb, chunk_scan, out_ids, out);
+            scan_exclusive_u32(chunk_left, chunk_scan, bound, L.sort_tmp, s);
+            k_sah_partition<<<bound, kSahThreads, 0, s>>>(rec[cur], rec[nx], nodes, nb, chunk_scan, out_ids, out);
             RT_CHECK_LAUNCH();
         }
         if (nbl) {
@@ -882,9 +885,9 @@ void build_sah_topology(Lbvh& L, uint32_t cluster_max, cudaStream_t s) {
         RT_CUDA(cudaStreamSynchronize(s));
         if (hc.err) throw Error(RT_ERR_INTERNAL, "SAH build: partition and binning disagree");
         nsplit += nb + nbl + nw;
-        nb = hc.nbig[nx];
-        nbl = hc.nblock[nx];
-        nw = hc.nwarp[nx];
+        nb = hc.next[nx][kBig];
+        nbl = hc.next[nx][kBlock];
+        nw = hc.next[nx][kWarp];
         cur ^= 1;
     }
     if (level == 0) {   // no node above the cluster size: the seed clusters only
