@@ -85,9 +85,9 @@ struct WaveState {
 };
 
 struct Queue {
-    float4* ori;   // origin.xyz, job-local path id
+    float4* ori;   // origin.xyz, job-local pixel
     float4* dir;   // direction.xyz, (job << 8) | bounce
-    float4* thr;   // throughput.rgb
+    float4* thr;   // throughput.rgb, sample
     float4* gn;    // guide normal (guides only)
     float4* ga;    // guide albedo (guides only)
 };
@@ -126,15 +126,16 @@ __device__ __forceinline__ uint32_t job_of_pixel(const JobDev* __restrict__ jobs
     return lo;
 }
 
-// Camera ray of job-local path pid (pixel-major: pid = pixel * spp + sample).
-// Consecutive paths are samples of one pixel, so the fresh rays of a block
+// Camera ray of a job's pixel and sample.  Paths are numbered pixel-major
+// (path = pixel * spp + sample; the queues carry pixel and sample, so shading
+// divides once per path, not once per ray).  Consecutive paths are samples of
+// one pixel, so the fresh rays of a block
 // start inside one pixel footprint and their bounces leave from nearby points:
 // measured on C1 (64 spp) against sample-major numbering, traversal -16 % and
 // shading -22 % (1888 vs 1566 Mrays/s); the image does not change (every
 // random number is keyed by pixel and sample).
-__device__ __forceinline__ void make_camera_ray(const JobDev& j, uint32_t pid, float3& o, float3& d) {
-    const uint32_t pixel = pid / j.spp;
-    const uint32_t sample = pid % j.spp;
+__device__ __forceinline__ void make_camera_ray(const JobDev& j, uint32_t pixel, uint32_t sample, float3& o,
+                                                float3& d) {
     Stream s(j.seed, j.key1, pixel, sample, 0);
     camera_ray(j.cam, pixel % j.W, pixel / j.W, j.W, j.H, s, o, d);
 }
@@ -172,11 +173,12 @@ __global__ void __launch_bounds__(kThreads) k_generate(const JobDev* __restrict_
     const uint32_t jx = job_of_path(jobs, nj, i);
     const JobDev& j = jobs[jx];
     const uint32_t pid = uint32_t(i - j.path_offset);
+    const uint32_t pixel = pid / j.spp, sample = pid % j.spp;
     float3 o, d;
-    make_camera_ray(j, pid, o, d);
-    q.ori[i] = make_float4(o.x, o.y, o.z, __uint_as_float(pid));
+    make_camera_ray(j, pixel, sample, o, d);
+    q.ori[i] = make_float4(o.x, o.y, o.z, __uint_as_float(pixel));
     q.dir[i] = make_float4(d.x, d.y, d.z, __uint_as_float(jx << 8));
-    q.thr[i] = make_float4(1.f, 1.f, 1.f, 0.f);
+    q.thr[i] = make_float4(1.f, 1.f, 1.f, __uint_as_float(sample));
     if (any_guides) {
         q.gn[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         q.ga[i] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -335,11 +337,12 @@ __global__ void __launch_bounds__(kThreads, 4)
     unsigned long long a_px = ~0ull, a_r = 0, a_g = 0, a_b = 0, a_n = 0;
     float3 no{}, nd{}, nthr{};
     float3 gN{}, gA{};
-    uint32_t pid = 0, bounce = 0, jx = 0;
+    uint32_t pixel = 0, sample = 0, bounce = 0, jx = 0;
     if (active) {
         const uint32_t q = wave_slot(st, cur, i);
         const float4 o4 = Q.ori[q], d4 = Q.dir[q], t4 = Q.thr[q], h4 = hits[i];
-        pid = __float_as_uint(o4.w);
+        pixel = __float_as_uint(o4.w);
+        sample = __float_as_uint(t4.w);
         const uint32_t tag = __float_as_uint(d4.w);
         jx = tag >> 8;
         bounce = tag & 0xFFu;
@@ -358,7 +361,7 @@ __global__ void __launch_bounds__(kThreads, 4)
         } else if (bounce + 1 >= j.depth) {
             ended = true;   // black at the depth limit (optx/optics_r.cu:34-42)
         } else {
-            Stream s(j.seed, j.key1, pid / j.spp, pid % j.spp, bounce + 1);
+            Stream s(j.seed, j.key1, pixel, sample, bounce + 1);
             float4 pa, pb, pc;
             if (ref >= 0) {   // the world-space record itself
                 pa = __ldg(tprims + 3 * ref);
@@ -380,7 +383,7 @@ __global__ void __launch_bounds__(kThreads, 4)
             }
         }
         if (ended) {
-            const size_t px = size_t(j.pix_offset) + pid / j.spp;
+            const size_t px = size_t(j.pix_offset) + pixel;
             a_px = px;
             a_r = fx_q(color.x);
             a_g = fx_q(color.y);
@@ -441,8 +444,10 @@ __global__ void __launch_bounds__(kThreads, 4)
             if (g < st->total_paths) {
                 jx = job_of_path(jobs, nj, g);
                 const JobDev& j = jobs[jx];
-                pid = uint32_t(g - j.path_offset);
-                make_camera_ray(j, pid, no, nd);
+                const uint32_t pid = uint32_t(g - j.path_offset);
+                pixel = pid / j.spp;
+                sample = pid % j.spp;
+                make_camera_ray(j, pixel, sample, no, nd);
                 nthr = mk(1.f, 1.f, 1.f);
                 gN = mk(0.f, 0.f, 0.f);
                 gA = mk(0.f, 0.f, 0.f);
@@ -479,9 +484,9 @@ __global__ void __launch_bounds__(kThreads, 4)
             const uint32_t lt = (1u << lane) - 1u;
             const uint32_t slot = cont ? uint32_t(s_base) + s_warp[warp] + __popc(pc & lt)
                                        : st->cap - 1u - (uint32_t(s_base2) + s_warp2[warp] + __popc(pf & lt));
-            N.ori[slot] = make_float4(no.x, no.y, no.z, __uint_as_float(pid));
+            N.ori[slot] = make_float4(no.x, no.y, no.z, __uint_as_float(pixel));
             N.dir[slot] = make_float4(nd.x, nd.y, nd.z, __uint_as_float((jx << 8) | bounce));
-            N.thr[slot] = make_float4(nthr.x, nthr.y, nthr.z, 0.f);
+            N.thr[slot] = make_float4(nthr.x, nthr.y, nthr.z, __uint_as_float(sample));
             if (any_guides) {
                 N.gn[slot] = make_float4(gN.x, gN.y, gN.z, 0.f);
                 N.ga[slot] = make_float4(gA.x, gA.y, gA.z, 0.f);
