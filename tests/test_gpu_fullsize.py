@@ -102,3 +102,19 @@ def test_c1_render_subset_bit_exact_and_properties(product, oracle, cuda, c1):
     ref = wd.render(oracle_camera(O, cam), W, H, spp, 50, 4711, pixels=pix, guides=False)
     assert np.array_equal(raw[pix].view(np.uint32), ref["rawRGB"].view(np.uint32))
     assert np.array_equal(rpp[pix], ref["rpp"])
+
+
+def test_c1_full_frame_bit_exact(product, oracle, cuda, c1):
+    """Every pixel of the benchmark frame (1200x800, 4 spp, depth 50) equals
+    the oracle's: colour bits and rays per pixel; sRGB bytes within one step."""
+    R, O = product, oracle
+    sc, wd = c1
+    spp = 4
+    cam = R.rtow_camera(W, H)
+    out = R.render(sc, cam, R.launch_params(W, H, spp, depth=50, seed=2024))
+    ref = wd.render(oracle_camera(O, cam), W, H, spp, 50, 2024, guides=False)
+    assert np.array_equal(out["rawRGB"].view(np.uint32), ref["rawRGB"].view(np.uint32))
+    assert np.array_equal(out["rpp"], ref["rpp"])
+    # sRGB: powf on the device against glibc's on the host, within one step
+    diff = np.abs(out["image"][:, :3].astype(int) - O.pp("srgb", ref["rawRGB"], W, H)[:, :3].astype(int))
+    assert diff.max() <= 1 and (diff > 0).mean() < 1e-2
