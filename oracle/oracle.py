@@ -78,6 +78,8 @@ def lib():
         L.orc_world_build.restype = ctypes.c_int
         L.orc_world_build_grouped.argtypes = [ctypes.c_void_p]
         L.orc_world_build_grouped.restype = ctypes.c_int
+        L.orc_world_build_sah.argtypes = [ctypes.c_void_p, ctypes.c_uint]
+        L.orc_world_build_sah.restype = ctypes.c_int
         L.orc_world_nprims.argtypes = [ctypes.c_void_p]
         L.orc_world_nprims.restype = ctypes.c_uint
         L.orc_world_lbvh.argtypes = [ctypes.c_void_p] + [ctypes.c_void_p] * 7
@@ -230,8 +232,12 @@ class World:
     def set_transform(self, thing, transform):
         return lib().orc_world_set_transform(self._w, thing, np.asarray(transform, np.float32))
 
-    def build(self, morton_bits=60, grouped=False):
-        if grouped:
+    def build(self, morton_bits=60, grouped=False, sah_cluster=0):
+        """Flat LBVH (30/60-bit Morton), things-grouped keys, or (sah_cluster > 0)
+        the binned-SAH hierarchy with clusters of at most sah_cluster records."""
+        if sah_cluster:
+            assert lib().orc_world_build_sah(self._w, sah_cluster) == 0
+        elif grouped:
             assert lib().orc_world_build_grouped(self._w) == 0
         else:
             assert lib().orc_world_build(self._w, morton_bits) == 0
@@ -333,7 +339,7 @@ def pp(kind, raw, w, h):
     return dst.reshape(h * w, 4)
 
 
-def rtow_world(level=None, rng_kind=0, seed=1, half_extent=11, morton_bits=60, grouped=False):
+def rtow_world(level=None, rng_kind=0, seed=1, half_extent=11, morton_bits=60, grouped=False, sah_cluster=0):
     """The final scene as analytic spheres (level None) or as spheres
     tessellated at `level` and instanced by their 3x4 transform."""
     sc = scene_rtow(rng_kind, seed, half_extent)
@@ -349,5 +355,5 @@ def rtow_world(level=None, rng_kind=0, seed=1, half_extent=11, morton_bits=60, g
         else:
             T = np.array([r, 0, 0, c[0], 0, r, 0, c[1], 0, 0, r, c[2]], np.float32)
             w.add_thing(int(t), a, float(f), float(ix), mesh, T)
-    w.build(morton_bits, grouped)
+    w.build(morton_bits, grouped, sah_cluster)
     return w, sc

@@ -379,6 +379,7 @@ struct orc_world {
     std::vector<uint32_t> order;         // sorted prim ids
     int morton_bits = 60;
     bool grouped = false;                // things-grouped keys (rank of the thing, then a code inside it)
+    unsigned sah_cluster = 0;            // > 0: binned-SAH hierarchy with clusters of at most this many records
     std::vector<int32_t> left, right;
     std::vector<Box> cbox0, cbox1;       // per internal node: child boxes
     F3 clo{0, 0, 0}, chi{0, 0, 0};
@@ -421,6 +422,180 @@ void flatten(orc_world& w) {
     }
 }
 
+void build_lbvh_topology(orc_world& w, const std::vector<Box>& pb, const std::vector<F3>& cen, F3 lo, F3 hi);
+void refit_tree(orc_world& w, const std::vector<Box>& pb);
+
+// ---- binned-SAH hierarchy (the product's RT_LAYOUT_SAH, rt_sah.cu) --------
+// Top-down over record positions: a node of more than cluster_max records is
+// binned (32 bins per axis over its centroid bounds: bin = int((c - lo) *
+// (32 / extent)) clamped to [0, 31]), split at the border of least cost
+// A(left) * n(left) + A(right) * n(right) (A = 2 (dx dy + dy dz + dz dx);
+// ties: the lower axis, then the lower border; no border with records on
+// both sides, or depth >= 64: the median position) and partitioned stably.
+// Smaller nodes are clusters: keys cluster << 30 | 30-bit Morton code inside
+// the cluster's centroid bounds, a Karras hierarchy per cluster, and each
+// split node in slot split - 1 (the spare slot of the cluster ending there).
+constexpr int kSahBins = 32;
+constexpr int kSahMaxLevels = 64;
+
+inline float sah_area(const Box& b) {
+    const float dx = fmaxf(b.hi.x - b.lo.x, 0.f), dy = fmaxf(b.hi.y - b.lo.y, 0.f), dz = fmaxf(b.hi.z - b.lo.z, 0.f);
+    return 2.f * (dx * dy + dy * dz + dz * dx);
+}
+
+inline int sah_bin(float c, float lo, float scale) {
+    const float f = (c - lo) * scale;
+    if (!(f > 0.f)) return 0;
+    if (f >= float(kSahBins)) return kSahBins - 1;
+    return int(f);
+}
+
+struct SahBuild {
+    const std::vector<Box>& pb;
+    const std::vector<F3>& cen;
+    std::vector<uint32_t> perm;          // record ids by position
+    unsigned cluster_max;
+    struct Split { int start, split, end, child[2]; };
+    struct Cluster { int start, count; F3 lo, hi; };
+    std::vector<Split> splits;
+    std::vector<Cluster> clusters;
+
+    void bounds(int b, int e, F3& lo, F3& hi) const {
+        const float inf = std::numeric_limits<float>::infinity();
+        lo = mk(inf, inf, inf);
+        hi = mk(-inf, -inf, -inf);
+        for (int i = b; i < e; ++i) {
+            const F3 c = cen[perm[i]];
+            lo = mk(fminf(lo.x, c.x), fminf(lo.y, c.y), fminf(lo.z, c.z));
+            hi = mk(fmaxf(hi.x, c.x), fmaxf(hi.y, c.y), fmaxf(hi.z, c.z));
+        }
+    }
+
+    // Returns the child reference of node [b, b + count): split index (>= 0)
+    // or ~cluster index.
+    int node(int b, int count, int level) {
+        F3 lo, hi;
+        bounds(b, b + count, lo, hi);
+        if (unsigned(count) <= cluster_max) {
+            clusters.push_back(Cluster{b, count, lo, hi});
+            return ~int(clusters.size() - 1);
+        }
+        const float clo[3] = {lo.x, lo.y, lo.z}, chi[3] = {hi.x, hi.y, hi.z};
+        float scale[3];
+        for (int a = 0; a < 3; ++a) {
+            const float ext = chi[a] - clo[a];
+            scale[a] = ext > 0.f ? float(kSahBins) / ext : 0.f;
+        }
+        int axis = -1, border = 0, nleft = count / 2;
+        if (level < kSahMaxLevels) {
+            float best = std::numeric_limits<float>::infinity();
+            const float inf = std::numeric_limits<float>::infinity();
+            for (int a = 0; a < 3; ++a) {
+                Box bb[kSahBins];
+                int cnt[kSahBins] = {};
+                for (int k = 0; k < kSahBins; ++k) bb[k] = Box{mk(inf, inf, inf), mk(-inf, -inf, -inf)};
+                for (int i = b; i < b + count; ++i) {
+                    const uint32_t r = perm[i];
+                    const float c = a == 0 ? cen[r].x : a == 1 ? cen[r].y : cen[r].z;
+                    const int k = sah_bin(c, clo[a], scale[a]);
+                    bb[k] = unite(bb[k], pb[r]);
+                    cnt[k] += 1;
+                }
+                Box pre[kSahBins], suf[kSahBins];
+                int pc[kSahBins], sc[kSahBins];
+                for (int k = 0; k < kSahBins; ++k) {
+                    pre[k] = k ? unite(pre[k - 1], bb[k]) : bb[k];
+                    pc[k] = (k ? pc[k - 1] : 0) + cnt[k];
+                }
+                for (int k = kSahBins - 1; k >= 0; --k) {
+                    suf[k] = k + 1 < kSahBins ? unite(suf[k + 1], bb[k]) : bb[k];
+                    sc[k] = (k + 1 < kSahBins ? sc[k + 1] : 0) + cnt[k];
+                }
+                for (int k = 0; k + 1 < kSahBins; ++k) {   // border k + 1
+                    if (pc[k] == 0 || sc[k + 1] == 0) continue;
+                    const float cost = sah_area(pre[k]) * float(pc[k]) + sah_area(suf[k + 1]) * float(sc[k + 1]);
+                    if (cost < best) {
+                        best = cost;
+                        axis = a;
+                        border = k + 1;
+                        nleft = pc[k];
+                    }
+                }
+            }
+        }
+        if (axis >= 0) {   // stable partition by bin < border
+            std::vector<uint32_t> L, R;
+            for (int i = b; i < b + count; ++i) {
+                const uint32_t r = perm[i];
+                const float c = axis == 0 ? cen[r].x : axis == 1 ? cen[r].y : cen[r].z;
+                (sah_bin(c, clo[axis], scale[axis]) < border ? L : R).push_back(r);
+            }
+            std::copy(L.begin(), L.end(), perm.begin() + b);
+            std::copy(R.begin(), R.end(), perm.begin() + b + int(L.size()));
+        }
+        const int id = int(splits.size());
+        splits.push_back(Split{b, b + nleft, b + count, {0, 0}});
+        const int c0 = node(b, nleft, level + 1);
+        const int c1 = node(b + nleft, count - nleft, level + 1);
+        splits[id].child[0] = c0;
+        splits[id].child[1] = c1;
+        return id;
+    }
+};
+
+void build_sah(orc_world& w, const std::vector<Box>& pb, const std::vector<F3>& cen) {
+    const int n = int(pb.size());
+    SahBuild sb{pb, cen, {}, w.sah_cluster, {}, {}};
+    sb.perm.resize(n);
+    std::iota(sb.perm.begin(), sb.perm.end(), 0u);
+    const int top = n ? sb.node(0, n, 0) : ~0;
+    // clusters in position order; keys cluster << 30 | local Morton code; stable sort
+    std::vector<int> rank(sb.clusters.size());
+    std::vector<int> by_pos(sb.clusters.size());
+    std::iota(by_pos.begin(), by_pos.end(), 0);
+    std::sort(by_pos.begin(), by_pos.end(), [&](int x, int y) { return sb.clusters[x].start < sb.clusters[y].start; });
+    for (size_t r = 0; r < by_pos.size(); ++r) rank[by_pos[r]] = int(r);
+    std::vector<uint64_t> code(n);
+    std::vector<uint32_t> ids(n);
+    for (const auto& c : sb.clusters) {
+        const F3 e = sub(c.hi, c.lo);
+        const int r = rank[&c - &sb.clusters[0]];
+        for (int i = c.start; i < c.start + c.count; ++i) {
+            const F3 q = cen[sb.perm[i]];
+            const uint32_t qx = quant10(q.x, c.lo.x, e.x), qy = quant10(q.y, c.lo.y, e.y), qz = quant10(q.z, c.lo.z, e.z);
+            code[i] = (uint64_t(r) << 30) | ((expand10(qx) << 2) | (expand10(qy) << 1) | expand10(qz));
+            ids[i] = sb.perm[i];
+        }
+    }
+    orc_stable_sort_pairs64(code.data(), ids.data(), unsigned(n));
+    w.codes = code;
+    w.order = ids;
+    w.left.assign(n > 1 ? n - 1 : 0, 0);
+    w.right.assign(n > 1 ? n - 1 : 0, 0);
+    std::vector<int32_t> L, R;
+    for (const auto& c : sb.clusters) {   // Karras per cluster, slots start + i
+        if (c.count < 2) continue;
+        L.assign(c.count - 1, 0);
+        R.assign(c.count - 1, 0);
+        karras(code.data() + c.start, c.count, L.data(), R.data());
+        auto g = [&](int32_t x) { return x >= 0 ? c.start + x : ~(c.start + ~x); };
+        for (int i = 0; i < c.count - 1; ++i) {
+            w.left[c.start + i] = g(L[i]);
+            w.right[c.start + i] = g(R[i]);
+        }
+    }
+    auto ref = [&](int x) {   // split -> its slot; cluster -> its root slot, or its single record
+        if (x >= 0) return sb.splits[x].split - 1;
+        const auto& c = sb.clusters[~x];
+        return c.count >= 2 ? c.start : ~c.start;
+    };
+    for (const auto& sp : sb.splits) {
+        w.left[sp.split - 1] = ref(sp.child[0]);
+        w.right[sp.split - 1] = ref(sp.child[1]);
+    }
+    w.root = n > 1 ? ref(top) : ~0;
+}
+
 void build_lbvh(orc_world& w) {
     const int n = int(w.prims.size());
     std::vector<Box> pb(n);
@@ -436,6 +611,17 @@ void build_lbvh(orc_world& w) {
         hi = mk(fmaxf(hi.x, cen[i].x), fmaxf(hi.y, cen[i].y), fmaxf(hi.z, cen[i].z));
     }
     w.clo = lo; w.chi = hi;
+    if (w.sah_cluster > 0) {
+        build_sah(w, pb, cen);
+    } else {
+        build_lbvh_topology(w, pb, cen, lo, hi);
+    }
+    refit_tree(w, pb);
+    w.built = true;
+}
+
+void build_lbvh_topology(orc_world& w, const std::vector<Box>& pb, const std::vector<F3>& cen, F3 lo, F3 hi) {
+    const int n = int(pb.size());
     std::vector<uint64_t> code(n);
     std::vector<uint32_t> ids(n);
     const float lo3[3] = {lo.x, lo.y, lo.z}, hi3[3] = {hi.x, hi.y, hi.z};
@@ -525,7 +711,11 @@ void build_lbvh(orc_world& w) {
             w.root = spare(0);
         }
     }
-    // bottom-up refit (post order, iterative)
+}
+
+// Bottom-up refit of the child boxes (post order, iterative).
+void refit_tree(orc_world& w, const std::vector<Box>& pb) {
+    const int n = int(pb.size());
     w.cbox0.assign(n > 1 ? n - 1 : 0, Box{});
     w.cbox1.assign(n > 1 ? n - 1 : 0, Box{});
     if (n > 1) {
@@ -555,7 +745,6 @@ void build_lbvh(orc_world& w) {
             nb[i] = unite(b0, b1);
         }
     }
-    w.built = true;
 }
 
 inline bool prim_hit(const Prim& p, F3 o, F3 d, float& t, float& u, float& v) {
@@ -1194,6 +1383,7 @@ int orc_world_build(orc_world* w, int morton_bits) {
     if (morton_bits != 30 && morton_bits != 60) return -1;
     w->morton_bits = morton_bits;
     w->grouped = false;
+    w->sah_cluster = 0;
     flatten(*w);
     build_lbvh(*w);
     return 0;
@@ -1202,6 +1392,17 @@ int orc_world_build(orc_world* w, int morton_bits) {
 int orc_world_build_grouped(orc_world* w) {
     w->morton_bits = 60;
     w->grouped = true;
+    w->sah_cluster = 0;
+    flatten(*w);
+    build_lbvh(*w);
+    return 0;
+}
+
+int orc_world_build_sah(orc_world* w, unsigned cluster_max) {
+    if (cluster_max < 1) return -1;
+    w->morton_bits = 60;
+    w->grouped = false;
+    w->sah_cluster = cluster_max;
     flatten(*w);
     build_lbvh(*w);
     return 0;

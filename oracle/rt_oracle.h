@@ -79,6 +79,11 @@ int orc_world_build(orc_world* w, int morton_bits);
  * their centroid-bounds centre, key = rank << 30 | 30-bit code inside the
  * thing's centroid bounds (the product's RT_LAYOUT_GROUPED). */
 int orc_world_build_grouped(orc_world* w);
+/* The same world under the binned-SAH hierarchy of the product's
+ * RT_LAYOUT_SAH (binned surface-area splits down to clusters of at most
+ * cluster_max records, a Karras hierarchy per cluster over local 30-bit
+ * codes, split nodes stitched into the clusters' spare slots). */
+int orc_world_build_sah(orc_world* w, unsigned cluster_max);
 unsigned orc_world_nprims(const orc_world* w);
 /* Copies out the LBVH: codes[n] (sorted), ids[n] (sorted prim ids), left/right[n-1],
  * boxes[(n-1)*12] (child0 lo,hi then child1 lo,hi per internal node), scene

@@ -214,3 +214,18 @@ def test_sah_update_refits_and_rebuilds(product, oracle, cuda):
     _check_tree(sc.lbvh(), wd.triangles())
     cam = R.rtow_camera(160, 96)
     _first_hits_match(R, O, cuda, sc, wd, cam, 160, 96)
+
+
+@pytest.mark.parametrize("level", [None, 2, 3])
+@pytest.mark.parametrize("cluster", [1, 16, 2048])
+def test_sah_bit_exact_vs_oracle_twin(product, oracle, cuda, sah_cluster, level, cluster):
+    """The GPU's binned-SAH hierarchy equals the oracle's restatement node for
+    node: cluster-local keys, record order, children and refit boxes."""
+    R, O = product, oracle
+    sah_cluster(cluster)
+    sc = R.rtow_scene(level, layout=R.RT_LAYOUT_SAH)
+    wd, _ = O.rtow_world(level, sah_cluster=cluster)
+    a, b = sc.lbvh(), wd.lbvh()
+    for k in ("codes", "ids", "left", "right"):
+        assert np.array_equal(a[k], b[k]), k
+    assert np.array_equal(a["boxes"].view(np.uint32), b["boxes"].view(np.uint32))
