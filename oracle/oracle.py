@@ -1,7 +1,7 @@
 """ctypes wrapper of the CPU oracle (``oracle/_build/liboracle.so``).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, ``__graft_entry__.smoke()`` and
-bench.py's CPU-baseline leg, as the checker.  The product package
+bench.py's CPU-baseline leg, to check the product against.  The product package
 (``rtxplay_gb300``) never imports this module.
 """
 import ctypes

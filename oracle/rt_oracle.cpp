@@ -1,8 +1,8 @@
 // CPU oracle for the GB300 path tracer -- TEST INFRASTRUCTURE ONLY.
 //
 // A plain C++ restatement of the reference's render path.  Only tests/,
-// __graft_entry__.smoke() and bench.py's CPU-baseline leg use it, as the
-// checker; the product library never links or calls it.
+// __graft_entry__.smoke() and bench.py's CPU-baseline leg use it, to check
+// the product against; the product library never links or calls it.
 //
 // Parity is pinned by golden vectors made from the reference's own code
 // (tests/golden/make_golden.py: optx/sphere.cxx tessellation bits, rtow.cxx

@@ -1,7 +1,7 @@
 /* CPU oracle for the GB300 path tracer -- TEST INFRASTRUCTURE ONLY.
  *
  * A plain C++ restatement of the reference's render path, used by tests/,
- * __graft_entry__.smoke() and bench.py's CPU-baseline leg as the checker.
+ * __graft_entry__.smoke() and bench.py's CPU-baseline leg, to check the product against.
  * Nothing in the product library links, loads or calls this code.
  *
  * Parity pins: the tessellator and the scene recipe are checked bit for bit
