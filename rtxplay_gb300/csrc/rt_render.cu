@@ -718,7 +718,9 @@ struct WaveLaunch {
     int any_guides;
 };
 
-// Blocks of a persistent extend kernel: resident blocks per SM x SMs.
+// Blocks of a persistent extend kernel: resident blocks per SM x SMs.  (A
+// zero shared-memory carveout, all of the SM's unified storage as L1 for
+// nodes and stacks, measured no change: C1 at 64 spp, 2302 against 2301.)
 unsigned persistent_grid(ExtendFn fn) {
     int per_sm = 0;
     RT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, reinterpret_cast<const void*>(fn), kThreads, 0));
