@@ -60,6 +60,9 @@ def parse():
     p.add_argument("--batch-scenes", type=int, default=256, help="scenes of the batched leg (0: skip it)")
     p.add_argument("--no-adjoint", action="store_true", help="skip the adjoint/forward leg")
     p.add_argument("--inverse-scenes", type=int, default=64, help="scenes of the inverse-rendering leg (0: skip)")
+    p.add_argument("--tune", action="store_true",
+                   help="search the launch shape (rt_tuning) of every workload and store it in the tuning cache")
+    p.add_argument("--no-tuning", action="store_true", help="built-in launch shape, ignore the tuning cache")
     p.add_argument("--inverse-iters", type=int, default=10,
                    help="Adam iterations of the inverse-rendering leg, batched and serial each")
     return p.parse_args()
@@ -201,6 +204,16 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def apply_tuning(R, tune, key, measure, mode):
+    """Launch shape for workload `key`: the cached one (mode "cache"), a new
+    search stored in the cache ("tune") or the built-in default ("off")."""
+    if mode == "off":
+        R.tuning_set(None)
+        return {"values": R.tuning_get(), "source": "default", "key": key}
+    t, src = tune.tuned(key, measure if mode == "tune" else None, retune=(mode == "tune"))
+    return {"values": R.tuning_get(), "source": src, "key": key}
+
+
 def batch_specs(n, seed):
     """The batched workload: n random final-scene variants (counter-RNG
     recipe), half-extent U{2..11}, tessellation level U{2..6}, width
@@ -218,9 +231,11 @@ def batch_specs(n, seed):
     return specs
 
 
-def batched_leg(R, torch, sptr, stream, nscenes, steps):
+def batched_leg(R, torch, sptr, stream, nscenes, steps, tuning_mode):
     """Many scenes in one launch against one launch per scene (same scenes,
-    same outputs); returns timings, rays and an equality check."""
+    same outputs); returns timings, rays and an equality check.  Each side
+    runs with its own launch shape from the tuning cache (or a fresh search)."""
+    from rtxplay_gb300 import tune
     lib = R.lib()
     specs = batch_specs(nscenes, 2024)
     scenes, frames, bufs = [], [], []
@@ -258,6 +273,9 @@ def batched_leg(R, torch, sptr, stream, nscenes, steps):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1), r
 
+    paths = int(sum(sp["w"] * sp["h"] * sp["spp"] for sp in specs))
+    key_b = tune.workload_key("batch", paths, binfo["n_prims"], 16, scenes=nscenes)
+    t_batch = apply_tuning(R, tune, key_b, tune.batch_timer(batch, repeats=1, stream=sptr), tuning_mode)
     batch.launch(stream=sptr)   # warm-up
     b_ms, b_rays = [], 0
     for _ in range(steps):
@@ -275,6 +293,21 @@ def batched_leg(R, torch, sptr, stream, nscenes, steps):
             rays += int(st.rays)
         return rays
 
+    def serial_probe(t, first=32):   # the tuning search times the first scenes only
+        before = R.tuning_get()
+        R.tuning_set(t)
+        try:
+            for k in range(2):
+                t0 = time.perf_counter()
+                for sc, cam, pa, fr in list(zip(scenes, cams, params, frames))[:first]:
+                    R.check(lib.rt_launch(sc.h, ctypes.byref(cam), ctypes.byref(pa), ctypes.byref(fr), sptr))
+                torch.cuda.synchronize()
+            return time.perf_counter() - t0
+        finally:
+            R.tuning_set(before)
+
+    key_s = tune.workload_key("serial", paths, binfo["n_prims"], 16, scenes=nscenes)
+    t_serial = apply_tuning(R, tune, key_s, serial_probe, tuning_mode)
     serial()   # warm-up
     s_ms, s_rays = [], 0
     for _ in range(steps):
@@ -289,6 +322,7 @@ def batched_leg(R, torch, sptr, stream, nscenes, steps):
             "images_equal_first8": bool(equal and b_rays == s_rays),
             "build_batched_s": batch_build_s, "build_serial_s": serial_build_s,
             "device_gib": binfo["device_bytes"] / 2**30,
+            "tuning_batched": t_batch, "tuning_serial": t_serial,
             "workload": "256 random final-scene variants: half-extent U{2..11}, level U{2..6}, "
                         "width U{128..1024} at 16:9 or 1:1, spp U{1..64}, depth 16"}
 
@@ -417,6 +451,17 @@ def main():
     rpp = torch.empty(npix, dtype=torch.int32, device="cuda")
     frame = R.Frame(ctypes.c_void_p(raw.data_ptr()), ctypes.c_void_p(rpp.data_ptr()), None, None)
 
+    tuning_mode = "off" if args.no_tuning else ("tune" if args.tune else "cache")
+    from rtxplay_gb300 import tune
+    key_c1 = tune.workload_key("render", npix * args.spp, info.n_prims, args.depth,
+                               layout={1: "flat", 2: "instanced", 3: "grouped", 4: "sah"}.get(info.layout, "?"))
+    probe = None
+    if tuning_mode == "tune":   # searched on the frame itself (a reduced-spp frame picked worse shapes)
+        probe = tune.render_timer(sc, cam, R.launch_params(W, H, args.spp, args.depth, 77, 0), repeats=1)
+    tuning_c1 = apply_tuning(R, tune, key_c1, probe, tuning_mode)
+    if probe:
+        probe.close()
+
     def step(seed, flags, spp=None):
         params = R.launch_params(W, H, spp or args.spp, args.depth, seed, flags)
         st = R.LaunchStats()
@@ -501,7 +546,8 @@ def main():
 
     batched = None
     if rank == 0 and world == 1 and args.batch_scenes > 0:
-        batched = batched_leg(R, torch, sptr, stream, args.batch_scenes, max(1, min(args.steps, 3)))
+        batched = batched_leg(R, torch, sptr, stream, args.batch_scenes, max(1, min(args.steps, 3)), tuning_mode)
+        R.tuning_set(None)   # the adjoint and inverse legs use the built-in shape
 
     adjoint = None
     if rank == 0 and world == 1 and not args.no_adjoint:
@@ -557,7 +603,7 @@ def main():
                            else "host-driven",
                            "l2": "inputs larger than L2 (LBVH + triangles "
                                  f"{info.device_bytes / 2**30:.2f} GiB on device)",
-                           "build_ms": info.build_ms},
+                           "build_ms": info.build_ms, "tuning": tuning_c1},
                 "rays_per_step": total_rays / args.steps / world,
                 "gpu_launches": launches,
                 "clocks": clk, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "batched": batched,

@@ -244,6 +244,28 @@ rt_status rt_scene_info_get(rt_scene scene, rt_scene_info* info);
 rt_status rt_scene_get_lbvh(rt_scene scene, unsigned long long* codes, unsigned int* ids,
                             int* left, int* right, float* boxes);
 
+/* -------------------------------------------------------------- tuning */
+/* Launch shape of the wavefront (no reference counterpart; OptiX chooses its
+ * own): the wave-queue size and the kernels' block shapes.  Process-wide,
+ * read by every later launch (rt_launch*, rt_batch_launch, the launcher);
+ * the image does not depend on it (tested bit for bit).  A zero field means
+ * the built-in default.  rtxplay_gb300/tune.py searches it per workload and
+ * keeps the results in a JSON cache. */
+typedef struct {
+    unsigned int wave_log2;            /* rays per wave queue = 2^wave_log2, 16..24 (default 23, or RTX_WAVE) */
+    unsigned int shade_block;          /* threads per shading block: 128, 256 or 512 (default 512) */
+    unsigned int extend_blocks_per_sm; /* persistent traversal blocks per SM, 1..32, capped at what fits
+                                          (default: what fits) */
+    unsigned int refill_below;         /* a traversal warp takes new rays when at most this many of its
+                                          lanes are busy, 1..31 (default 12) */
+    unsigned int steps_per_check;      /* traversal steps between those checks, 1..64 (default 16) */
+} rt_tuning;
+
+/* Sets the tuning (NULL: all defaults); RT_ERR_INVALID_ARG for a field out
+ * of range.  rt_tuning_get returns the tuning in effect, defaults filled in. */
+rt_status rt_tuning_set(const rt_tuning* tuning);
+rt_status rt_tuning_get(rt_tuning* tuning);
+
 /* -------------------------------------------------------------- render */
 /* Launcher::ignite + __raygen__camera / __closesthit__* / __miss__ambient
  * (optx/launcher.cxx:49-77, optx/camera_i.cu:24-141, optx/optics_i.cu:23-288):

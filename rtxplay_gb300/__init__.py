@@ -83,6 +83,13 @@ class SceneInfo(ctypes.Structure):
                 ("n_instances", ctypes.c_uint), ("n_top_records", ctypes.c_uint), ("n_bottom_records", ctypes.c_uint)]
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [("wave_log2", ctypes.c_uint), ("shade_block", ctypes.c_uint), ("extend_blocks_per_sm", ctypes.c_uint),
+                ("refill_below", ctypes.c_uint), ("steps_per_check", ctypes.c_uint)]
+
+
+TUNING_FIELDS = tuple(f[0] for f in Tuning._fields_)
+
 _P = ctypes.c_void_p
 _U = ctypes.c_uint
 _I = ctypes.c_int
@@ -142,6 +149,8 @@ SIGNATURES = {
     "rt_batch_set_albedos": [_P, _P, _P],
     "rt_l2_loss_grad": [_P, _P, _P, _U, _P, _P],
     "rt_adam_step": [_P, _P, _P, _P, _U, _F, _F, _F, _F, _U, _F, _F, _P],
+    "rt_tuning_set": [ctypes.POINTER(Tuning)],
+    "rt_tuning_get": [ctypes.POINTER(Tuning)],
 }
 
 _lib = None
@@ -456,6 +465,25 @@ def l2_loss_grad(image, target, grad_image, n, loss=None, stream=None):
 def adam_step(theta, grad, m, v, n, step, lr=1e-2, beta1=0.9, beta2=0.999, eps=1e-8, lo=0.0, hi=1.0, stream=None):
     """rt_adam_step on device pointers."""
     check(lib().rt_adam_step(theta, grad, m, v, n, lr, beta1, beta2, eps, step, lo, hi, stream))
+
+
+def tuning_set(tuning=None):
+    """rt_tuning_set from a dict of rt_tuning fields (missing or 0: default; None: all defaults)."""
+    if tuning is None:
+        check(lib().rt_tuning_set(None))
+        return
+    unknown = set(tuning) - set(TUNING_FIELDS)
+    if unknown:
+        raise ValueError(f"unknown tuning fields {sorted(unknown)}")
+    t = Tuning(**{k: int(v) for k, v in tuning.items()})
+    check(lib().rt_tuning_set(ctypes.byref(t)))
+
+
+def tuning_get():
+    """The tuning in effect (rt_tuning_get) as a dict."""
+    t = Tuning()
+    check(lib().rt_tuning_get(ctypes.byref(t)))
+    return {k: getattr(t, k) for k in TUNING_FIELDS}
 
 
 def render(scene, cam, params, guides=False):

@@ -23,6 +23,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "rt_scene.h"
@@ -185,6 +186,14 @@ __global__ void __launch_bounds__(kThreads) k_generate(const JobDev* __restrict_
     }
 }
 
+// Refill rule of the persistent traversal (rt_tuning: refill_below,
+// steps_per_check); the counting pass takes it too, unused, so both kernels
+// share one signature.
+struct ExtTune {
+    uint32_t refill_below;
+    int steps;
+};
+
 // One thread per queued ray (the counting pass; rendering uses the persistent
 // k_extend_p below); kInst selects the two-level traversal.  Warp-cooperative
 // traversal with parked leaf tests measured slower (active lanes 9.6 -> 12.9,
@@ -196,7 +205,7 @@ __global__ void __launch_bounds__(kThreads) k_generate(const JobDev* __restrict_
 template <bool kCount, bool kInst>
 __global__ void __launch_bounds__(kThreads)
     k_extend(Queues qs, float4* __restrict__ hits, uint32_t* __restrict__ hthing, WaveState* st,
-             const JobDev* __restrict__ jobs, GeoView g) {
+             const JobDev* __restrict__ jobs, GeoView g, ExtTune) {
     const uint32_t cur = *((volatile uint32_t*)&st->cur);
     if (blockIdx.x == 0 && threadIdx.x == 0) {   // the next queue starts empty
         st->count[cur ^ 1] = 0;
@@ -247,7 +256,7 @@ constexpr int kStepsPerCheck = 16;
 template <bool kInst>
 __global__ void __launch_bounds__(kThreads, kInst ? 4 : 5)
     k_extend_p(Queues qs, float4* __restrict__ hits, uint32_t* __restrict__ hthing, WaveState* st,
-               const JobDev* __restrict__ jobs, GeoView g) {
+               const JobDev* __restrict__ jobs, GeoView g, ExtTune tn) {
     const uint32_t cur = *((volatile uint32_t*)&st->cur);
     if (blockIdx.x == 0 && threadIdx.x == 0) {   // the next queue starts empty
         st->count[cur ^ 1] = 0;
@@ -263,7 +272,7 @@ __global__ void __launch_bounds__(kThreads, kInst ? 4 : 5)
     bool busy = false, drained = false;
     while (true) {
         uint32_t bm = __ballot_sync(0xFFFFFFFFu, busy);
-        if (!drained && uint32_t(__popc(bm)) <= kRefillBelow) {
+        if (!drained && uint32_t(__popc(bm)) <= tn.refill_below) {
             const uint32_t idle = ~bm;
             uint32_t base = 0;
             if (lane == 0) base = atomicAdd(&st->ext_next[cur], uint32_t(__popc(idle)));
@@ -288,7 +297,7 @@ __global__ void __launch_bounds__(kThreads, kInst ? 4 : 5)
         }
         if (busy) {
 #pragma unroll 1
-            for (int k = 0; k < kStepsPerCheck; ++k) {
+            for (int k = 0; k < tn.steps; ++k) {
                 if (!trav_step<false, kInst>(s, stack, g, nvis, ntest)) {
                     const HitRec& h = s.h;
                     const int ref = !h.hit ? -1 : (h.leaf >= 0 ? h.leaf : -2 - int(h.id));
@@ -303,7 +312,7 @@ __global__ void __launch_bounds__(kThreads, kInst ? 4 : 5)
     }
 }
 
-using ExtendFn = void (*)(Queues, float4*, uint32_t*, WaveState*, const JobDev*, GeoView);
+using ExtendFn = void (*)(Queues, float4*, uint32_t*, WaveState*, const JobDev*, GeoView, ExtTune);
 
 // 64-bit fixed-point sample sums: round-half-even(x * 2^32) as two's
 // complement, added with integer atomics (exact, order-free).
@@ -317,13 +326,15 @@ __device__ __forceinline__ unsigned long long fx_q(float x) {
 // (2 barriers instead of 5), and the hit's thing id written by k_extend so its
 // optics load beside the primitive record (k_extend then needs 51 registers,
 // 4 % slower overall unless held to 48).
-__global__ void __launch_bounds__(kThreads, 4)
+// kB threads per block (rt_tuning: shade_block), held to 64 registers.
+template <int kB>
+__global__ void __launch_bounds__(kB, 1024 / kB)
     k_shade(Queues qs, const float4* __restrict__ hits, const uint32_t* __restrict__ hthing, WaveState* st,
             const JobDev* __restrict__ jobs, uint32_t nj, const float4* __restrict__ tprims,
             const FlatDesc* __restrict__ desc, const ThingDev* __restrict__ things, Acc acc, int any_guides) {
     // per-warp counts, turned into block-exclusive offsets by thread 0, and the
     // block's bases from one global atomic per block (not one per warp)
-    __shared__ uint32_t s_warp[kThreads / 32], s_warp2[kThreads / 32];
+    __shared__ uint32_t s_warp[kB / 32], s_warp2[kB / 32];
     __shared__ unsigned long long s_base, s_base2;
     const uint32_t cur = *((volatile uint32_t*)&st->cur);
     const uint32_t n = *((volatile uint32_t*)&st->count[cur]);
@@ -429,7 +440,7 @@ __global__ void __launch_bounds__(kThreads, 4)
     __syncthreads();
     if (threadIdx.x == 0) {
         uint32_t tot = 0;
-        for (uint32_t w = 0; w < kThreads / 32; ++w) {
+        for (uint32_t w = 0; w < kB / 32; ++w) {
             const uint32_t c = s_warp[w];
             s_warp[w] = tot;
             tot += c;
@@ -468,7 +479,7 @@ __global__ void __launch_bounds__(kThreads, 4)
     __syncthreads();
     if (threadIdx.x == 0) {
         uint32_t tc = 0, tf = 0;
-        for (uint32_t w = 0; w < kThreads / 32; ++w) {
+        for (uint32_t w = 0; w < kB / 32; ++w) {
             const uint32_t c = s_warp[w], f = s_warp2[w];
             s_warp[w] = tc;
             s_warp2[w] = tf;
@@ -650,6 +661,42 @@ uint32_t env_u32(const char* name, uint32_t dflt) {
     return x ? uint32_t(x) : dflt;
 }
 
+// Launch shape set by rt_tuning_set (process-wide; zero fields: defaults).
+// The defaults are the autotuner's choice for the full C1 frame (1200x800,
+// 500 spp, 7,979,008 triangles): 2^23-ray waves and 512-thread shading
+// blocks, 2840 Mrays/s against 2720 with 2^22 and 256 (the earlier defaults).
+constexpr uint32_t kWaveDefault = 1u << 23;
+constexpr int kShadeBlockDefault = 512;
+std::mutex g_tune_mu;
+rt_tuning g_tune{};
+
+struct LaunchShape {
+    uint32_t wave;        // rays per wave queue
+    int shade_block;      // threads per k_shade block
+    uint32_t ext_bpsm;    // persistent traversal blocks per SM (0: all that fit)
+    ExtTune ext;
+};
+
+LaunchShape launch_shape() {
+    rt_tuning t;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        t = g_tune;
+    }
+    LaunchShape r;
+    r.wave = t.wave_log2 ? (1u << t.wave_log2) : env_u32("RTX_WAVE", kWaveDefault);
+    r.shade_block = t.shade_block ? int(t.shade_block) : kShadeBlockDefault;
+    r.ext_bpsm = t.extend_blocks_per_sm;
+    r.ext.refill_below = t.refill_below ? t.refill_below : kRefillBelow;
+    r.ext.steps = t.steps_per_check ? int(t.steps_per_check) : kStepsPerCheck;
+    return r;
+}
+
+using ShadeFn = void (*)(Queues, const float4*, const uint32_t*, WaveState*, const JobDev*, uint32_t, const float4*,
+                         const FlatDesc*, const ThingDev*, Acc, int);
+
+ShadeFn shade_fn(int block) { return block == 128 ? k_shade<128> : block == 512 ? k_shade<512> : k_shade<256>; }
+
 // The wave loop captured once as a graph: a conditional WHILE node whose body
 // is extend -> shade -> ctrl; rebuilt whenever a baked-in pointer or launch
 // shape changes.
@@ -705,7 +752,11 @@ bool graph_mode() {
 struct WaveLaunch {
     ExtendFn ext_fn;
     unsigned egrid;    // extend grid (persistent: fills the GPU once)
-    unsigned qgrid;
+    unsigned qgrid;    // one thread per wave slot, kThreads per block
+    ShadeFn shade;
+    unsigned sgrid;    // shading grid, sblock threads per block
+    int sblock;
+    ExtTune tn;
     Queues qs;
     float4* hits;      // t, u, v, hit reference
     uint32_t* hthing;  // thing of an instanced hit
@@ -718,13 +769,16 @@ struct WaveLaunch {
     int any_guides;
 };
 
-// Blocks of a persistent extend kernel: resident blocks per SM x SMs.  (A
-// zero shared-memory carveout, all of the SM's unified storage as L1 for
-// nodes and stacks, measured no change: C1 at 64 spp, 2302 against 2301.)
-unsigned persistent_grid(ExtendFn fn) {
+// Blocks of a persistent extend kernel: resident blocks per SM (at most
+// `bpsm` when nonzero) x SMs.  (A zero shared-memory carveout, all of the
+// SM's unified storage as L1 for nodes and stacks, measured no change: C1 at
+// 64 spp, 2302 against 2301.)
+unsigned persistent_grid(ExtendFn fn, uint32_t bpsm) {
     int per_sm = 0;
     RT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, reinterpret_cast<const void*>(fn), kThreads, 0));
-    return unsigned(std::max(1, per_sm) * sm_count());
+    per_sm = std::max(1, per_sm);
+    if (bpsm) per_sm = std::min(per_sm, int(bpsm));
+    return unsigned(per_sm * sm_count());
 }
 
 void build_wave_graph(Workspace& ws, const WaveLaunch& L) {
@@ -745,7 +799,7 @@ void build_wave_graph(Workspace& ws, const WaveLaunch& L) {
     WaveLaunch l = L;   // kernel arguments must stay addressable while the nodes are added
     cudaKernelNodeParams kp = {};
     cudaGraphNode_t n_ext, n_shade, n_ctrl;
-    void* ext_args[] = {&l.qs, &l.hits, &l.hthing, &l.st, &l.jobs, &l.geo};
+    void* ext_args[] = {&l.qs, &l.hits, &l.hthing, &l.st, &l.jobs, &l.geo, &l.tn};
     kp.func = reinterpret_cast<void*>(l.ext_fn);
     kp.gridDim = dim3(l.egrid);
     kp.blockDim = dim3(kThreads);
@@ -757,8 +811,9 @@ void build_wave_graph(Workspace& ws, const WaveLaunch& L) {
     const FlatDesc* desc_c = l.geo.desc;
     void* shade_args[] = {&l.qs,      &hits_c, &hthing_c, &l.st,  &l.jobs,       &l.nj,
                           &tprims_c, &desc_c, &l.things, &l.acc, &l.any_guides};
-    kp.func = reinterpret_cast<void*>(k_shade);
-    kp.gridDim = dim3(l.qgrid);
+    kp.func = reinterpret_cast<void*>(l.shade);
+    kp.gridDim = dim3(l.sgrid);
+    kp.blockDim = dim3(unsigned(l.sblock));
     kp.kernelParams = shade_args;
     RT_CUDA(cudaGraphAddKernelNode(&n_shade, body, &n_ext, 1, &kp));
     int in_graph = 1;
@@ -823,8 +878,10 @@ void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s
         max_depth = std::max(max_depth, d.depth);
     }
     RT_REQUIRE(total_pix < (uint64_t(1) << 31), "too many pixels in one launch (>= 2^31)");
-    // wave capacity: measured on C1 (64 spp) 2^22: 1217, 2^21: 1210, 2^20: 1137, 2^19: 1020 Mrays/s
-    const uint32_t W = uint32_t(std::min<unsigned long long>(env_u32("RTX_WAVE", 1u << 22), total_paths));
+    // wave capacity (one-thread-per-ray traversal, C1 at 64 spp): 2^22: 1217, 2^21: 1210, 2^20: 1137,
+    // 2^19: 1020 Mrays/s; the current default comes from the autotuner (see launch_shape)
+    const LaunchShape shape = launch_shape();
+    const uint32_t W = uint32_t(std::min<unsigned long long>(shape.wave, total_paths));
     // wave bound: the queue holds W rays while paths remain to start and a
     // path is queued at most max_depth times
     const uint64_t max_iter64 = total_paths * max_depth / W + max_depth + 8;
@@ -854,7 +911,11 @@ void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s
     L.ext_fn = g.ninstances ? (count ? k_extend<true, true> : k_extend_p<true>)
                             : (count ? k_extend<true, false> : k_extend_p<false>);
     L.qgrid = grid_for(W);
-    L.egrid = count ? L.qgrid : persistent_grid(L.ext_fn);
+    L.egrid = count ? L.qgrid : persistent_grid(L.ext_fn, shape.ext_bpsm);
+    L.sblock = shape.shade_block;
+    L.shade = shade_fn(L.sblock);
+    L.sgrid = grid_for(W, L.sblock);
+    L.tn = shape.ext;
     L.hits = ws.hits.as<float4>();
     L.hthing = ws.hthing.as<uint32_t>();
     L.st = ws.state.as<WaveState>();
@@ -884,7 +945,9 @@ void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s
     if (use_graph) {
         const std::vector<const void*> key = {
             reinterpret_cast<const void*>(L.ext_fn), reinterpret_cast<const void*>(uintptr_t(L.qgrid)),
-            reinterpret_cast<const void*>(uintptr_t(L.egrid)),
+            reinterpret_cast<const void*>(uintptr_t(L.egrid)), reinterpret_cast<const void*>(L.shade),
+            reinterpret_cast<const void*>(uintptr_t(L.sgrid)), reinterpret_cast<const void*>(uintptr_t(L.tn.refill_below)),
+            reinterpret_cast<const void*>(uintptr_t(L.tn.steps)),
             L.qs.q[0].ori, L.qs.q[0].gn, L.qs.q[1].ori, L.qs.q[1].gn, L.hits, L.hthing, L.st, L.jobs,
             reinterpret_cast<const void*>(uintptr_t(nj)), L.geo.tnodes, L.geo.tprims, L.geo.bnodes, L.geo.bprims,
             L.geo.inst, L.geo.desc, L.things, L.acc.col[0], L.acc.gd[0], reinterpret_cast<const void*>(uintptr_t(total_pix)),
@@ -897,7 +960,14 @@ void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s
     } else {
         size_t ev = 0;
         const uint32_t kBatch = 8;
-        void* ext_args[] = {&L.qs, &L.hits, &L.hthing, &L.st, &L.jobs, &L.geo};
+        void* ext_args[] = {&L.qs, &L.hits, &L.hthing, &L.st, &L.jobs, &L.geo, &L.tn};
+        const float4* hits_c = L.hits;
+        const uint32_t* hthing_c = L.hthing;
+        const float4* tprims_c = L.geo.tprims;
+        const FlatDesc* desc_c = L.geo.desc;
+        uint32_t nj_c = nj;
+        void* shade_args[] = {&L.qs,      &hits_c, &hthing_c, &L.st,  &L.jobs,       &nj_c,
+                              &tprims_c, &desc_c, &L.things, &L.acc, &L.any_guides};
         cudaGraphConditionalHandle no_handle = 0;
         while (true) {
             for (uint32_t b = 0; b < kBatch; ++b) {
@@ -914,8 +984,8 @@ void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s
                     timed.push_back({ev, 1});
                     ev += 2;
                 }
-                k_shade<<<L.qgrid, kThreads, 0, s>>>(L.qs, L.hits, L.hthing, L.st, L.jobs, nj, L.geo.tprims,
-                                                      L.geo.desc, L.things, L.acc, any_guides);
+                RT_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(L.shade), dim3(L.sgrid),
+                                         dim3(unsigned(L.sblock)), shade_args, 0, s));
                 if (stage_timing) RT_CUDA(cudaEventRecord(ws.event(ev - 1), s));
                 k_wave_ctrl<<<1, 1, 0, s>>>(L.st, no_handle, 0);
                 RT_CHECK_LAUNCH();
@@ -1050,6 +1120,41 @@ Batch* batch_from(rt_batch b) {
 using namespace rt;
 
 extern "C" {
+
+rt_status rt_tuning_set(const rt_tuning* tuning) {
+    return guarded([&] {
+        rt_tuning t{};
+        if (tuning) t = *tuning;
+        RT_REQUIRE(t.wave_log2 == 0 || (t.wave_log2 >= 16 && t.wave_log2 <= 24), "wave_log2 outside 16..24");
+        RT_REQUIRE(t.shade_block == 0 || t.shade_block == 128 || t.shade_block == 256 || t.shade_block == 512,
+                   "shade_block must be 128, 256 or 512");
+        RT_REQUIRE(t.extend_blocks_per_sm <= 32, "extend_blocks_per_sm outside 1..32");
+        RT_REQUIRE(t.refill_below <= 31, "refill_below outside 1..31");
+        RT_REQUIRE(t.steps_per_check <= 64, "steps_per_check outside 1..64");
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune = t;
+    });
+}
+
+rt_status rt_tuning_get(rt_tuning* tuning) {
+    return guarded([&] {
+        RT_REQUIRE(tuning != nullptr, "tuning is NULL");
+        rt_tuning t;
+        {
+            std::lock_guard<std::mutex> lk(g_tune_mu);
+            t = g_tune;
+        }
+        const LaunchShape r = launch_shape();
+        if (!t.wave_log2) {   // the default (or RTX_WAVE), rounded down to a power of two
+            t.wave_log2 = 0;
+            while ((2ull << t.wave_log2) <= r.wave) ++t.wave_log2;
+        }
+        t.shade_block = unsigned(r.shade_block);
+        t.refill_below = r.ext.refill_below;
+        t.steps_per_check = unsigned(r.ext.steps);
+        *tuning = t;   // extend_blocks_per_sm stays 0 (all that fit) unless set
+    });
+}
 
 rt_status rt_launch(rt_scene scene, const rt_camera* cam, const rt_launch_params* params, const rt_frame* frame,
                     void* stream) {
