@@ -517,7 +517,16 @@ def main():
         img_host = np.empty((npix, 4), np.uint8)
         rpp_host = np.empty(npix, np.uint32)
         L = R.Launcher(W, H)
-        h2d = mesh_host[0].nbytes + mesh_host[1].nbytes + len(spheres["radii"]) * (16 + 48 + 20)
+        # the things as host arrays (rt_optics records, 3x4 transforms), added with one call per step
+        nth = len(spheres["radii"])
+        th_optics = (R.Optics * nth)(*[R.optics(int(t_), a_, float(f_), float(i_)) for t_, a_, f_, i_ in
+                                       zip(spheres["types"], spheres["albedos"], spheres["fuzz"], spheres["index"])])
+        th_T = np.zeros((nth, 12), np.float32)
+        rr = np.asarray(spheres["radii"], np.float32)
+        cc = np.asarray(spheres["centers"], np.float32)
+        th_T[:, 0] = th_T[:, 5] = th_T[:, 10] = rr
+        th_T[:, 3], th_T[:, 7], th_T[:, 11] = cc[:, 0], cc[:, 1], cc[:, 2]
+        h2d = mesh_host[0].nbytes + mesh_host[1].nbytes + nth * (ctypes.sizeof(R.Optics) + 48 + 4)
         d2h = img_host.nbytes + rpp_host.nbytes
         e2e_rays = 0
         torch.cuda.synchronize()
@@ -525,10 +534,7 @@ def main():
         for k in range(args.steps):
             s2 = R.Scene()
             mid = s2.add_mesh(mesh_host[0], mesh_host[1])
-            for c, r_, t_, a_, f_, i_ in zip(spheres["centers"], spheres["radii"], spheres["types"],
-                                             spheres["albedos"], spheres["fuzz"], spheres["index"]):
-                T = np.array([r_, 0, 0, c[0], 0, r_, 0, c[1], 0, 0, r_, c[2]], np.float32)
-                s2.add_thing(R.optics(int(t_), a_, float(f_), float(i_)), mid, T)
+            s2.add_things(th_optics, np.full(nth, mid, np.uint32), th_T)
             s2.build(args.morton_bits, layout=LAYOUTS[args.layout])
             params = R.launch_params(W, H, args.spp, args.depth, 4711 + k, 0)
             L.ignite(s2, cam, params)

@@ -152,6 +152,12 @@ rt_status rt_scene_get_mesh(rt_scene scene, unsigned int mesh_id, rt_float3* vce
  * of mesh_id with its optics and 3x4 row-major object-to-world transform. */
 rt_status rt_scene_add_thing(rt_scene scene, const rt_optics* optics, unsigned int mesh_id,
                              const float transform[12], unsigned int* thing_id);
+/* n rt_scene_add_thing calls in one (the loop of RTWO::load,
+ * optx/rtwo.cxx:137-244, for callers behind a foreign-function boundary):
+ * optics[k], mesh_ids[k] and transforms[12k..12k+11] make thing
+ * first_id + k.  All n are checked before any is added. */
+rt_status rt_scene_add_things(rt_scene scene, unsigned int n, const rt_optics* optics,
+                              const unsigned int* mesh_ids, const float* transforms, unsigned int* first_id);
 
 /* An analytic sphere thing (rtow's Sphere, sphere.h:9-48). */
 rt_status rt_scene_add_analytic_sphere(rt_scene scene, rt_float3 center, float radius,

@@ -107,6 +107,7 @@ SIGNATURES = {
     "rt_obj_parse": [ctypes.c_char_p, _U, _P, _PU, _P, _PU, _PU],
     "rt_scene_get_mesh": [_P, _U, _P, _PU, _P, _PU],
     "rt_scene_add_thing": [_P, ctypes.POINTER(Optics), _U, _P, _PU],
+    "rt_scene_add_things": [_P, _U, _P, _P, _P, _PU],
     "rt_scene_add_analytic_sphere": [_P, float3, _F, ctypes.POINTER(Optics), _PU],
     "rt_rtow_spheres": [_I, _U, _I, _U, _P, _P, _P, _PU],
     "rt_scene_load_rtow": [_P, _I, _U, _I, _I, _PU],
@@ -294,6 +295,20 @@ class Scene:
         tid = ctypes.c_uint()
         check(lib().rt_scene_add_thing(self.h, ctypes.byref(opt), mesh_id, _ptr(t), ctypes.byref(tid)))
         return tid.value
+
+    def add_things(self, optics, mesh_ids, transforms):
+        """rt_scene_add_things: optics a sequence of Optics (or an Optics array), mesh_ids n ints,
+        transforms n x 12 floats; returns the new thing ids."""
+        n = len(mesh_ids)
+        opt = optics if isinstance(optics, ctypes.Array) else (Optics * max(1, n))(*optics)
+        ids = np.ascontiguousarray(mesh_ids, np.uint32)
+        T = np.ascontiguousarray(transforms, np.float32).reshape(n, 12) if n else np.zeros((1, 12), np.float32)
+        if len(opt) < n or ids.shape != (n,):
+            raise ValueError("optics, mesh_ids and transforms need n entries each")
+        first = ctypes.c_uint()
+        check(lib().rt_scene_add_things(self.h, n, ctypes.cast(opt, ctypes.c_void_p), _ptr(ids), _ptr(T),
+                                        ctypes.byref(first)))
+        return list(range(first.value, first.value + n))
 
     def add_analytic_sphere(self, center, radius, opt):
         tid = ctypes.c_uint()

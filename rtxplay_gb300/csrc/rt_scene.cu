@@ -1140,6 +1140,30 @@ rt_status rt_scene_add_thing(rt_scene scene, const rt_optics* optics, unsigned i
     });
 }
 
+rt_status rt_scene_add_things(rt_scene scene, unsigned int n, const rt_optics* optics, const unsigned int* mesh_ids,
+                              const float* transforms, unsigned int* first_id) {
+    return guarded([&] {
+        Scene* sc = scene_from(scene);
+        RT_REQUIRE(first_id != nullptr, "first_id is NULL");
+        RT_REQUIRE(n == 0 || (optics && mesh_ids && transforms), "optics/mesh_ids/transforms is NULL");
+        for (unsigned k = 0; k < n; ++k) {
+            check_optics(optics + k);
+            check_transform(transforms + 12 * size_t(k));
+            RT_REQUIRE(mesh_ids[k] < sc->meshes.size(), "bad mesh id");
+        }
+        *first_id = unsigned(sc->things.size());
+        sc->things.reserve(sc->things.size() + n);
+        for (unsigned k = 0; k < n; ++k) {
+            ThingHost th;
+            th.optics = optics[k];
+            th.mesh = int(mesh_ids[k]);
+            std::memcpy(th.T, transforms + 12 * size_t(k), sizeof(th.T));
+            sc->things.push_back(th);
+        }
+        if (n) sc->topology_dirty = true;
+    });
+}
+
 rt_status rt_scene_add_analytic_sphere(rt_scene scene, rt_float3 center, float radius, const rt_optics* optics,
                                        unsigned int* thing_id) {
     return guarded([&] {

@@ -99,3 +99,24 @@ def test_scene_handle_logic_without_device(product):
     assert sc.set_transform(0, T) == R.RT_OK
     assert sc.get_transform(0)[1][3] == 9.0
     sc.close()
+
+
+def test_add_things_checks_everything_first(product):
+    """rt_scene_add_things refuses the whole call for one bad entry (no device needed)."""
+    R = product
+    sc = R.Scene()
+    assert sc.add_analytic_sphere((0, 0, 0), 1.0, R.optics(R.RT_OPTICS_DIFFUSE, (0.5, 0.5, 0.5))) == 0
+    T = np.tile(np.array([1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0], np.float32), (3, 1))
+    opts = [R.optics(R.RT_OPTICS_DIFFUSE, (0.1, 0.2, 0.3))] * 3
+    with pytest.raises(R.RTError) as e:   # no mesh 0 in this scene
+        sc.add_things(opts, [0, 0, 0], T)
+    assert e.value.status == R.RT_ERR_INVALID_ARG and b"mesh" in R.lib().rt_last_error_string()
+    bad = T.copy()
+    bad[1, 0] = np.nan
+    with pytest.raises(R.RTError):
+        sc.add_things(opts, [0, 0, 0], bad)
+    assert sc.add_things([], [], np.zeros((0, 12), np.float32)) == []
+    assert sc.add_analytic_sphere((1, 0, 0), 1.0, R.optics(R.RT_OPTICS_DIFFUSE, (0.5, 0.5, 0.5))) == 1
+    first = ctypes.c_uint()
+    assert R.lib().rt_scene_add_things(sc.h, 2, None, None, None, ctypes.byref(first)) == R.RT_ERR_INVALID_ARG
+    sc.close()
