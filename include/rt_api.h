@@ -37,6 +37,11 @@ const char* rt_last_error_string(void);
 /* Library version string, e.g. "rtxplay_gb300 0.1 sm_103a". */
 const char* rt_version(void);
 
+/* Fault injection on the host (tests): the n-th device allocation from now
+ * fails as cudaMalloc's out-of-memory would (RT_ERR_OUT_OF_MEMORY from the call
+ * that made it); n = 0 switches it off.  Process-wide. */
+rt_status rt_debug_fail_alloc(unsigned int n);
+
 /* ------------------------------------------------------------- data types */
 typedef struct { float x, y, z; } rt_float3;
 typedef struct { unsigned int x, y, z; } rt_uint3;
@@ -249,6 +254,36 @@ rt_status rt_scene_info_get(rt_scene scene, rt_scene_info* info);
  * n, n-1, n-1, 12*(n-1) with n = n_top_records; any may be NULL. */
 rt_status rt_scene_get_lbvh(rt_scene scene, unsigned long long* codes, unsigned int* ids,
                             int* left, int* right, float* boxes);
+
+/* ------------------------------------------------------ progressive render */
+/* Progressive rendering with checkpoint and resume (no reference counterpart:
+ * every Launcher::ignite renders all spp afresh, optx/camera_i.cu:58).  An
+ * accumulator keeps the exact fixed-point pixel sums (colour and rays) of the
+ * samples rendered so far and their count.  Sample k of a pixel draws from
+ * its own counter-RNG stream, so rendering samples [0, a), then [a, b), ...
+ * with one seed gives the sums, and so the image and rays per pixel, of one
+ * launch of b samples bit for bit. */
+typedef struct rt_accum_s* rt_accum;
+rt_status rt_accum_create(rt_accum* out, unsigned int w, unsigned int h);
+rt_status rt_accum_destroy(rt_accum acc);
+/* Back to zero samples (also the way out of a failed rt_launch_accum). */
+rt_status rt_accum_reset(rt_accum acc, void* stream);
+rt_status rt_accum_samples(rt_accum acc, unsigned long long* samples);
+/* Renders the next params->spp samples of every pixel (sample indices from the
+ * accumulator's count on) into the accumulator and writes frame->rawRGB and
+ * frame->rpp as the mean, and the sum of rays, over all its samples
+ * (stats->rays counts this launch's rays only).
+ * params->image_w/h must be the accumulator's size; RT_FLAG_GUIDES is not
+ * supported; RT_ERR_LIMIT once samples x depth would reach 2^32.
+ * Synchronous like rt_launch. */
+rt_status rt_launch_accum(rt_scene scene, const rt_camera* cam, const rt_launch_params* params, rt_accum acc,
+                          const rt_frame* frame, void* stream, rt_launch_stats* stats);
+/* Checkpoint and resume: the accumulator's state as host bytes (a header with
+ * size and sample count, then the sums), and back into an accumulator of the
+ * same image size; a render resumed from it continues bit for bit. */
+rt_status rt_accum_state_size(rt_accum acc, size_t* bytes);
+rt_status rt_accum_save(rt_accum acc, void* host, size_t bytes, void* stream);
+rt_status rt_accum_load(rt_accum acc, const void* host, size_t bytes, void* stream);
 
 /* -------------------------------------------------------------- tuning */
 /* Launch shape of the wavefront (no reference counterpart; OptiX chooses its

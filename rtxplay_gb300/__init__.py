@@ -150,7 +150,17 @@ SIGNATURES = {
     "rt_batch_set_albedos": [_P, _P, _P],
     "rt_l2_loss_grad": [_P, _P, _P, _U, _P, _P],
     "rt_adam_step": [_P, _P, _P, _P, _U, _F, _F, _F, _F, _U, _F, _F, _P],
+    "rt_accum_create": [ctypes.POINTER(_P), _U, _U],
+    "rt_accum_destroy": [_P],
+    "rt_accum_reset": [_P, _P],
+    "rt_accum_samples": [_P, ctypes.POINTER(ctypes.c_ulonglong)],
+    "rt_launch_accum": [_P, ctypes.POINTER(Camera), ctypes.POINTER(LaunchParams), _P, ctypes.POINTER(Frame), _P,
+                        ctypes.POINTER(LaunchStats)],
+    "rt_accum_state_size": [_P, ctypes.POINTER(ctypes.c_size_t)],
+    "rt_accum_save": [_P, _P, ctypes.c_size_t, _P],
+    "rt_accum_load": [_P, _P, ctypes.c_size_t, _P],
     "rt_tuning_set": [ctypes.POINTER(Tuning)],
+    "rt_debug_fail_alloc": [_U],
     "rt_tuning_get": [ctypes.POINTER(Tuning)],
 }
 
@@ -480,6 +490,54 @@ def l2_loss_grad(image, target, grad_image, n, loss=None, stream=None):
 def adam_step(theta, grad, m, v, n, step, lr=1e-2, beta1=0.9, beta2=0.999, eps=1e-8, lo=0.0, hi=1.0, stream=None):
     """rt_adam_step on device pointers."""
     check(lib().rt_adam_step(theta, grad, m, v, n, lr, beta1, beta2, eps, step, lo, hi, stream))
+
+
+class Accum:
+    """rt_accum: progressive rendering with checkpoint and resume."""
+
+    def __init__(self, w, h):
+        self.h = ctypes.c_void_p()
+        self.w, self.hgt = w, h
+        check(lib().rt_accum_create(ctypes.byref(self.h), w, h))
+
+    def close(self):
+        if self.h:
+            lib().rt_accum_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def samples(self):
+        n = ctypes.c_ulonglong()
+        check(lib().rt_accum_samples(self.h, ctypes.byref(n)))
+        return n.value
+
+    def reset(self, stream=None):
+        check(lib().rt_accum_reset(self.h, stream))
+
+    def launch(self, scene, cam, params, frame, stream=None):
+        """rt_launch_accum into a Frame of device pointers; returns LaunchStats."""
+        st = LaunchStats()
+        check(lib().rt_launch_accum(scene.h, ctypes.byref(cam), ctypes.byref(params), self.h, ctypes.byref(frame),
+                                    stream, ctypes.byref(st)))
+        return st
+
+    def save(self, stream=None):
+        """The checkpoint as bytes."""
+        n = ctypes.c_size_t()
+        check(lib().rt_accum_state_size(self.h, ctypes.byref(n)))
+        buf = ctypes.create_string_buffer(n.value)
+        check(lib().rt_accum_save(self.h, buf, n.value, stream))
+        return buf.raw
+
+    def load(self, state, stream=None):
+        buf = ctypes.create_string_buffer(bytes(state), len(state))
+        check(lib().rt_accum_load(self.h, buf, len(state), stream))
 
 
 def tuning_set(tuning=None):

@@ -1,4 +1,5 @@
 // rt_api.cu -- C ABI glue: error reporting, version, camera set-up.
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <string>
@@ -9,6 +10,15 @@
 namespace rt {
 namespace {
 thread_local std::string g_last_error;
+std::atomic<long long> g_fail_alloc{0};   // allocations until the injected failure (0: none)
+}
+
+bool injected_alloc_failure() {
+    long long n = g_fail_alloc.load();
+    while (n > 0) {
+        if (g_fail_alloc.compare_exchange_weak(n, n - 1)) return n == 1;
+    }
+    return false;
 }
 
 void set_last_error(const std::string& msg) { g_last_error = msg; }
@@ -38,6 +48,11 @@ using namespace rt;
 extern "C" {
 
 const char* rt_last_error_string(void) { return g_last_error.c_str(); }
+
+rt_status rt_debug_fail_alloc(unsigned int n) {
+    g_fail_alloc.store((long long)n);
+    return RT_OK;
+}
 
 const char* rt_version(void) { return "rtxplay_gb300 0.1 sm_103a"; }
 

@@ -24,6 +24,10 @@ void clear_last_error();
 
 [[noreturn]] void throw_cuda(cudaError_t e, const char* what, const char* file, int line);
 
+// Fault injection (rt_debug_fail_alloc): true when this device allocation is
+// the one chosen to fail.
+bool injected_alloc_failure();
+
 #define RT_CUDA(call)                                                        \
     do {                                                                     \
         cudaError_t rt_e_ = (call);                                          \
@@ -78,6 +82,8 @@ struct DevBuf {
         if (n <= bytes) return;
         release();
         if (n == 0) return;
+        if (injected_alloc_failure())
+            throw Error(RT_ERR_OUT_OF_MEMORY, "cudaMalloc of " + std::to_string(n) + " bytes failed (injected)");
         cudaError_t e = cudaMalloc(&p, n);
         if (e == cudaErrorMemoryAllocation) {
             cudaGetLastError();

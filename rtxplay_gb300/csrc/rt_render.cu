@@ -61,6 +61,8 @@ struct JobDev {              // one render job on the device
     CamDev cam;
     float3 ambient, white;
     uint32_t W, H, npix, spp, depth, seed, key1;
+    uint32_t first_sample;   // sample index of the job's first sample (progressive rendering)
+    uint32_t mean_spp;       // samples per pixel in the sums (spp, or more when accumulating)
     int root;                // root node of the job's scene, -1: empty scene
     uint32_t pix_offset;     // first pixel of the job in the accumulators
     int guides;
@@ -174,7 +176,7 @@ __global__ void __launch_bounds__(kThreads) k_generate(const JobDev* __restrict_
     const uint32_t jx = job_of_path(jobs, nj, i);
     const JobDev& j = jobs[jx];
     const uint32_t pid = uint32_t(i - j.path_offset);
-    const uint32_t pixel = pid / j.spp, sample = pid % j.spp;
+    const uint32_t pixel = pid / j.spp, sample = j.first_sample + pid % j.spp;
     float3 o, d;
     make_camera_ray(j, pixel, sample, o, d);
     q.ori[i] = make_float4(o.x, o.y, o.z, __uint_as_float(pixel));
@@ -457,7 +459,7 @@ __global__ void __launch_bounds__(kB, 1024 / kB)
                 const JobDev& j = jobs[jx];
                 const uint32_t pid = uint32_t(g - j.path_offset);
                 pixel = pid / j.spp;
-                sample = pid % j.spp;
+                sample = j.first_sample + pid % j.spp;
                 make_camera_ray(j, pixel, sample, no, nd);
                 nthr = mk(1.f, 1.f, 1.f);
                 gN = mk(0.f, 0.f, 0.f);
@@ -537,8 +539,9 @@ __global__ void __launch_bounds__(kThreads) k_finalize(const JobDev* __restrict_
     if (gp < total_pix) {
         const JobDev& j = jobs[job_of_pixel(jobs, nj, gp)];
         const uint32_t p = gp - j.pix_offset;
-        j.rawRGB[p] = rt_float3{clamp01(fx_mean(acc.col[0][gp], j.spp)), clamp01(fx_mean(acc.col[1][gp], j.spp)),
-                                clamp01(fx_mean(acc.col[2][gp], j.spp))};
+        j.rawRGB[p] = rt_float3{clamp01(fx_mean(acc.col[0][gp], j.mean_spp)),
+                                clamp01(fx_mean(acc.col[1][gp], j.mean_spp)),
+                                clamp01(fx_mean(acc.col[2][gp], j.mean_spp))};
         r = acc.rays[gp];
         if (j.rpp) j.rpp[p] = acc.rays[gp];
         if (j.guides) {
@@ -828,8 +831,17 @@ void build_wave_graph(Workspace& ws, const WaveLaunch& L) {
 
 }  // namespace
 
-void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s, rt_launch_stats* stats) {
+void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s, rt_launch_stats* stats,
+                 AccumState* accum) {
     RT_REQUIRE(!jobs.empty(), "no jobs to render");
+    if (accum) {
+        RT_REQUIRE(jobs.size() == 1, "an accumulator takes one job");
+        const rt_launch_params& p = jobs[0].params;
+        RT_REQUIRE(p.image_w == accum->W && p.image_h == accum->H, "image size differs from the accumulator's");
+        RT_REQUIRE(!(p.flags & RT_FLAG_GUIDES), "RT_FLAG_GUIDES is not supported with an accumulator");
+        // the per-pixel ray count is u32 and the RNG's sample index u32
+        RT_REQUIRE((accum->samples + p.spp) * p.depth < (1ull << 32), "accumulator full (samples x depth >= 2^32)");
+    }
     uint32_t flags_union = 0;
     for (const Job& j : jobs) {
         check_params(&j.params);
@@ -865,6 +877,8 @@ void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s
         d.depth = jb.params.depth;
         d.seed = jb.params.seed;
         d.key1 = 0;
+        d.first_sample = accum ? uint32_t(accum->samples) : 0u;
+        d.mean_spp = accum ? uint32_t(accum->samples + d.spp) : d.spp;
         d.root = g.root(jb.seg);
         d.pix_offset = uint32_t(total_pix);
         d.guides = (jb.params.flags & RT_FLAG_GUIDES) ? 1 : 0;
@@ -924,7 +938,7 @@ void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s
     L.geo = g.view();
     L.things = g.things_dev.as<ThingDev>();
     {
-        unsigned long long* c = ws.acc.as<unsigned long long>();
+        unsigned long long* c = accum ? accum->sums.as<unsigned long long>() : ws.acc.as<unsigned long long>();
         for (int k = 0; k < 3; ++k) L.acc.col[k] = c + size_t(k) * total_pix;
         L.acc.rays = reinterpret_cast<uint32_t*>(c + 3 * size_t(total_pix));
         unsigned long long* gd = any_guides ? ws.acc_gd.as<unsigned long long>() : nullptr;
@@ -933,7 +947,7 @@ void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s
     L.any_guides = any_guides;
 
     RT_CUDA(cudaMemcpyAsync(ws.jobs.p, ws.jobs_host.data(), size_t(nj) * sizeof(JobDev), cudaMemcpyHostToDevice, s));
-    RT_CUDA(cudaMemsetAsync(ws.acc.p, 0, size_t(total_pix) * 28, s));
+    if (!accum) RT_CUDA(cudaMemsetAsync(ws.acc.p, 0, size_t(total_pix) * 28, s));
     if (any_guides) RT_CUDA(cudaMemsetAsync(ws.acc_gd.p, 0, size_t(total_pix) * 48, s));
     const uint32_t n0 = W;
     k_init_state<<<1, 1, 0, s>>>(L.st, n0, total_paths, uint32_t(max_iter64), W);
@@ -1005,10 +1019,17 @@ void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s
     const WaveState hs = *ws.host_state;
     if (hs.err & 1u) throw Error(RT_ERR_LIMIT, "traversal stack overflow (LBVH deeper than the stack)");
     if (hs.err & 2u) throw Error(RT_ERR_LIMIT, "wave loop exceeded its bound");
+    // with an accumulator the pixel sums (and so hs.rays) cover every sample so far
+    unsigned long long launch_rays = hs.rays;
+    if (accum) {
+        launch_rays = hs.rays - accum->rays;
+        accum->rays = hs.rays;
+        accum->samples += jobs[0].params.spp;
+    }
     if (use_graph) launches += 3 * hs.iter;
     if (stats) {
         std::memset(stats, 0, sizeof(*stats));
-        stats->rays = hs.rays;
+        stats->rays = launch_rays;
         stats->paths = total_paths;
         stats->node_visits = hs.nodes;
         stats->prim_tests = hs.prims;
@@ -1057,7 +1078,7 @@ void first_hit_rect(Scene& sc, const rt_camera& cam, const rt_launch_params& p, 
 }
 
 void render_scene(Scene& sc, const rt_camera& cam, const rt_launch_params& p, const rt_frame& f, cudaStream_t s,
-                  rt_launch_stats* stats) {
+                  rt_launch_stats* stats, AccumState* accum = nullptr) {
     if (!sc.built || sc.topology_dirty) throw Error(RT_ERR_NOT_BUILT, "scene not built (call rt_scene_build)");
     if (sc.xf_dirty) throw Error(RT_ERR_NOT_BUILT, "transforms changed; call rt_scene_update");
     sync_optics(sc.geo, {&sc}, s);
@@ -1066,7 +1087,22 @@ void render_scene(Scene& sc, const rt_camera& cam, const rt_launch_params& p, co
     jobs[0].cam = cam;
     jobs[0].params = p;
     jobs[0].frame = f;
-    render_jobs(sc.geo, jobs, s, stats);
+    render_jobs(sc.geo, jobs, s, stats, accum);
+}
+
+// Checkpoint bytes of an accumulator: a header, then the sums as on the device.
+struct AccumHeader {
+    char magic[8];   // "rtaccum1"
+    uint32_t W, H;
+    unsigned long long samples, rays;
+    unsigned long long sum_bytes;
+};
+
+size_t accum_sum_bytes(const AccumState& a) { return size_t(a.W) * a.H * 28; }
+
+AccumState* accum_from(rt_accum a) {
+    RT_REQUIRE(a != nullptr, "accumulator handle is NULL");
+    return reinterpret_cast<AccumState*>(a);
 }
 
 void postproc(const rt_float3* src, rt_uchar4* dst, int w, int h, int mode, cudaStream_t s) {
@@ -1120,6 +1156,100 @@ Batch* batch_from(rt_batch b) {
 using namespace rt;
 
 extern "C" {
+
+rt_status rt_accum_create(rt_accum* out, unsigned int w, unsigned int h) {
+    return guarded([&] {
+        RT_REQUIRE(out != nullptr, "out is NULL");
+        RT_REQUIRE(w > 0 && h > 0 && uint64_t(w) * h < (1ull << 31), "bad accumulator size");
+        auto* a = new AccumState();
+        try {
+            a->W = w;
+            a->H = h;
+            a->sums.reserve(accum_sum_bytes(*a));
+            RT_CUDA(cudaMemset(a->sums.p, 0, accum_sum_bytes(*a)));
+        } catch (...) {
+            delete a;
+            throw;
+        }
+        *out = reinterpret_cast<rt_accum>(a);
+    });
+}
+
+rt_status rt_accum_destroy(rt_accum acc) {
+    return guarded([&] { delete reinterpret_cast<AccumState*>(acc); });
+}
+
+rt_status rt_accum_reset(rt_accum acc, void* stream) {
+    return guarded([&] {
+        AccumState* a = accum_from(acc);
+        cudaStream_t s = as_stream(stream);
+        RT_CUDA(cudaMemsetAsync(a->sums.p, 0, accum_sum_bytes(*a), s));
+        RT_CUDA(cudaStreamSynchronize(s));
+        a->samples = 0;
+        a->rays = 0;
+    });
+}
+
+rt_status rt_accum_samples(rt_accum acc, unsigned long long* samples) {
+    return guarded([&] {
+        RT_REQUIRE(samples != nullptr, "samples is NULL");
+        *samples = accum_from(acc)->samples;
+    });
+}
+
+rt_status rt_launch_accum(rt_scene scene, const rt_camera* cam, const rt_launch_params* params, rt_accum acc,
+                          const rt_frame* frame, void* stream, rt_launch_stats* stats) {
+    return guarded([&] {
+        RT_REQUIRE(cam && params && frame, "cam/params/frame is NULL");
+        AccumState* a = accum_from(acc);
+        render_scene(*scene_from(scene), *cam, *params, *frame, as_stream(stream), stats, a);
+    });
+}
+
+rt_status rt_accum_state_size(rt_accum acc, size_t* bytes) {
+    return guarded([&] {
+        RT_REQUIRE(bytes != nullptr, "bytes is NULL");
+        *bytes = sizeof(AccumHeader) + accum_sum_bytes(*accum_from(acc));
+    });
+}
+
+rt_status rt_accum_save(rt_accum acc, void* host, size_t bytes, void* stream) {
+    return guarded([&] {
+        AccumState* a = accum_from(acc);
+        RT_REQUIRE(host != nullptr, "host is NULL");
+        RT_REQUIRE(bytes == sizeof(AccumHeader) + accum_sum_bytes(*a), "state size differs (rt_accum_state_size)");
+        AccumHeader h{};
+        std::memcpy(h.magic, "rtaccum1", 8);
+        h.W = a->W;
+        h.H = a->H;
+        h.samples = a->samples;
+        h.rays = a->rays;
+        h.sum_bytes = accum_sum_bytes(*a);
+        std::memcpy(host, &h, sizeof h);
+        cudaStream_t s = as_stream(stream);
+        RT_CUDA(cudaMemcpyAsync(static_cast<char*>(host) + sizeof h, a->sums.p, h.sum_bytes, cudaMemcpyDeviceToHost, s));
+        RT_CUDA(cudaStreamSynchronize(s));
+    });
+}
+
+rt_status rt_accum_load(rt_accum acc, const void* host, size_t bytes, void* stream) {
+    return guarded([&] {
+        AccumState* a = accum_from(acc);
+        RT_REQUIRE(host != nullptr, "host is NULL");
+        RT_REQUIRE(bytes == sizeof(AccumHeader) + accum_sum_bytes(*a), "state size differs (rt_accum_state_size)");
+        AccumHeader h;
+        std::memcpy(&h, host, sizeof h);
+        RT_REQUIRE(std::memcmp(h.magic, "rtaccum1", 8) == 0, "not an accumulator state");
+        RT_REQUIRE(h.W == a->W && h.H == a->H && h.sum_bytes == accum_sum_bytes(*a),
+                   "accumulator state of another image size");
+        cudaStream_t s = as_stream(stream);
+        RT_CUDA(cudaMemcpyAsync(a->sums.p, static_cast<const char*>(host) + sizeof h, h.sum_bytes,
+                                cudaMemcpyHostToDevice, s));
+        RT_CUDA(cudaStreamSynchronize(s));
+        a->samples = h.samples;
+        a->rays = h.rays;
+    });
+}
 
 rt_status rt_tuning_set(const rt_tuning* tuning) {
     return guarded([&] {
@@ -1333,6 +1463,7 @@ rt_status rt_batch_build(rt_batch b, unsigned int morton_bits, void* stream) {
     return guarded([&] {
         Batch* B = batch_from(b);
         RT_REQUIRE(!B->scenes.empty(), "batch is empty");
+        B->built = false;   // a build that fails half way leaves no launchable batch behind
         build_geometry(B->geo, B->scenes, int(morton_bits), B->layout, as_stream(stream));
         B->built = true;
     });

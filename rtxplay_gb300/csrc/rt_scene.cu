@@ -995,6 +995,7 @@ Scene* scene_from(rt_scene h) {
 namespace {
 
 void scene_build(Scene& sc, int morton_bits, cudaStream_t s) {
+    sc.built = false;   // a build that fails half way leaves no renderable scene behind
     build_geometry(sc.geo, {&sc}, morton_bits, sc.layout, s);
     sc.built = true;
     sc.topology_dirty = false;

@@ -140,12 +140,24 @@ struct Job {
     rt_frame frame;
 };
 
+// Pixel sums kept across launches (rt_accum): 3 x u64 colour + u32 rays per
+// pixel, and the samples per pixel they hold.
+struct AccumState {
+    uint32_t W = 0, H = 0;
+    unsigned long long samples = 0;
+    unsigned long long rays = 0;   // sum of the per-pixel ray counts
+    DevBuf sums;
+};
+
 // Device camera of a host camera; launch-parameter validation (rt_render.cu).
 CamDev cam_dev(const rt_camera& c);
 void check_params(const rt_launch_params* p);
 
 // Renders all jobs over `g` in one wavefront (rt_render.cu).
-void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s, rt_launch_stats* stats);
+// With `accum` (one job only): samples [accum->samples, + spp) of every pixel
+// are added to its sums and the frame is their mean over all samples so far.
+void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s, rt_launch_stats* stats,
+                 AccumState* accum = nullptr);
 
 // One adjoint job: the rendered image of a job, dL/d(clamped image) and the
 // output gradients (device pointers; a NULL output is skipped).

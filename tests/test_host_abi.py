@@ -120,3 +120,26 @@ def test_add_things_checks_everything_first(product):
     first = ctypes.c_uint()
     assert R.lib().rt_scene_add_things(sc.h, 2, None, None, None, ctypes.byref(first)) == R.RT_ERR_INVALID_ARG
     sc.close()
+
+
+def test_accum_host_errors(product):
+    """Accumulator calls check their arguments before any device work."""
+    R = product
+    lib = R.lib()
+    h = ctypes.c_void_p()
+    assert lib.rt_accum_create(None, 4, 4) == R.RT_ERR_INVALID_ARG
+    assert lib.rt_accum_create(ctypes.byref(h), 0, 4) == R.RT_ERR_INVALID_ARG
+    assert lib.rt_accum_create(ctypes.byref(h), 1 << 16, 1 << 15) == R.RT_ERR_INVALID_ARG
+    n = ctypes.c_ulonglong()
+    assert lib.rt_accum_samples(None, ctypes.byref(n)) == R.RT_ERR_INVALID_ARG
+    sz = ctypes.c_size_t()
+    assert lib.rt_accum_state_size(None, ctypes.byref(sz)) == R.RT_ERR_INVALID_ARG
+    assert lib.rt_accum_destroy(None) == R.RT_OK
+    assert lib.rt_launch_accum(None, None, None, None, None, None, None) == R.RT_ERR_INVALID_ARG
+
+
+def test_fail_alloc_hook_without_device(product):
+    """The injection hook is host state; a zero switches it off."""
+    R = product
+    assert R.lib().rt_debug_fail_alloc(3) == R.RT_OK
+    assert R.lib().rt_debug_fail_alloc(0) == R.RT_OK
