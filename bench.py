@@ -321,6 +321,10 @@ def batched_leg(R, torch, sptr, stream, nscenes, steps, tuning_mode):
             "batched_mrays_s": b_rays / (bm * 1e-3) / 1e6, "serial_mrays_s": s_rays / (sm * 1e-3) / 1e6,
             "images_equal_first8": bool(equal and b_rays == s_rays),
             "build_batched_s": batch_build_s, "build_serial_s": serial_build_s,
+            # the same comparison with the hierarchy builds included (one segmented build
+            # of all scenes against one build per scene)
+            "batched_with_build_ms": bm + batch_build_s * 1e3, "serial_with_build_ms": sm + serial_build_s * 1e3,
+            "speedup_with_build": (sm + serial_build_s * 1e3) / (bm + batch_build_s * 1e3),
             "device_gib": binfo["device_bytes"] / 2**30,
             "tuning_batched": t_batch, "tuning_serial": t_serial,
             "workload": "256 random final-scene variants: half-extent U{2..11}, level U{2..6}, "

@@ -154,6 +154,19 @@ public:
               "rt_launcher_ignite");
         return st;
     }
+    // Progressive form of ignite (no reference counterpart): the next p.spp
+    // samples go into `acc`, the launcher's buffers get the mean over all of
+    // its samples (image through pp_sRGB as ignite does).
+    rt_launch_stats ignite(const Scene& scene, const Camera& cam, const rt_launch_params& p, rt_accum acc,
+                           void* stream = nullptr) {
+        rt_frame f{};
+        rt_uchar4* image = nullptr;
+        check(rt_launcher_frame(l_, &f, &image, nullptr), "rt_launcher_frame");
+        rt_launch_stats st{};
+        check(rt_launch_accum(scene.handle(), cam.abi(), &p, acc, &f, stream, &st), "rt_launch_accum");
+        check(rt_postproc_srgb(f.rawRGB, image, int(w_), int(h_), stream), "rt_postproc_srgb");
+        return st;
+    }
     void download(rt_float3* raw, unsigned int* rpp, rt_float3* normals, rt_float3* albedos, rt_uchar4* image,
                   unsigned int* pick_id) {
         check(rt_launcher_download(l_, raw, rpp, normals, albedos, image, pick_id), "rt_launcher_download");
@@ -164,6 +177,33 @@ public:
 private:
     rt_launcher l_ = nullptr;
     unsigned int w_, h_;
+};
+
+// rt_accum: exact pixel sums kept across launches, saved to and restored from
+// host bytes (checkpoint and resume).
+class Accum {
+public:
+    Accum(unsigned int w, unsigned int h) { check(rt_accum_create(&a_, w, h), "rt_accum_create"); }
+    ~Accum() { rt_accum_destroy(a_); }
+    Accum(const Accum&) = delete;
+    Accum& operator=(const Accum&) = delete;
+    rt_accum handle() const { return a_; }
+    unsigned long long samples() const {
+        unsigned long long n = 0;
+        check(rt_accum_samples(a_, &n), "rt_accum_samples");
+        return n;
+    }
+    std::vector<unsigned char> save() const {
+        size_t n = 0;
+        check(rt_accum_state_size(a_, &n), "rt_accum_state_size");
+        std::vector<unsigned char> b(n);
+        check(rt_accum_save(a_, b.data(), n, nullptr), "rt_accum_save");
+        return b;
+    }
+    void load(const std::vector<unsigned char>& b) { check(rt_accum_load(a_, b.data(), b.size(), nullptr), "rt_accum_load"); }
+
+private:
+    rt_accum a_ = nullptr;
 };
 
 }  // namespace rtwo

@@ -1236,12 +1236,15 @@ rt_status rt_accum_load(rt_accum acc, const void* host, size_t bytes, void* stre
     return guarded([&] {
         AccumState* a = accum_from(acc);
         RT_REQUIRE(host != nullptr, "host is NULL");
-        RT_REQUIRE(bytes == sizeof(AccumHeader) + accum_sum_bytes(*a), "state size differs (rt_accum_state_size)");
+        RT_REQUIRE(bytes >= sizeof(AccumHeader), "not an accumulator state (too short)");
         AccumHeader h;
         std::memcpy(&h, host, sizeof h);
         RT_REQUIRE(std::memcmp(h.magic, "rtaccum1", 8) == 0, "not an accumulator state");
-        RT_REQUIRE(h.W == a->W && h.H == a->H && h.sum_bytes == accum_sum_bytes(*a),
-                   "accumulator state of another image size");
+        RT_REQUIRE(h.W == a->W && h.H == a->H,
+                   "accumulator state of another image size (" + std::to_string(h.W) + "x" + std::to_string(h.H) +
+                       ", not " + std::to_string(a->W) + "x" + std::to_string(a->H) + ")");
+        RT_REQUIRE(h.sum_bytes == accum_sum_bytes(*a) && bytes == sizeof h + h.sum_bytes,
+                   "accumulator state truncated or damaged");
         cudaStream_t s = as_stream(stream);
         RT_CUDA(cudaMemcpyAsync(a->sums.p, static_cast<const char*>(host) + sizeof h, h.sum_bytes,
                                 cudaMemcpyHostToDevice, s));

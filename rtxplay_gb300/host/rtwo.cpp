@@ -22,12 +22,19 @@
 //   --seed <n>                      counter-RNG seed (4711)
 //   --scene-seed <n>                glibc rand() seed of the scene recipe (1)
 //   --morton 30|60                  LBVH key width (60)
+//   --resume <file>                 continue a render from a checkpoint: -s more
+//                                   samples on top of the saved ones
+//   --checkpoint <file>             save the pixel sums after rendering (the
+//                                   image is the mean over all samples so far)
 //   --print-args                    print the parsed options as JSON and exit
 // The image goes to stdout as PPM (P3), rows bottom-up (optx/rtwo.cxx:622-666).
 #include <getopt.h>
 
 #include <chrono>
 #include <cstdio>
+#include <fstream>
+#include <iterator>
+#include <memory>
 #include <cstdlib>
 #include <cstring>
 #include <iostream>
@@ -58,6 +65,7 @@ struct Options {
     std::string scene = "rtwo";
     int level = 6;
     unsigned seed = 4711, scene_seed = 1, morton = 60;
+    std::string resume, checkpoint;
     bool print_args = false;
 };
 
@@ -71,7 +79,8 @@ void usage() {
                  "  -S, --print-statistics         -D, --apply-denoiser <type>\n"
                  "  -q, --quiet, --silent          -v, --verbose   -t, --trace-sm   -h, --help, --usage\n"
                  "  --scene rtwo|tess|analytic     --level <n>     --seed <n>\n"
-                 "  --scene-seed <n>               --morton 30|60  --print-args\n";
+                 "  --scene-seed <n>               --morton 30|60  --print-args\n"
+                 "  --resume <file>                --checkpoint <file>\n";
 }
 
 Options parse(int argc, char** argv) {
@@ -96,6 +105,8 @@ Options parse(int argc, char** argv) {
                                    {"seed", required_argument, nullptr, 1003},
                                    {"scene-seed", required_argument, nullptr, 1004},
                                    {"morton", required_argument, nullptr, 1005},
+                                   {"resume", required_argument, nullptr, 1006},
+                                   {"checkpoint", required_argument, nullptr, 1007},
                                    {"print-args", no_argument, &pa, 1},
                                    {nullptr, 0, nullptr, 0}};
     int c;
@@ -149,6 +160,8 @@ Options parse(int argc, char** argv) {
             case 1003: o.seed = unsigned(std::strtoul(optarg, nullptr, 10)); break;
             case 1004: o.scene_seed = unsigned(std::strtoul(optarg, nullptr, 10)); break;
             case 1005: o.morton = unsigned(std::strtoul(optarg, nullptr, 10)); break;
+            case 1006: o.resume = optarg; break;
+            case 1007: o.checkpoint = optarg; break;
             case 0: break;   // long flag stored through its pointer
             default: throw std::invalid_argument("try 'rtwo --help' for more information.");
         }
@@ -216,6 +229,18 @@ void pnm(const char* magic, unsigned w, unsigned h, int maxval, const std::vecto
 
 int clampbyte(float x) { return int((x < 0.f ? 0.f : (x > 1.f ? 1.f : x)) * 255); }
 
+std::vector<unsigned char> read_file(const std::string& path) {
+    std::ifstream f(path, std::ios::binary);
+    if (!f) throw std::runtime_error("cannot read " + path);
+    return std::vector<unsigned char>(std::istreambuf_iterator<char>(f), std::istreambuf_iterator<char>());
+}
+
+void write_file(const std::string& path, const std::vector<unsigned char>& b) {
+    std::ofstream f(path, std::ios::binary);
+    f.write(reinterpret_cast<const char*>(b.data()), std::streamsize(b.size()));
+    if (!f) throw std::runtime_error("cannot write " + path);
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -238,9 +263,11 @@ int main(int argc, char** argv) {
     if (o.print_args) {
         std::printf("{\"w\": %u, \"h\": %u, \"spp\": %u, \"depth\": %u, \"quiet\": %d, \"stats\": %d, \"rpp\": %d, "
                     "\"guides\": %d, \"denoiser\": \"%s\", \"scene\": \"%s\", \"level\": %d, \"seed\": %u, "
-                    "\"scene_seed\": %u, \"morton\": %u, \"verbose\": %d, \"trace\": %d}\n",
+                    "\"scene_seed\": %u, \"morton\": %u, \"verbose\": %d, \"trace\": %d, \"resume\": \"%s\", "
+                    "\"checkpoint\": \"%s\"}\n",
                     w, h, spp, depth, int(o.quiet), int(o.stats), int(o.rpp), int(o.guides), o.denoiser.c_str(),
-                    o.scene.c_str(), o.level, o.seed, o.scene_seed, o.morton, int(o.verbose), int(o.trace));
+                    o.scene.c_str(), o.level, o.seed, o.scene_seed, o.morton, int(o.verbose), int(o.trace),
+                    o.resume.c_str(), o.checkpoint.c_str());
         return 0;
     }
     try {
@@ -264,9 +291,16 @@ int main(int argc, char** argv) {
         p.ambient = rt_float3{.5f, .7f, 1.f};   // miss SBT record, optx/rtwo.cxx:110-111
         p.white = rt_float3{1.f, 1.f, 1.f};
         rtwo::Launcher launcher(w, h);
+        std::unique_ptr<rtwo::Accum> acc;   // progressive render: resumed and/or checkpointed
+        if (!o.resume.empty() || !o.checkpoint.empty()) {
+            if (denoise) throw std::invalid_argument("--resume/--checkpoint do not keep guide layers (-D)");
+            acc.reset(new rtwo::Accum(w, h));
+            if (!o.resume.empty()) acc->load(read_file(o.resume));
+        }
         const auto t0 = std::chrono::high_resolution_clock::now();
-        const rt_launch_stats st = launcher.ignite(scene, camera, p);
+        const rt_launch_stats st = acc ? launcher.ignite(scene, camera, p, acc->handle()) : launcher.ignite(scene, camera, p);
         const auto t1 = std::chrono::high_resolution_clock::now();
+        if (acc && !o.checkpoint.empty()) write_file(o.checkpoint, acc->save());
         const size_t n = size_t(w) * h;
         std::vector<rt_uchar4> image(n);
         std::vector<unsigned int> rpp(n);

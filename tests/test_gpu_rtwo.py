@@ -67,3 +67,28 @@ def test_rtwo_print_args_and_errors(product, cuda):
     assert (a["w"], a["h"], a["spp"], a["depth"]) == (320, 200, 7, 9)
     bad = subprocess.run([exe, "--scene", "nosuch"], capture_output=True, text=True, timeout=60)
     assert bad.returncode != 0 and "rtwo:" in bad.stderr
+
+
+def test_rtwo_checkpoint_and_resume(product, cuda, tmp_path):
+    """rtwo -s 3 --checkpoint f, then rtwo -s 4 --resume f: the image and rays per
+    pixel of one 7-spp render."""
+    R = product
+    exe, w, h, seed = _rtwo(), 64, 48, 9
+    ck = str(tmp_path / "ck.bin")
+    base = [exe, "-g", f"{w}x{h}", "-d", "50", "--scene", "tess", "--level", "2", "--seed", str(seed), "-A", "RPP"]
+    r1 = subprocess.run(base + ["-s", "3", "--checkpoint", ck], capture_output=True, text=True, timeout=300)
+    assert r1.returncode == 0, r1.stderr
+    r2 = subprocess.run(base + ["-s", "4", "--resume", ck, "--checkpoint", ck], capture_output=True, text=True,
+                        timeout=300)
+    assert r2.returncode == 0, r2.stderr
+    blocks = _pnm_blocks(r2.stdout)
+    img = blocks[0][3].reshape(h, w, 3)[::-1].reshape(-1, 3)
+    rpp = blocks[1][3].reshape(h, w)[::-1].reshape(-1)
+    sc = R.rtow_scene(2, R.RT_RECIPE_GLIBC, 1, 11)
+    out = R.render(sc, R.rtow_camera(w, h), R.launch_params(w, h, 7, depth=50, seed=seed))
+    assert np.array_equal(rpp, out["rpp"].astype(np.int64))
+    assert np.array_equal(img, out["image"][:, :3].astype(np.int64))
+    # a checkpoint of another image size is refused
+    bad = subprocess.run([exe, "-g", "32x32", "-s", "1", "--scene", "tess", "--level", "2", "--resume", ck, "-q"],
+                         capture_output=True, text=True, timeout=300)
+    assert bad.returncode != 0 and "image size" in bad.stderr
