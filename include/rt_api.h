@@ -294,7 +294,7 @@ rt_status rt_accum_load(rt_accum acc, const void* host, size_t bytes, void* stre
  * keeps the results in a JSON cache. */
 typedef struct {
     unsigned int wave_log2;            /* rays per wave queue = 2^wave_log2, 16..24 (default 23, or RTX_WAVE) */
-    unsigned int shade_block;          /* threads per shading block: 128, 256 or 512 (default 512) */
+    unsigned int shade_block;          /* threads per shading block: 128, 256, 512 or 1024 (default 512) */
     unsigned int extend_blocks_per_sm; /* persistent traversal blocks per SM, 1..32, capped at what fits
                                           (default: what fits) */
     unsigned int refill_below;         /* a traversal warp takes new rays when at most this many of its

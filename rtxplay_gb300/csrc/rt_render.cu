@@ -698,7 +698,9 @@ LaunchShape launch_shape() {
 using ShadeFn = void (*)(Queues, const float4*, const uint32_t*, WaveState*, const JobDev*, uint32_t, const float4*,
                          const FlatDesc*, const ThingDev*, Acc, int);
 
-ShadeFn shade_fn(int block) { return block == 128 ? k_shade<128> : block == 512 ? k_shade<512> : k_shade<256>; }
+ShadeFn shade_fn(int block) {
+    return block == 128 ? k_shade<128> : block == 512 ? k_shade<512> : block == 1024 ? k_shade<1024> : k_shade<256>;
+}
 
 // The wave loop captured once as a graph: a conditional WHILE node whose body
 // is extend -> shade -> ctrl; rebuilt whenever a baked-in pointer or launch
@@ -1259,8 +1261,9 @@ rt_status rt_tuning_set(const rt_tuning* tuning) {
         rt_tuning t{};
         if (tuning) t = *tuning;
         RT_REQUIRE(t.wave_log2 == 0 || (t.wave_log2 >= 16 && t.wave_log2 <= 24), "wave_log2 outside 16..24");
-        RT_REQUIRE(t.shade_block == 0 || t.shade_block == 128 || t.shade_block == 256 || t.shade_block == 512,
-                   "shade_block must be 128, 256 or 512");
+        RT_REQUIRE(t.shade_block == 0 || t.shade_block == 128 || t.shade_block == 256 || t.shade_block == 512 ||
+                       t.shade_block == 1024,
+                   "shade_block must be 128, 256, 512 or 1024");
         RT_REQUIRE(t.extend_blocks_per_sm <= 32, "extend_blocks_per_sm outside 1..32");
         RT_REQUIRE(t.refill_below <= 31, "refill_below outside 1..31");
         RT_REQUIRE(t.steps_per_check <= 64, "steps_per_check outside 1..64");

@@ -33,7 +33,7 @@ DEFAULT = {"wave_log2": 23, "shade_block": 512, "extend_blocks_per_sm": 0, "refi
 # candidate values per knob (extend_blocks_per_sm 0: as many as fit)
 SPACE = {
     "wave_log2": (20, 21, 22, 23),
-    "shade_block": (128, 256, 512),
+    "shade_block": (128, 256, 512, 1024),
     "extend_blocks_per_sm": (0, 4, 3, 2),
     "refill_below": (4, 8, 12, 16, 20),
     "steps_per_check": (8, 16, 32),

@@ -15,7 +15,8 @@ pytestmark = pytest.mark.gpu
 SHAPES = [
     {"wave_log2": 16, "shade_block": 128, "extend_blocks_per_sm": 1, "refill_below": 1, "steps_per_check": 1},
     {"wave_log2": 16, "shade_block": 512, "extend_blocks_per_sm": 2, "refill_below": 31, "steps_per_check": 64},
-    {"wave_log2": 17, "shade_block": 256, "extend_blocks_per_sm": 32, "refill_below": 20, "steps_per_check": 5},
+    {"wave_log2": 17, "shade_block": 1024, "extend_blocks_per_sm": 32, "refill_below": 20, "steps_per_check": 5},
+    {"wave_log2": 17, "shade_block": 256, "extend_blocks_per_sm": 3, "refill_below": 8, "steps_per_check": 32},
 ]
 
 
