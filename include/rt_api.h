@@ -83,6 +83,8 @@ typedef struct {
 #define RT_FLAG_GUIDES        0x1u  /* write normals/albedos guide layers */
 #define RT_FLAG_STAGE_TIMING  0x2u  /* time the traversal and shading kernels with CUDA events */
 #define RT_FLAG_COUNT_VISITS  0x4u  /* count BVH nodes visited and primitives tested (slower) */
+#define RT_FLAG_RTOW_PIXELS   0x8u  /* rtow's pixel mapping s = 2(x+r)/(w-1) - 1 (rtow.cxx:112-113) instead of
+                                       rtwo's 2(x+r)/w - 1 (optx/camera_i.cu:61); needs w, h >= 2 */
 
 /* Output buffers (device pointers, caller-owned): the image buffers of
  * LpGeneral allocated by Launcher::resize (optx/launcher.cxx:36-47). */

@@ -32,7 +32,7 @@ class _Camera(ctypes.Structure):
     _fields_ = [("eye", ctypes.c_float * 3), ("u", ctypes.c_float * 3), ("v", ctypes.c_float * 3),
                 ("w", ctypes.c_float * 3), ("hvec", ctypes.c_float * 3),
                 ("wvec", ctypes.c_float * 3), ("dvec", ctypes.c_float * 3),
-                ("aperture", ctypes.c_float)]
+                ("aperture", ctypes.c_float), ("rtow_pixels", ctypes.c_int)]
 
 
 _lib = None

@@ -166,15 +166,19 @@ struct GlibcRand {
 struct Cam {
     F3 eye, u, v, w, hvec, wvec, dvec;
     float aperture;
+    bool rtow_px = false;   // rtow's pixel mapping (rtow.cxx:112-113)
 };
 
-// optx/camera.h:67-77 plus the jitter of optx/camera_i.cu:61-65.
+// optx/camera.h:67-77 plus the jitter of optx/camera_i.cu:61-65; with
+// rtow_px the jittered pixel maps over w - 1 and h - 1 as rtow.cxx:112-113.
 inline void camera_ray(const Cam& c, unsigned x, unsigned y, unsigned W, unsigned H, Stream& s,
                        F3& ori, F3& dir) {
     const float jx = s.next();
     const float jy = s.next();
-    const float sx = 2.f * (float(x) + jx) / float(W) - 1.f;
-    const float ty = 2.f * (float(y) + jy) / float(H) - 1.f;
+    const float dw = c.rtow_px ? float(W - 1) : float(W);
+    const float dh = c.rtow_px ? float(H - 1) : float(H);
+    const float sx = 2.f * (float(x) + jx) / dw - 1.f;
+    const float ty = 2.f * (float(y) + jy) / dh - 1.f;
     const F3 r = mul(c.aperture / 2.f, rndVin1disk(s));
     const F3 o = add(mul(r.x, c.u), mul(r.y, c.v));
     ori = add(c.eye, o);
@@ -1086,6 +1090,7 @@ Cam to_cam(const orc_camera* c) {
     k.eye = ld3(c->eye); k.u = ld3(c->u); k.v = ld3(c->v); k.w = ld3(c->w);
     k.hvec = ld3(c->hvec); k.wvec = ld3(c->wvec); k.dvec = ld3(c->dvec);
     k.aperture = c->aperture;
+    k.rtow_px = c->rtow_pixels != 0;
     return k;
 }
 

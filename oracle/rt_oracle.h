@@ -97,6 +97,7 @@ typedef struct {
     float eye[3];
     float u[3], v[3], w[3], hvec[3], wvec[3], dvec[3];
     float aperture;
+    int rtow_pixels;   /* 1: rtow's pixel mapping over w - 1, h - 1 (rtow.cxx:112-113) */
 } orc_camera;
 
 /* Primary-ray closest hit for sample `sample` of every pixel (x,y) of a w*h

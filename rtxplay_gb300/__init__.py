@@ -24,7 +24,7 @@ RT_ERR_LIMIT = 5
 RT_ERR_INTERNAL = 6
 
 RT_OPTICS_DIFFUSE, RT_OPTICS_REFLECT, RT_OPTICS_REFRACT = 0, 1, 2
-RT_FLAG_GUIDES, RT_FLAG_STAGE_TIMING, RT_FLAG_COUNT_VISITS = 0x1, 0x2, 0x4
+RT_FLAG_GUIDES, RT_FLAG_STAGE_TIMING, RT_FLAG_COUNT_VISITS, RT_FLAG_RTOW_PIXELS = 0x1, 0x2, 0x4, 0x8
 RT_RECIPE_GLIBC, RT_RECIPE_COUNTER = 0, 1
 RT_LAYOUT_AUTO, RT_LAYOUT_FLAT, RT_LAYOUT_INSTANCED, RT_LAYOUT_GROUPED, RT_LAYOUT_SAH = 0, 1, 2, 3, 4
 

@@ -51,6 +51,7 @@ struct AdjJob {
     float3 ambient, white;
     uint32_t W, H, npix, spp, depth, seed, key1;
     int root;
+    int rtow_px;             // RT_FLAG_RTOW_PIXELS
     uint32_t thing_begin, nthings;
     unsigned long long path_offset;
     uint32_t pix_offset;     // first pixel of the job in the per-pixel gradient array
@@ -196,7 +197,7 @@ __device__ uint32_t adjoint_path(const AdjJob* __restrict__ jobs, uint32_t nj, u
     float3 o, d;
     {
         Stream s(j.seed, j.key1, pix, smp, 0);
-        camera_ray(j.cam, pix % j.W, pix / j.W, j.W, j.H, s, o, d);
+        camera_ray(j.cam, pix % j.W, pix / j.W, j.W, j.H, j.rtow_px != 0, s, o, d);
     }
     AdjVtx V[kAdjMaxDepth - 1];
     uint32_t ne = 0;
@@ -407,6 +408,7 @@ void adjoint_jobs(const Geometry& g, const std::vector<AdjointJob>& jobs, cudaSt
         d.seed = a.params.seed;
         d.key1 = 0;
         d.root = g.root(a.seg);
+        d.rtow_px = (a.params.flags & RT_FLAG_RTOW_PIXELS) ? 1 : 0;
         d.thing_begin = g.thing_begin[a.seg];
         d.nthings = (a.seg + 1 < g.nsegs ? g.thing_begin[a.seg + 1] : g.nthings) - d.thing_begin;
         d.path_offset = total;

@@ -112,13 +112,16 @@ struct CamDev {
     float aperture;
 };
 
-// optx/camera.h:67-77 with the pixel jitter of optx/camera_i.cu:61-65.
+// optx/camera.h:67-77 with the pixel jitter of optx/camera_i.cu:61-65, or
+// with rtow's mapping over w - 1 and h - 1 (rtow.cxx:112-113) when rtow_px.
 __device__ __forceinline__ void camera_ray(const CamDev& c, uint32_t x, uint32_t y, uint32_t W, uint32_t H,
-                                           Stream& s, float3& ori, float3& dir) {
+                                           bool rtow_px, Stream& s, float3& ori, float3& dir) {
     const float jx = s.next();
     const float jy = s.next();
-    const float sx = 2.f * (float(x) + jx) / float(W) - 1.f;
-    const float ty = 2.f * (float(y) + jy) / float(H) - 1.f;
+    const float dw = rtow_px ? float(W - 1) : float(W);
+    const float dh = rtow_px ? float(H - 1) : float(H);
+    const float sx = 2.f * (float(x) + jx) / dw - 1.f;
+    const float ty = 2.f * (float(y) + jy) / dh - 1.f;
     const float3 r = mul(c.aperture / 2.f, rndVin1disk(s));
     const float3 o = add(mul(r.x, c.u), mul(r.y, c.v));
     ori = add(c.eye, o);

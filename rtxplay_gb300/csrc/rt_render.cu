@@ -50,6 +50,10 @@ void check_params(const rt_launch_params* p) {
     RT_REQUIRE(p->spp >= 1, "spp must be >= 1");
     RT_REQUIRE(uint64_t(p->image_w) * p->image_h * p->spp <= 0xFFFFFFFFull, "w*h*spp must fit in 32 bits");
     RT_REQUIRE(p->depth >= 1 && p->depth <= 255, "depth must be 1..255");
+    RT_REQUIRE((p->flags & ~(RT_FLAG_GUIDES | RT_FLAG_STAGE_TIMING | RT_FLAG_COUNT_VISITS | RT_FLAG_RTOW_PIXELS)) == 0,
+               "unknown flags");
+    if (p->flags & RT_FLAG_RTOW_PIXELS)
+        RT_REQUIRE(p->image_w >= 2 && p->image_h >= 2, "RT_FLAG_RTOW_PIXELS needs an image of at least 2x2");
 }
 
 namespace {
@@ -66,6 +70,7 @@ struct JobDev {              // one render job on the device
     int root;                // root node of the job's scene, -1: empty scene
     uint32_t pix_offset;     // first pixel of the job in the accumulators
     int guides;
+    int rtow_px;             // RT_FLAG_RTOW_PIXELS
     unsigned long long path_offset;   // first global path of the job
     rt_float3* rawRGB;
     uint32_t* rpp;
@@ -140,7 +145,7 @@ __device__ __forceinline__ uint32_t job_of_pixel(const JobDev* __restrict__ jobs
 __device__ __forceinline__ void make_camera_ray(const JobDev& j, uint32_t pixel, uint32_t sample, float3& o,
                                                 float3& d) {
     Stream s(j.seed, j.key1, pixel, sample, 0);
-    camera_ray(j.cam, pixel % j.W, pixel / j.W, j.W, j.H, s, o, d);
+    camera_ray(j.cam, pixel % j.W, pixel / j.W, j.W, j.H, j.rtow_px != 0, s, o, d);
 }
 
 // Queue slot of the i-th ray of a wave: continuing rays first, then the fresh
@@ -589,6 +594,7 @@ struct FirstHitArgs {
     CamDev cam;
     uint32_t W, H, seed, key1, sample, x0, y0, nx, ny;
     int root;
+    int rtow_px;
 };
 
 // Primary-ray closest hit of one sample for a pixel rectangle.
@@ -600,7 +606,7 @@ __global__ void __launch_bounds__(kThreads) k_first_hit(FirstHitArgs a, GeoView 
     const uint32_t pixel = a.W * y + x;
     Stream s(a.seed, a.key1, pixel, a.sample, 0);
     float3 o, d;
-    camera_ray(a.cam, x, y, a.W, a.H, s, o, d);
+    camera_ray(a.cam, x, y, a.W, a.H, a.rtow_px != 0, s, o, d);
     uint32_t nv = 0, nt = 0;
     const HitRec h = closest_hit_any<false>(g, a.root, o, d, nv, nt);
     if (h.overflow) atomicOr(err, 1u);
@@ -884,6 +890,7 @@ void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s
         d.root = g.root(jb.seg);
         d.pix_offset = uint32_t(total_pix);
         d.guides = (jb.params.flags & RT_FLAG_GUIDES) ? 1 : 0;
+        d.rtow_px = (jb.params.flags & RT_FLAG_RTOW_PIXELS) ? 1 : 0;
         d.path_offset = total_paths;
         d.rawRGB = jb.frame.rawRGB;
         d.rpp = jb.frame.rpp;
@@ -1069,6 +1076,7 @@ void first_hit_rect(Scene& sc, const rt_camera& cam, const rt_launch_params& p, 
     a.nx = nx;
     a.ny = ny;
     a.root = sc.geo.root(0);
+    a.rtow_px = (p.flags & RT_FLAG_RTOW_PIXELS) ? 1 : 0;
     uint32_t* err = sc.geo.misc.as<uint32_t>();
     RT_CUDA(cudaMemsetAsync(err, 0, 4, s));
     k_first_hit<<<grid_for(uint64_t(nx) * ny), kThreads, 0, s>>>(a, sc.geo.view(), prim, thing, t, u, v, t64, err);

@@ -60,9 +60,11 @@ def device_first_hit(R, torch, sc, cam, params, sample=0):
                 u=u.cpu().numpy(), v=v.cpu().numpy(), t64=t64.cpu().numpy())
 
 
-def oracle_camera(O, cam):
-    """Oracle camera struct from the product's rt_camera (same float bits)."""
+def oracle_camera(O, cam, rtow_pixels=False):
+    """Oracle camera struct from the product's rt_camera (same float bits); rtow_pixels:
+    rtow's pixel mapping, the product's RT_FLAG_RTOW_PIXELS."""
     oc = O._Camera()
+    oc.rtow_pixels = 1 if rtow_pixels else 0
     oc.eye[:] = [cam.eye.x, cam.eye.y, cam.eye.z]
     for name in ("u", "v", "w", "hvec", "wvec", "dvec"):
         f = getattr(cam, name)
