@@ -47,24 +47,27 @@ def _close(a, b, rel=1e-9):
     assert np.abs(a - b).max() <= rel * scale, (np.abs(a - b).max(), scale)
 
 
-@pytest.mark.parametrize("level,spp,depth", [(None, 8, 8), (2, 6, 8), (3, 4, 16)])
-def test_adjoint_matches_fp64_oracle(product, oracle, cuda, level, spp, depth):
+@pytest.mark.parametrize("level,spp,depth,rtow_px", [(None, 8, 8, False), (2, 6, 8, False), (3, 4, 16, False),
+                                                     (2, 5, 8, True)])
+def test_adjoint_matches_fp64_oracle(product, oracle, cuda, level, spp, depth, rtow_px):
     R, O, torch = product, oracle, cuda
     W, H, seed = 40, 30, 9
     sc = R.rtow_scene(level, R.RT_RECIPE_GLIBC, 1, 3)
     wd, _ = O.rtow_world(level, 0, 1, 3)
     cam = R.rtow_camera(W, H)
-    params = R.launch_params(W, H, spp, depth=depth, seed=seed, ambient=AMB, white=WHT)
+    params = R.launch_params(W, H, spp, depth=depth, seed=seed, ambient=AMB, white=WHT,
+                             flags=R.RT_FLAG_RTOW_PIXELS if rtow_px else 0)
     img = _render(R, torch, sc, cam, params)
     I = img.cpu().numpy().reshape(-1, 3)
-    ref_img = wd.render(oracle_camera(O, cam), W, H, spp, depth, seed, ambient=AMB, white=WHT, guides=False)
+    ocam = oracle_camera(O, cam, rtow_pixels=rtow_px)
+    ref_img = wd.render(ocam, W, H, spp, depth, seed, ambient=AMB, white=WHT, guides=False)
     assert np.array_equal(I.view(np.uint32), ref_img["rawRGB"].view(np.uint32))
     rng = np.random.default_rng(3)
     T = np.clip(I + rng.normal(0, 0.05, I.shape), 0, 1).astype(np.float32)
     G = (2.0 * (np.clip(I, 0, 1) - T)).astype(np.float32)
     g_dev = torch.from_numpy(G.reshape(-1)).cuda()
     got = _adjoint(R, torch, sc, cam, params, img, g_dev)
-    ref = wd.adjoint(oracle_camera(O, cam), W, H, spp, depth, seed, I, G, ambient=AMB, white=WHT)
+    ref = wd.adjoint(ocam, W, H, spp, depth, seed, I, G, ambient=AMB, white=WHT)
     _close(got["albedo"], ref["albedo"], rel=1e-5)   # binary32 terms against FP64 ones
     _close(got["sky"], ref["sky"], rel=1e-5)
     if np.abs(ref["fuzz"]).max() > 0:
