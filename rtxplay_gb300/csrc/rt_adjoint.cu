@@ -380,6 +380,7 @@ AdjWorkspace& adj_workspace() {
 }  // namespace
 
 void adjoint_jobs(const Geometry& g, const std::vector<AdjointJob>& jobs, cudaStream_t s) {
+    NvtxRange nvtx("rt adjoint");
     RT_REQUIRE(!jobs.empty(), "no adjoint jobs");
     RT_REQUIRE(jobs.size() < (1u << 24), "too many jobs (>= 2^24)");
     AdjWorkspace& ws = adj_workspace();

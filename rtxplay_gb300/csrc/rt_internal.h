@@ -7,6 +7,7 @@
 #include <string>
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include "../../include/rt_api.h"
 
@@ -23,6 +24,15 @@ void set_last_error(const std::string& msg);
 void clear_last_error();
 
 [[noreturn]] void throw_cuda(cudaError_t e, const char* what, const char* file, int line);
+
+// NVTX range for the scope (header-only NVTX v3: a no-op unless a profiler
+// such as ncu or nsys is attached; `ncu --nvtx --nvtx-include` filters by it).
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // Fault injection (rt_debug_fail_alloc): true when this device allocation is
 // the one chosen to fail.

@@ -841,6 +841,7 @@ void build_wave_graph(Workspace& ws, const WaveLaunch& L) {
 
 void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s, rt_launch_stats* stats,
                  AccumState* accum) {
+    NvtxRange nvtx("rt render");
     RT_REQUIRE(!jobs.empty(), "no jobs to render");
     if (accum) {
         RT_REQUIRE(jobs.size() == 1, "an accumulator takes one job");
@@ -979,6 +980,7 @@ void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s
             build_wave_graph(ws, L);
             ws.graph.key = key;
         }
+        NvtxRange nvtx_loop("wave loop (graph)");
         RT_CUDA(cudaGraphLaunch(ws.graph.exec, s));
     } else {
         size_t ev = 0;
@@ -999,16 +1001,22 @@ void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s
                     timed.push_back({ev, 0});
                     ev += 2;
                 }
-                RT_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(L.ext_fn), dim3(L.egrid), dim3(kThreads),
-                                         ext_args, 0, s));
+                {
+                    NvtxRange r("wave: extend");
+                    RT_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(L.ext_fn), dim3(L.egrid),
+                                             dim3(kThreads), ext_args, 0, s));
+                }
                 if (stage_timing) {
                     RT_CUDA(cudaEventRecord(ws.event(ev - 1), s));
                     RT_CUDA(cudaEventRecord(ws.event(ev), s));
                     timed.push_back({ev, 1});
                     ev += 2;
                 }
-                RT_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(L.shade), dim3(L.sgrid),
-                                         dim3(unsigned(L.sblock)), shade_args, 0, s));
+                {
+                    NvtxRange r("wave: shade");
+                    RT_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(L.shade), dim3(L.sgrid),
+                                             dim3(unsigned(L.sblock)), shade_args, 0, s));
+                }
                 if (stage_timing) RT_CUDA(cudaEventRecord(ws.event(ev - 1), s));
                 k_wave_ctrl<<<1, 1, 0, s>>>(L.st, no_handle, 0);
                 RT_CHECK_LAUNCH();

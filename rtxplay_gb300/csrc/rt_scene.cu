@@ -793,6 +793,7 @@ void build_lbvh(Lbvh& L, int morton_bits, cudaStream_t s, const FlatDesc* desc =
                                                         L.bounds.as<uint32_t>(), 0);
     RT_CHECK_LAUNCH();
     if (L.sah) {
+        NvtxRange nvtx("rt build: binned SAH");
         build_sah_topology(L, sah_cluster_max(), s);
     } else if (L.grouped) {
         const uint32_t T = nthings;
@@ -864,6 +865,7 @@ void set_blas_roots(const Lbvh& blas, std::vector<FlatDesc>& desc, std::vector<I
 }
 
 void build_geometry(Geometry& g, const std::vector<Scene*>& scenes, int morton_bits, int layout, cudaStream_t s) {
+    NvtxRange nvtx("rt build");
     RT_REQUIRE(morton_bits == 0 || morton_bits == 30 || morton_bits == 60, "morton_bits must be 0, 30 or 60");
     RT_REQUIRE(layout >= RT_LAYOUT_AUTO && layout <= RT_LAYOUT_SAH, "unknown layout");
     RT_REQUIRE(!scenes.empty(), "no scenes to build");
@@ -904,6 +906,7 @@ void build_geometry(Geometry& g, const std::vector<Scene*>& scenes, int morton_b
 }
 
 void refit_geometry(Geometry& g, const std::vector<Scene*>& scenes, cudaStream_t s) {
+    NvtxRange nvtx("rt refit");
     const Plan P = make_plan(scenes, g.layout_req);
     if (P.inst_class != g.inst_class || P.ntop != g.top.nprims || P.nbottom != g.blas.nprims) {
         // a thing changed between instanced and flattened: the hierarchy changes
