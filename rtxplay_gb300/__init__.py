@@ -13,7 +13,9 @@ import numpy as np
 
 from . import _build
 
-LIB_PATH = _build.LIB
+# RTX_LIB: another build of the same library (the bounds-checked variant of
+# _build.build_checked()); never a non-native fallback
+LIB_PATH = os.environ.get("RTX_LIB") or _build.LIB
 
 RT_OK = 0
 RT_ERR_INVALID_ARG = 1

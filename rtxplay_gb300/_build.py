@@ -2,7 +2,9 @@
 
 ``build_library()`` compiles every ``csrc/*.cu`` translation unit in parallel
 and links ``rtxplay_gb300/_build/librtxplay_gb300.so``; ``build_rtwo()`` builds
-the ``rtwo`` command-line launcher against it.  Arithmetic-sensitive flags:
+the ``rtwo`` command-line launcher against it; ``build_checked()`` builds the
+bounds-checked debug variant (``-DRT_CHECKS``) into ``_build/checked/``, which
+a process loads instead by setting ``RTX_LIB`` to its path.  Arithmetic-sensitive flags:
 ``--fmad=false`` (no silent multiply-add contraction on the device),
 ``-prec-div/-prec-sqrt=true`` (IEEE division and square root) and
 ``-ffp-contract=off`` for host code, so device kernels, the host camera
@@ -51,8 +53,8 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def _compile(src, extra):
-    obj = os.path.join(OUT, os.path.basename(src)[:-3] + ".o")
+def _compile(src, extra, out=OUT):
+    obj = os.path.join(out, os.path.basename(src)[:-3] + ".o")
     if _stale(obj, [src, __file__] + _headers()):
         cmd = [nvcc()] + NVCC_FLAGS + extra + ["-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -61,20 +63,29 @@ def _compile(src, extra):
     return obj
 
 
-def build_library(extra=(), verbose=False, jobs=None):
-    """Compiles and links librtxplay_gb300.so (incremental); returns its path."""
-    os.makedirs(OUT, exist_ok=True)
+def build_library(extra=(), verbose=False, jobs=None, out=OUT):
+    """Compiles and links librtxplay_gb300.so into `out` (incremental); returns its path."""
+    os.makedirs(out, exist_ok=True)
+    lib = os.path.join(out, os.path.basename(LIB))
     srcs = _sources()
     with cf.ThreadPoolExecutor(max_workers=jobs or min(8, len(srcs))) as ex:
-        objs = list(ex.map(lambda s: _compile(s, list(extra)), srcs))
-    if _stale(LIB, objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart_static", "-lrt", "-ldl", "-lpthread"]
+        objs = list(ex.map(lambda s: _compile(s, list(extra), out), srcs))
+    if _stale(lib, objs):
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", lib] + objs + ["-lcudart_static", "-lrt", "-ldl", "-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     if verbose:
-        print("built", LIB)
-    return LIB
+        print("built", lib)
+    return lib
+
+
+CHECKED = os.path.join(OUT, "checked")
+
+
+def build_checked(verbose=False):
+    """The bounds-checked debug variant (-DRT_CHECKS); returns its path."""
+    return build_library(extra=("-DRT_CHECKS",), verbose=verbose, out=CHECKED)
 
 
 def build_rtwo():

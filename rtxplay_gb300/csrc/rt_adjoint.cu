@@ -439,7 +439,9 @@ void adjoint_jobs(const Geometry& g, const std::vector<AdjointJob>& jobs, cudaSt
                                                                            uint32_t(total_pix), ws.gpix.as<float>());
         RT_CHECK_LAUNCH();
         const unsigned grid = unsigned((total + kAdjPathsPerBlock - 1) / kAdjPathsPerBlock);
-        k_adjoint<<<grid, kAdjThreads, shmem, s>>>(ws.jobs.as<AdjJob>(), nj, total, g.view(),
+        GeoView gv = g.view();
+        gv.err = ws.err.as<uint32_t>();
+        k_adjoint<<<grid, kAdjThreads, shmem, s>>>(ws.jobs.as<AdjJob>(), nj, total, gv,
                                                    g.things_dev.as<ThingDev>(), ws.gpix.as<float>(),
                                                    ws.G.as<double>(), g.nthings, sh_things, ws.err.as<uint32_t>());
         RT_CHECK_LAUNCH();
@@ -450,6 +452,7 @@ void adjoint_jobs(const Geometry& g, const std::vector<AdjointJob>& jobs, cudaSt
     uint32_t herr = 0;
     RT_CUDA(cudaMemcpyAsync(&herr, ws.err.p, 4, cudaMemcpyDeviceToHost, s));
     RT_CUDA(cudaStreamSynchronize(s));
+    if (herr & kErrBounds) throw Error(RT_ERR_INTERNAL, "bounds check failed (RT_CHECKS build)");
     if (herr) throw Error(RT_ERR_LIMIT, "traversal stack overflow (LBVH deeper than the stack)");
 }
 

@@ -54,7 +54,11 @@ rt_status rt_debug_fail_alloc(unsigned int n) {
     return RT_OK;
 }
 
+#ifdef RT_CHECKS
+const char* rt_version(void) { return "rtxplay_gb300 0.1 sm_103a bounds-checked"; }
+#else
 const char* rt_version(void) { return "rtxplay_gb300 0.1 sm_103a"; }
+#endif
 
 // Camera::set (optx/camera.h:30-48) in binary32 on the host; the compiler
 // contracts nothing here (-ffp-contract=off), matching the CPU oracle.

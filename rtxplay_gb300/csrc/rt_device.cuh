@@ -189,7 +189,26 @@ struct GeoView {
     const InstDev* inst;      // per thing
     const FlatDesc* desc;     // per thing
     int instanced;            // the top level has instance records
+    // array lengths and the launch's error word, read by the bounds-checked
+    // build only (RT_CHECKS)
+    uint32_t ntnodes, ntprims, nbnodes, nbprims, nthings;
+    uint32_t* err;
 };
+
+// Bounds-checked debug build (-DRT_CHECKS; compute-sanitizer is not
+// available): every node, record, instance and thing index that traversal
+// and shading take from memory is checked against its array.  A bad index
+// sets kErrBounds in the launch's error word and ends the ray instead of
+// reading out of bounds (no trap); the call then fails with RT_ERR_INTERNAL.
+constexpr uint32_t kErrBounds = 4u;
+#ifdef RT_CHECKS
+__device__ __forceinline__ bool rt_in_bounds(bool ok, uint32_t* err) {
+    if (!ok && err) atomicOr(err, kErrBounds);
+    return ok;
+}
+#else
+__device__ __forceinline__ bool rt_in_bounds(bool, uint32_t*) { return true; }
+#endif
 
 // Object-to-world transform of one vertex, in the reference's operation
 // order (optx/optics_i.cu:46-62), row-major 3x4.
@@ -337,6 +356,7 @@ __device__ __forceinline__ void trav_keep(Trav& s, float t, float u, float v, ui
 template <bool kCount>
 __device__ __forceinline__ void trav_leaf_top(Trav& s, const GeoView& g, int li, uint32_t& ntest) {
     if (kCount) ++ntest;
+    if (!rt_in_bounds(uint32_t(li) < g.ntprims, g.err)) return;
     const float4 a = __ldg(g.tprims + 3 * li);
     const float4 b = __ldg(g.tprims + 3 * li + 1);
     const float4 c = __ldg(g.tprims + 3 * li + 2);
@@ -357,6 +377,7 @@ __device__ __forceinline__ void trav_leaf_top(Trav& s, const GeoView& g, int li,
 template <bool kCount>
 __device__ __forceinline__ void trav_leaf_bottom(Trav& s, const GeoView& g, int li, uint32_t& ntest) {
     if (kCount) ++ntest;
+    if (!rt_in_bounds(uint32_t(li) < g.nbprims, g.err)) return;
     const float4 a = __ldg(g.bprims + 3 * li);
     const float4 b = __ldg(g.bprims + 3 * li + 1);
     const float4 c = __ldg(g.bprims + 3 * li + 2);
@@ -371,6 +392,10 @@ __device__ __forceinline__ void trav_leaf_bottom(Trav& s, const GeoView& g, int 
 // leaves the instance when popped, traversal continues at the bottom root.
 __device__ __forceinline__ void trav_enter(Trav& s, int* stack, const GeoView& g, int li) {
     const uint32_t thing = __float_as_uint(__ldg(g.tprims + 3 * li).w);
+    if (!rt_in_bounds(uint32_t(li) < g.ntprims && thing < g.nthings, g.err)) {
+        s.h.overflow = true;   // ends the traversal
+        return;
+    }
     const InstDev in = g.inst[thing];
     if (s.sp < kStackSize) stack[s.sp++] = kInstMarker;
     else { s.h.overflow = true; return; }
@@ -446,6 +471,7 @@ __device__ __forceinline__ bool trav_step(Trav& s, int* stack, const GeoView& g,
     const bool bottom = kInst && s.in_inst;
     const float4* nodes = bottom ? g.bnodes : g.tnodes;
     const int node = s.node;
+    if (!rt_in_bounds(uint32_t(node) < (bottom ? g.nbnodes : g.ntnodes), g.err)) return false;
     float4 n0, n1, n2, n3;
     ld_node(nodes + 4 * node, n0, n1, n2, n3);
     if (bottom) {

@@ -338,7 +338,8 @@ template <int kB>
 __global__ void __launch_bounds__(kB, 1024 / kB)
     k_shade(Queues qs, const float4* __restrict__ hits, const uint32_t* __restrict__ hthing, WaveState* st,
             const JobDev* __restrict__ jobs, uint32_t nj, const float4* __restrict__ tprims,
-            const FlatDesc* __restrict__ desc, const ThingDev* __restrict__ things, Acc acc, int any_guides) {
+            const FlatDesc* __restrict__ desc, const ThingDev* __restrict__ things, Acc acc, int any_guides,
+            uint2 lim) {
     // per-warp counts, turned into block-exclusive offsets by thread 0, and the
     // block's bases from one global atomic per block (not one per warp)
     __shared__ uint32_t s_warp[kB / 32], s_warp2[kB / 32];
@@ -381,14 +382,19 @@ __global__ void __launch_bounds__(kB, 1024 / kB)
         } else {
             Stream s(j.seed, j.key1, pixel, sample, bounce + 1);
             float4 pa, pb, pc;
-            if (ref >= 0) {   // the world-space record itself
-                pa = __ldg(tprims + 3 * ref);
-                pb = __ldg(tprims + 3 * ref + 1);
-                pc = __ldg(tprims + 3 * ref + 2);
-            } else {          // an instanced triangle, rebuilt exactly as the flat layout stores it
-                world_prim(desc, hthing[i], uint32_t(-2 - ref), pa, pb, pc);
+            bool ok = ref >= 0 ? rt_in_bounds(uint32_t(ref) < lim.x, &st->err)
+                               : rt_in_bounds(hthing[i] < lim.y, &st->err);
+            if (ok) {
+                if (ref >= 0) {   // the world-space record itself
+                    pa = __ldg(tprims + 3 * ref);
+                    pb = __ldg(tprims + 3 * ref + 1);
+                    pc = __ldg(tprims + 3 * ref + 2);
+                } else {          // an instanced triangle, rebuilt exactly as the flat layout stores it
+                    world_prim(desc, hthing[i], uint32_t(-2 - ref), pa, pb, pc);
+                }
+                ok = rt_in_bounds(__float_as_uint(pa.w) < lim.y, &st->err);
             }
-            const ScatterOut so = scatter(pa, pb, pc, things, o, d, h4, s);
+            const ScatterOut so = ok ? scatter(pa, pb, pc, things, o, d, h4, s) : ScatterOut{};
             if (so.guide) {
                 if (isnull(gN)) gN = so.N;
                 if (isnull(gA)) gA = so.albedo;
@@ -702,7 +708,7 @@ LaunchShape launch_shape() {
 }
 
 using ShadeFn = void (*)(Queues, const float4*, const uint32_t*, WaveState*, const JobDev*, uint32_t, const float4*,
-                         const FlatDesc*, const ThingDev*, Acc, int);
+                         const FlatDesc*, const ThingDev*, Acc, int, uint2);
 
 ShadeFn shade_fn(int block) {
     return block == 128 ? k_shade<128> : block == 512 ? k_shade<512> : block == 1024 ? k_shade<1024> : k_shade<256>;
@@ -768,6 +774,7 @@ struct WaveLaunch {
     unsigned sgrid;    // shading grid, sblock threads per block
     int sblock;
     ExtTune tn;
+    uint2 lim;         // record and thing counts (bounds-checked build)
     Queues qs;
     float4* hits;      // t, u, v, hit reference
     uint32_t* hthing;  // thing of an instanced hit
@@ -821,7 +828,7 @@ void build_wave_graph(Workspace& ws, const WaveLaunch& L) {
     const float4* tprims_c = l.geo.tprims;
     const FlatDesc* desc_c = l.geo.desc;
     void* shade_args[] = {&l.qs,      &hits_c, &hthing_c, &l.st,  &l.jobs,       &l.nj,
-                          &tprims_c, &desc_c, &l.things, &l.acc, &l.any_guides};
+                          &tprims_c, &desc_c, &l.things, &l.acc, &l.any_guides, &l.lim};
     kp.func = reinterpret_cast<void*>(l.shade);
     kp.gridDim = dim3(l.sgrid);
     kp.blockDim = dim3(unsigned(l.sblock));
@@ -946,6 +953,8 @@ void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s
     L.jobs = ws.jobs.as<JobDev>();
     L.nj = nj;
     L.geo = g.view();
+    L.geo.err = &L.st->err;   // the bounds-checked build reports there
+    L.lim = make_uint2(L.geo.ntprims, L.geo.nthings);
     L.things = g.things_dev.as<ThingDev>();
     {
         unsigned long long* c = accum ? accum->sums.as<unsigned long long>() : ws.acc.as<unsigned long long>();
@@ -992,7 +1001,7 @@ void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s
         const FlatDesc* desc_c = L.geo.desc;
         uint32_t nj_c = nj;
         void* shade_args[] = {&L.qs,      &hits_c, &hthing_c, &L.st,  &L.jobs,       &nj_c,
-                              &tprims_c, &desc_c, &L.things, &L.acc, &L.any_guides};
+                              &tprims_c, &desc_c, &L.things, &L.acc, &L.any_guides, &L.lim};
         cudaGraphConditionalHandle no_handle = 0;
         while (true) {
             for (uint32_t b = 0; b < kBatch; ++b) {
@@ -1034,6 +1043,7 @@ void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s
     RT_CUDA(cudaMemcpyAsync(ws.host_state, L.st, sizeof(WaveState), cudaMemcpyDeviceToHost, s));
     RT_CUDA(cudaStreamSynchronize(s));
     const WaveState hs = *ws.host_state;
+    if (hs.err & kErrBounds) throw Error(RT_ERR_INTERNAL, "bounds check failed (RT_CHECKS build)");
     if (hs.err & 1u) throw Error(RT_ERR_LIMIT, "traversal stack overflow (LBVH deeper than the stack)");
     if (hs.err & 2u) throw Error(RT_ERR_LIMIT, "wave loop exceeded its bound");
     // with an accumulator the pixel sums (and so hs.rays) cover every sample so far
@@ -1087,11 +1097,14 @@ void first_hit_rect(Scene& sc, const rt_camera& cam, const rt_launch_params& p, 
     a.rtow_px = (p.flags & RT_FLAG_RTOW_PIXELS) ? 1 : 0;
     uint32_t* err = sc.geo.misc.as<uint32_t>();
     RT_CUDA(cudaMemsetAsync(err, 0, 4, s));
-    k_first_hit<<<grid_for(uint64_t(nx) * ny), kThreads, 0, s>>>(a, sc.geo.view(), prim, thing, t, u, v, t64, err);
+    GeoView gv = sc.geo.view();
+    gv.err = err;
+    k_first_hit<<<grid_for(uint64_t(nx) * ny), kThreads, 0, s>>>(a, gv, prim, thing, t, u, v, t64, err);
     RT_CHECK_LAUNCH();
     uint32_t herr = 0;
     RT_CUDA(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, s));
     RT_CUDA(cudaStreamSynchronize(s));
+    if (herr & kErrBounds) throw Error(RT_ERR_INTERNAL, "bounds check failed (RT_CHECKS build)");
     if (herr) throw Error(RT_ERR_LIMIT, "traversal stack overflow (LBVH deeper than the stack)");
 }
 

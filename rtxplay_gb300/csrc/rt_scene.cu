@@ -981,6 +981,12 @@ GeoView Geometry::view() const {
     v.inst = inst.as<InstDev>();
     v.desc = desc.as<FlatDesc>();
     v.instanced = ninstances > 0 ? 1 : 0;
+    v.ntnodes = uint32_t(top.nodes.bytes / 64);
+    v.ntprims = uint32_t(top.prims.bytes / 48);
+    v.nbnodes = uint32_t(blas.nodes.bytes / 64);
+    v.nbprims = uint32_t(blas.prims.bytes / 48);
+    v.nthings = nthings;
+    v.err = nullptr;   // set by each launch
     return v;
 }
 
