@@ -314,6 +314,10 @@ struct HitRec {
 // a ring, deeper ones spilled to local memory) measured 7 % slower on C1 at
 // 64 spp (2139 / 2163 / 2164 against 2317 Mrays/s): the ring bookkeeping
 // costs more issue slots and spills than the pops' local-memory latency.
+// Keeping each pushed node's entry distance beside it (8-B entries) and
+// skipping a popped node entered beyond the closest hit so far cut node
+// visits by 7.5 % (37.1 -> 34.3 per ray, hits unchanged) but measured 10 %
+// slower (2545 against 2841 Mrays/s): twice the stack traffic, more spills.
 constexpr int kStackSize = 64;   // > the depth of the hierarchies in practice (50 at 8M flat triangles)
 constexpr int kInstMarker = int(0x80000000u);   // stack entry: leave the current instance
 
