@@ -16,23 +16,25 @@ pytestmark = pytest.mark.gpu
 
 
 def _cycle(R, torch):
-    w, h = 96, 64
+    # images large enough that every per-cycle buffer (launcher images, the
+    # accumulator's 5.5 MB of sums, the scenes' hierarchies) spans several MiB
+    w, h = 512, 384
     cam = R.rtow_camera(w, h)
-    sc = R.rtow_scene(2)
-    R.render(sc, cam, R.launch_params(w, h, 2, depth=8, seed=1))
-    inst = R.rtow_scene(2, layout=R.RT_LAYOUT_INSTANCED)
-    R.render(inst, cam, R.launch_params(w, h, 2, depth=8, seed=1))
+    sc = R.rtow_scene(3)
+    R.render(sc, cam, R.launch_params(w, h, 1, depth=4, seed=1))
+    inst = R.rtow_scene(3, layout=R.RT_LAYOUT_INSTANCED)
+    R.render(inst, cam, R.launch_params(w, h, 1, depth=4, seed=1))
     raw = torch.zeros(w * h * 3, dtype=torch.float32, device="cuda")
     rpp = torch.zeros(w * h, dtype=torch.int32, device="cuda")
     fr = R.Frame(ctypes.c_void_p(raw.data_ptr()), ctypes.c_void_p(rpp.data_ptr()), None, None)
     acc = R.Accum(w, h)
-    acc.launch(sc, cam, R.launch_params(w, h, 2, depth=8, seed=1), fr)
+    acc.launch(sc, cam, R.launch_params(w, h, 1, depth=4, seed=1), fr)
     acc.close()
     raw2 = torch.zeros(w * h * 3, dtype=torch.float32, device="cuda")
     fr2 = R.Frame(ctypes.c_void_p(raw2.data_ptr()), None, None, None)
     b = R.Batch()
-    b.add(sc, cam, R.launch_params(w, h, 1, depth=8, seed=2), fr)
-    b.add(inst, cam, R.launch_params(w, h, 1, depth=8, seed=3), fr2)
+    b.add(sc, cam, R.launch_params(w, h, 1, depth=4, seed=2), fr)
+    b.add(inst, cam, R.launch_params(w, h, 1, depth=4, seed=3), fr2)
     b.build(60)
     b.launch()
     b.close()
