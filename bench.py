@@ -53,7 +53,7 @@ def parse():
     p.add_argument("--level", type=int, default=6)
     p.add_argument("--morton-bits", type=int, default=60)
     p.add_argument("--layout", default="auto", choices=sorted(LAYOUTS),
-                   help="acceleration-structure layout (auto: instanced meshes, as the reference's GAS/IAS)")
+                   help="acceleration-structure layout (auto: the binned-SAH layout, RT_LAYOUT_SAH)")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample time")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     p.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")

@@ -135,12 +135,18 @@ rt_status rt_scene_add_mesh(rt_scene scene, const rt_float3* vces, unsigned int 
  * A shape's mesh holds the vertices its faces reference in order of first
  * reference.  mesh_ids (cap entries, may be NULL) receives the new mesh ids,
  * n_meshes their count.  RT_ERR_INVALID_ARG for unreadable files, malformed
- * records and out-of-range indices (with file:line in the message). */
+ * records and out-of-range indices (with file:line in the message); nothing
+ * is added then.  If adding a later shape's mesh fails (out of memory), the
+ * meshes added before it stay in the scene: mesh_ids and n_meshes report
+ * them, and the call returns the failure. */
 rt_status rt_scene_add_obj(rt_scene scene, const char* path, unsigned int* mesh_ids, unsigned int cap,
                            unsigned int* n_meshes);
 /* The same parser alone (host memory, no device use): the number of shapes,
  * and for shape `shape` its vertex and triangle counts and arrays (any
- * pointer may be NULL; with all four NULL only nshapes is filled). */
+ * pointer may be NULL; with all four NULL only nshapes is filled).  To fill
+ * vces (ices), pass its capacity in entries in *nv (*ni); the call fails with
+ * RT_ERR_INVALID_ARG, writing nothing, when the shape does not fit (the file
+ * is read again on every call).  On return *nv and *ni hold the counts. */
 rt_status rt_obj_parse(const char* path, unsigned int shape, rt_float3* vces, unsigned int* nv,
                        rt_uint3* ices, unsigned int* ni, unsigned int* nshapes);
 

@@ -5,8 +5,10 @@
 #   oracle/_ref/rtow               unmodified rtow.cxx (FP64 CPU renderer)
 #   oracle/_ref/ref_golden_scene   rtow.cxx scene() + a dump driver
 #   oracle/_ref/ref_golden_sphere  optx/sphere.cxx + a dump driver
-# Needs the reference checkout (REF, default /root/reference); exits 0 without
-# doing anything when it is absent, because nothing at run time depends on it.
+# Needs the reference checkout: RTX_REFERENCE, else the checkout location of
+# the build container (this recipe is the one place that names it); exits 0
+# without doing anything when it is absent (as on the GPU machines), because
+# nothing at run time depends on it.
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
 REF="${RTX_REFERENCE:-/root/reference}"

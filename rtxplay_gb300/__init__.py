@@ -234,7 +234,7 @@ def obj_parse(path):
         check(lib().rt_obj_parse(path.encode(), k, None, ctypes.byref(nv), None, ctypes.byref(ni), None))
         v = np.zeros((nv.value, 3), np.float32)
         i = np.zeros((ni.value, 3), np.uint32)
-        check(lib().rt_obj_parse(path.encode(), k, _ptr(v), None, _ptr(i), None, None))
+        check(lib().rt_obj_parse(path.encode(), k, _ptr(v), ctypes.byref(nv), _ptr(i), ctypes.byref(ni), None))
         out.append((v, i))
     return out
 

@@ -31,13 +31,20 @@ void throw_cuda(cudaError_t e, const char* what, const char* file, int line) {
     throw Error(e == cudaErrorMemoryAllocation ? RT_ERR_OUT_OF_MEMORY : RT_ERR_CUDA, buf);
 }
 
+// SM count of the current device, cached per device ordinal (atomics: host
+// threads may ask concurrently; a race only repeats the query).
 int sm_count() {
-    static int n = 0;
-    if (n == 0) {
-        int dev = 0;
-        RT_CUDA(cudaGetDevice(&dev));
-        RT_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+    constexpr int kMaxDevices = 64;
+    static std::atomic<int> cache[kMaxDevices];
+    int dev = 0;
+    RT_CUDA(cudaGetDevice(&dev));
+    if (dev >= 0 && dev < kMaxDevices) {
+        const int c = cache[dev].load(std::memory_order_relaxed);
+        if (c > 0) return c;
     }
+    int n = 0;
+    RT_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+    if (dev >= 0 && dev < kMaxDevices) cache[dev].store(n, std::memory_order_relaxed);
     return n;
 }
 

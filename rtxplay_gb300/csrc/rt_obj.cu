@@ -131,10 +131,16 @@ rt_status rt_obj_parse(const char* path, unsigned int shape, rt_float3* vces, un
         if (!nv && !ni && !vces && !ices) return;
         RT_REQUIRE(shape < shapes.size(), "shape index out of range");
         const ObjShape& s = shapes[shape];
-        if (nv) *nv = unsigned(s.v.size());
-        if (ni) *ni = unsigned(s.i.size());
+        // an array to fill comes with its capacity in *nv / *ni; the file is
+        // read again on every call, so check what it holds now against it
+        RT_REQUIRE(!vces || nv, "vces needs nv (its capacity on input)");
+        RT_REQUIRE(!ices || ni, "ices needs ni (its capacity on input)");
+        RT_REQUIRE(!vces || s.v.size() <= *nv, "shape has more vertices than vces holds (*nv)");
+        RT_REQUIRE(!ices || s.i.size() <= *ni, "shape has more triangles than ices holds (*ni)");
         if (vces) std::memcpy(vces, s.v.data(), s.v.size() * sizeof(rt_float3));
         if (ices) std::memcpy(ices, s.i.data(), s.i.size() * sizeof(rt_uint3));
+        if (nv) *nv = unsigned(s.v.size());
+        if (ni) *ni = unsigned(s.i.size());
     });
 }
 
@@ -144,14 +150,16 @@ rt_status rt_scene_add_obj(rt_scene scene, const char* path, unsigned int* mesh_
         const std::vector<ObjShape> shapes = parse_obj(path);
         RT_REQUIRE(!shapes.empty(), std::string(path) + ": no triangle faces");
         RT_REQUIRE(mesh_ids == nullptr || cap >= shapes.size(), "mesh_ids holds fewer entries than the file's shapes");
+        if (n_meshes) *n_meshes = 0;
         for (size_t k = 0; k < shapes.size(); ++k) {
             unsigned int id = 0;
             const rt_status st = rt_scene_add_mesh(scene, shapes[k].v.data(), unsigned(shapes[k].v.size()),
                                                    shapes[k].i.data(), unsigned(shapes[k].i.size()), &id);
+            // on a failure the meshes added so far stay in the scene and are reported
             if (st != RT_OK) throw Error(st, rt_last_error_string());
             if (mesh_ids) mesh_ids[k] = id;
+            if (n_meshes) *n_meshes = unsigned(k + 1);
         }
-        if (n_meshes) *n_meshes = unsigned(shapes.size());
     });
 }
 

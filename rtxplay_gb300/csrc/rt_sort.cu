@@ -22,6 +22,18 @@ constexpr int kScanThreads = 256;
 constexpr int kScanItems = 4;
 constexpr int kScanTile = kScanThreads * kScanItems;   // 1024 elements per block
 
+// Words of scratch that scan_rec needs for n elements: the partial sums of
+// every level of its recursion, plus one.  Both the allocating sort and the
+// fixed-scratch sort size their scan tree with this one function.
+constexpr size_t scan_tmp_words(uint32_t n) {
+    size_t words = 0;
+    while (n > uint32_t(kScanTile)) {
+        n = (n + kScanTile - 1) / kScanTile;
+        words += n;
+    }
+    return words + 1;
+}
+
 // Block-wide exclusive scan of one value per thread; returns the block total.
 __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t x, uint32_t& total) {
     __shared__ uint32_t warp_sums[kScanThreads / 32];
@@ -94,14 +106,6 @@ void scan_rec(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* tmp, cuda
     RT_CHECK_LAUNCH();
 }
 
-size_t scan_tmp_words(uint32_t n) {
-    size_t words = 0;
-    while (n > uint32_t(kScanTile)) {
-        n = (n + kScanTile - 1) / kScanTile;
-        words += n;
-    }
-    return words + 1;
-}
 
 // ------------------------------------------------------------- radix sort
 constexpr int kSortThreads = 256;
@@ -256,14 +260,6 @@ struct NoAllocLayout {
 // Offsets of the sort's scratch inside the fixed array, for n pairs of
 // key_bytes-wide keys (alternate keys and values, digit histograms, scan tree).
 constexpr size_t noalloc_align(size_t b) { return (b + 255) & ~size_t(255); }
-constexpr size_t noalloc_scan_words(uint32_t n) {
-    size_t words = 0;
-    while (n > uint32_t(kScanTile)) {
-        n = (n + kScanTile - 1) / kScanTile;
-        words += n;
-    }
-    return words + 1;
-}
 constexpr NoAllocLayout noalloc_layout(uint32_t n, size_t key_bytes) {
     const uint32_t nblocks = (n + kSortTile - 1) / kSortTile;
     const uint32_t nhist = kRadix * nblocks;
@@ -271,7 +267,7 @@ constexpr NoAllocLayout noalloc_layout(uint32_t n, size_t key_bytes) {
     const size_t vals = keys + noalloc_align(size_t(n) * key_bytes);
     const size_t hist = vals + noalloc_align(size_t(n) * sizeof(uint32_t));
     const size_t scan = hist + noalloc_align(size_t(nhist) * sizeof(uint32_t));
-    const size_t total = scan + noalloc_align(noalloc_scan_words(nhist) * sizeof(uint32_t));
+    const size_t total = scan + noalloc_align(scan_tmp_words(nhist) * sizeof(uint32_t));
     return NoAllocLayout{keys, vals, hist, scan, total};
 }
 
@@ -286,13 +282,22 @@ constexpr int kNoAllocMaxDevices = 64;
 std::mutex g_noalloc_mu;
 void* g_noalloc_ptr[kNoAllocMaxDevices] = {};
 
-// Device address of the scratch on the current device (set up on first use).
-unsigned char* noalloc_scratch() {
+// Device address of the scratch on the current device.  The first call on a
+// device sets it up.  Later calls made outside a stream capture look it up
+// again (a cheap query), so a cudaDeviceReset between calls, which reloads
+// the module at a possibly different address, leaves no stale pointer behind;
+// calls made during a capture use the address cached by the last lookup.
+unsigned char* noalloc_scratch(cudaStream_t s) {
     int dev = 0;
     RT_CUDA(cudaGetDevice(&dev));
     RT_REQUIRE(dev >= 0 && dev < kNoAllocMaxDevices, "device ordinal out of range for the fixed scratch");
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) {   // e.g. the legacy stream while another captures
+        (void)cudaGetLastError();
+        cap = cudaStreamCaptureStatusActive;
+    }
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
+    if (!g_noalloc_ptr[dev] || cap == cudaStreamCaptureStatusNone) {
         void* p = nullptr;
         RT_CUDA(cudaGetSymbolAddress(&p, g_noalloc_sort_scratch));
         g_noalloc_ptr[dev] = p;
@@ -353,8 +358,8 @@ extern "C" rt_status rt_radix_sort_pairs_noalloc(void* keys, unsigned int* vals,
             throw Error(RT_ERR_INVALID_ARG, "rt_radix_sort_pairs_noalloc: n = " + std::to_string(n) +
                                                 " exceeds the fixed scratch limit of " +
                                                 std::to_string(kNoAllocMaxPairs) + " pairs");
-        unsigned char* scratch = noalloc_scratch();
         cudaStream_t s = as_stream(stream);
+        unsigned char* scratch = noalloc_scratch(s);
         if (key_bits <= 32)
             radix_sort_pairs_fixed<uint32_t>(static_cast<uint32_t*>(keys), vals, n, int(key_bits), scratch, s);
         else

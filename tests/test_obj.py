@@ -64,6 +64,27 @@ def test_errors_carry_file_and_line(product, tmp_path, text, msg):
     assert msg in str(e.value) and "bad.obj:" in str(e.value)
 
 
+def test_parse_checks_capacity(product, tmp_path):
+    """A file that grew between the size query and the fill call does not
+    overrun the caller's arrays: the fill call is refused and writes nothing."""
+    R = product
+    p = _write(tmp_path, "c.obj", "v 0 0 0\nv 1 0 0\nv 1 1 0\nv 0 1 0\nf 1 2 3 4\n")
+    v = np.full((3, 3), -7.0, np.float32)   # room for 3 of 4 vertices
+    i = np.zeros((2, 3), np.uint32)
+    nv, ni = ctypes.c_uint(3), ctypes.c_uint(2)
+    st = R.lib().rt_obj_parse(p.encode(), 0, ctypes.c_void_p(v.ctypes.data), ctypes.byref(nv),
+                              ctypes.c_void_p(i.ctypes.data), ctypes.byref(ni), None)
+    assert st == R.RT_ERR_INVALID_ARG and b"vces" in R.lib().rt_last_error_string()
+    assert (v == -7.0).all()
+    nv.value = 4
+    st = R.lib().rt_obj_parse(p.encode(), 0, ctypes.c_void_p(v.ctypes.data), None, None, None, None)
+    assert st == R.RT_ERR_INVALID_ARG   # an array without its capacity
+    v4 = np.zeros((4, 3), np.float32)
+    assert R.lib().rt_obj_parse(p.encode(), 0, ctypes.c_void_p(v4.ctypes.data), ctypes.byref(nv),
+                                ctypes.c_void_p(i.ctypes.data), ctypes.byref(ni), None) == R.RT_OK
+    assert nv.value == 4 and ni.value == 2 and v4[2].tolist() == [1, 1, 0]
+
+
 def test_missing_file(product, tmp_path):
     R = product
     with pytest.raises(R.RTError) as e:
