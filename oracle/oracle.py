@@ -106,6 +106,10 @@ def lib():
         L.orc_fuzz_path_check.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Camera), ctypes.c_uint, ctypes.c_uint,
                                           ctypes.c_uint, ctypes.c_uint, ctypes.c_uint32, ctypes.c_int,
                                           ctypes.c_float, _f32p, _f32p, _f64p]
+        L.orc_fuzz_held_delta.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Camera), ctypes.c_uint, ctypes.c_uint,
+                                          ctypes.c_uint, ctypes.c_uint, ctypes.c_uint32, ctypes.c_uint32,
+                                          ctypes.c_int, ctypes.c_double, _f32p, _f32p, ctypes.c_void_p,
+                                          ctypes.c_void_p, _f64p, _f64p, _f64p, ctypes.c_int]
         for name in ("orc_pp_srgb", "orc_pp_none", "orc_pp_gamma2"):
             getattr(L, name).argtypes = [_f32p, _u8p, ctypes.c_int, ctypes.c_int]
         _lib = L
@@ -300,6 +304,24 @@ class World:
                                   np.asarray(ambient, np.float32), np.asarray(white, np.float32), out)
         return dict(compared=int(out[0]), skipped=int(out[1]), max_rel=out[2], sum_abs_fd=out[3],
                     outliers=int(out[4]), sum_adj=out[5], sum_fd=out[6])
+
+    def fuzz_held_delta(self, cam, w, h, spp, depth, seed, thing, step=1e-6, ambient=(0.5, 0.7, 1.0),
+                        white=(1.0, 1.0, 1.0), image=None, grad_image=None, scene=0, nthreads=0):
+        """Per-pixel change of the image (w*h, 3; doubles) when metal `thing`'s
+        fuzz moves by +step and -step with every path's visibility held fixed
+        (double-precision replay), counts (replayed, degenerate, paths a plain
+        re-render sees jump) and, given image and grad_image, the adjoint's
+        fuzz gradient over the replayed paths on their replayed trajectories."""
+        dp = np.zeros((w * h, 3), np.float64)
+        dm = np.zeros((w * h, 3), np.float64)
+        out = np.zeros(4, np.float64)
+        im = None if image is None else np.ascontiguousarray(image, np.float32).reshape(-1)
+        gi = None if grad_image is None else np.ascontiguousarray(grad_image, np.float32).reshape(-1)
+        lib().orc_fuzz_held_delta(self._w, ctypes.byref(cam), w, h, spp, depth, seed, scene, thing, step,
+                                  np.asarray(ambient, np.float32), np.asarray(white, np.float32),
+                                  _ptr(im), _ptr(gi), dp, dm, out, nthreads)
+        return dict(plus=dp, minus=dm, replayed=int(out[0]), degenerate=int(out[1]), changed=int(out[2]),
+                    adjoint=float(out[3]))
 
     def set_optics(self, thing, otype, albedo, fuzz, index):
         assert lib().orc_world_set_optics(self._w, thing, otype, np.asarray(albedo, np.float32), fuzz,

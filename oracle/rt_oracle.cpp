@@ -915,7 +915,7 @@ inline F3 sky(F3 d, F3 ambient, F3 white) {
 
 PathOut trace_path(const orc_world& w, const Cam& cam, unsigned x, unsigned y, unsigned W,
                    unsigned H, unsigned depth, uint32_t seed, uint32_t scene, uint32_t sample,
-                   F3 ambient, F3 white, PathRec* rec = nullptr) {
+                   F3 ambient, F3 white, PathRec* rec = nullptr, int fthing = -1, float fuzz = 0.f) {
     const uint32_t pix = W * y + x;
     PathOut out{mk(1.f, 1.f, 1.f), mk(0, 0, 0), mk(0, 0, 0), 0};
     F3 o, d;
@@ -955,7 +955,7 @@ PathOut trace_path(const orc_world& w, const Cam& cam, unsigned x, unsigned y, u
             const F3 d1V = unitV(d);
             const F3 refl = sub(d1V, mul(2.f * dot(d1V, g.N), g.N));
             const F3 v = rndVin1sphere(s);
-            const F3 dir = add(refl, mul(th.fuzz, v));
+            const F3 dir = add(refl, mul(w.prims[h.prim].thing == fthing ? fuzz : th.fuzz, v));
             vx.v = v;
             if (isnull(out.normal)) out.normal = g.N;
             if (isnull(out.albedo)) out.albedo = th.albedo;
@@ -996,6 +996,14 @@ PathOut trace_path(const orc_world& w, const Cam& cam, unsigned x, unsigned y, u
         if (rec) rec->vtx.push_back(vx);
     }
     return out;
+}
+
+// trace_path with the fuzz of thing `fthing` replaced by `fuzz` (the world is
+// not modified, so threads can trace different values at once).
+inline PathOut trace_path_fuzz(const orc_world& w, const Cam& cam, unsigned x, unsigned y, unsigned W,
+                               unsigned H, unsigned depth, uint32_t seed, uint32_t scene, uint32_t sample,
+                               F3 ambient, F3 white, int fthing, float fuzz, PathRec* rec) {
+    return trace_path(w, cam, x, y, W, H, depth, seed, scene, sample, ambient, white, rec, fthing, fuzz);
 }
 
 // ------------------------------------------------------------- adjoint --
@@ -1583,6 +1591,196 @@ void orc_fuzz_path_check(orc_world* wd, const orc_camera* cam, unsigned w, unsig
     }
     out[0] = compared; out[1] = skipped; out[2] = maxrel; out[3] = sumfd;
     out[4] = outliers; out[5] = sadj; out[6] = sfd;
+}
+
+// Colour of recorded path `rec` replayed in double precision with its
+// visibility held fixed and metal `fthing`'s fuzz replaced by `fuzz`: the
+// same random numbers, the same primitive at every vertex (the ray meets the
+// recorded triangle's plane -- Moller-Trumbore without the barycentric
+// bounds -- or the recorded sphere's root chosen by the same rule), the
+// recorded facing, branches and near-zero fallbacks.  This is the function
+// whose derivative the adjoint forms (the tangent differentiates it
+// analytically), so a central difference of it at image level checks the
+// fuzz gradient without the hit-sequence changes that a plain re-render
+// mixes in; double precision lets the step be small enough to follow the
+// steep near-silhouette paths.  Returns false when a replayed vertex is
+// degenerate (a ray parallel to a recorded plane, or missing a recorded
+// sphere).
+static bool replay_held(const orc_world& w, const Cam& cam, const PathRec& rec, unsigned x, unsigned y, unsigned W,
+                        unsigned H, uint32_t seed, uint32_t scene, uint32_t sample, F3 ambient, F3 white, int fthing,
+                        double fuzz, D3& color, PathRec* out = nullptr) {
+    auto cr = [](D3 a, D3 b) { return D3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; };
+    auto unit = [](D3 a) { return (1.0 / dlen(a)) * a; };
+    auto mv = [](D3 a, D3 b) { return D3{a.x * b.x, a.y * b.y, a.z * b.z}; };
+    const uint32_t pix = W * y + x;
+    D3 o, d;
+    {
+        F3 of, df;
+        Stream s(seed, scene, pix, sample, 0);
+        camera_ray(cam, x, y, W, H, s, of, df);
+        o = dd3(of);
+        d = dd3(df);
+    }
+    auto f3 = [](D3 a) { return mk(float(a.x), float(a.y), float(a.z)); };
+    if (out) { *out = rec; }
+    D3 thr{1, 1, 1};
+    for (size_t k = 0; k < rec.vtx.size(); ++k) {
+        const Vtx& v = rec.vtx[k];
+        const Prim& p = w.prims[v.prim];
+        const D3 o_in = o, d_in = d;
+        D3 hp, N;
+        if (p.kind == 0) {
+            const D3 A = dd3(p.a), e1 = dd3(p.b) - A, e2 = dd3(p.c) - A;
+            const D3 pv = cr(d, e2);
+            const double det = ddot(e1, pv);
+            if (det == 0.0) return false;
+            const D3 tv = o - A, qv = cr(tv, e1);
+            const double u = ddot(tv, pv) / det, vv = ddot(d, qv) / det;
+            hp = A + u * e1 + vv * e2;
+            N = unit(cr(e1, e2));
+            if (ddot(d, N) > 0.0) N = -1.0 * N;
+        } else {
+            const D3 c = dd3(p.a), oc = o - c;
+            const double a = ddot(d, d), b = ddot(d, oc), cc = ddot(oc, oc) - double(p.r) * double(p.r);
+            const double disc = b * b - a * cc;
+            if (disc < 0.0) return false;
+            const double xs = std::sqrt(disc);
+            double t = (-b - xs) / a;
+            if (t < double(kTmin)) t = (-b + xs) / a;
+            if (t < double(kTmin)) return false;
+            hp = o + t * d;
+            const D3 outward = (1.0 / double(p.r)) * (hp - c);
+            N = v.front ? outward : -1.0 * outward;   // facing held as recorded
+        }
+        if (out) {   // the replayed vertex, for a tangent evaluated on this trajectory
+            Vtx& r = out->vtx[k];
+            r.o = f3(o_in); r.d = f3(d_in); r.p = f3(hp); r.N = f3(N);
+            r.t = float(ddot(hp - o_in, d_in) / ddot(d_in, d_in));
+        }
+        const Thing& th = w.things[v.thing];
+        Stream s(seed, scene, pix, sample, uint32_t(k + 1));
+        if (v.type == OPT_DIFFUSE) {
+            const D3 u = dd3(rndVon1sphere(s));
+            d = v.branch ? N : N + u;
+            thr = mv(thr, dd3(th.albedo));
+        } else if (v.type == OPT_REFLECT) {
+            const D3 d1 = unit(d);
+            const D3 refl = d1 - (2.0 * ddot(d1, N)) * N;
+            const D3 vv = dd3(rndVin1sphere(s));
+            const double fz = int(v.thing) == fthing ? fuzz : double(th.fuzz);
+            d = refl + fz * vv;
+            thr = mv(thr, dd3(th.albedo));
+        } else {
+            const D3 d1 = unit(d);
+            const double ratio = v.front ? 1.0 / double(th.index) : double(th.index);
+            if (v.branch == 0) {
+                d = d1 - (2.0 * ddot(d1, N)) * N;
+            } else {
+                const double theta = std::min(ddot(-1.0 * d1, N), 1.0);
+                const D3 perpen = ratio * (d1 + theta * N);
+                d = perpen + (-std::sqrt(std::fabs(1.0 - ddot(perpen, perpen)))) * N;
+            }
+        }
+        o = hp;
+    }
+    if (out) out->d_last = f3(d);
+    const D3 u = unit(d);
+    const double sv = 0.5 * (u.y + 1.0);
+    color = mv(thr, D3{(1.0 - sv) * white.x + sv * ambient.x, (1.0 - sv) * white.y + sv * ambient.y,
+                       (1.0 - sv) * white.z + sv * ambient.z});
+    return true;
+}
+
+// Image-level central difference of the fuzz of metal `thing` with
+// visibility held fixed: for every path that ends in the sky and reflects off
+// `thing`, its colour replayed with fuzz f0 + step and f0 - step
+// (replay_held); delta_plus / delta_minus (w*h*3 doubles) receive the per-pixel
+// change of the mean over spp.  out[0] = paths replayed, out[1] = paths with a
+// degenerate replay (left out), out[2] = paths whose plain re-render at
+// f0 +- step changes its hit sequence or branches (the paths a whole-image
+// difference of re-renders would see jump), out[3] = (with image and
+// grad_image given) the adjoint's fuzz gradient over the same paths, its
+// tangent evaluated on the replayed double-precision trajectory -- the
+// trajectory the difference follows, which on chaotic paths (chains of
+// reflections off small spheres) drifts from the binary32 one.
+void orc_fuzz_held_delta(const orc_world* wd, const orc_camera* cam, unsigned w, unsigned h, unsigned spp,
+                         unsigned depth, uint32_t seed, uint32_t scene, int thing, double step,
+                         const float ambient[3], const float white[3], const float* image, const float* grad_image,
+                         double* delta_plus, double* delta_minus, double* out, int nthreads) {
+    const Cam c = to_cam(cam);
+    const F3 amb = ld3(ambient), wht = ld3(white);
+    const double f0 = wd->things[thing].fuzz;
+    const double fp = f0 + step, fm = f0 - step;
+    std::fill(delta_plus, delta_plus + size_t(w) * h * 3, 0.0);
+    std::fill(delta_minus, delta_minus + size_t(w) * h * 3, 0.0);
+    double replayed = 0, degenerate = 0, changed = 0, adj = 0;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+#pragma omp parallel reduction(+ : replayed, degenerate, changed, adj)
+    {
+        PathRec r0, rr;
+#pragma omp for schedule(dynamic, 16)
+        for (long pix = 0; pix < long(w) * long(h); ++pix) {
+            const unsigned x = unsigned(pix % w), y = unsigned(pix / w);
+            for (unsigned smp = 0; smp < spp; ++smp) {
+                trace_path(*wd, c, x, y, w, h, depth, seed, scene, smp, amb, wht, &r0);
+                if (!r0.miss) continue;
+                bool touches = false;
+                for (const Vtx& v : r0.vtx) touches |= (v.thing == thing && v.type == OPT_REFLECT);
+                if (!touches) continue;
+                D3 c0, cp, cm;
+                if (!replay_held(*wd, c, r0, x, y, w, h, seed, scene, smp, amb, wht, thing, f0, c0, &rr) ||
+                    !replay_held(*wd, c, r0, x, y, w, h, seed, scene, smp, amb, wht, thing, fp, cp) ||
+                    !replay_held(*wd, c, r0, x, y, w, h, seed, scene, smp, amb, wht, thing, fm, cm)) {
+                    degenerate += 1;
+                    continue;
+                }
+                replayed += 1;
+                const double inv = 1.0 / double(spp);
+                if (image && grad_image) {   // the adjoint's term of this path, on the replayed trajectory
+                    double g[3];
+                    for (int ch = 0; ch < 3; ++ch) {
+                        const float I = image[3 * pix + ch];
+                        g[ch] = (I > 0.f && I < 1.f) ? double(grad_image[3 * pix + ch]) * inv : 0.0;
+                    }
+                    D3 thr{1, 1, 1};
+                    for (const Vtx& v : rr.vtx)
+                        if (v.type != OPT_REFRACT) {
+                            const F3 a = wd->things[v.thing].albedo;
+                            thr = D3{thr.x * a.x, thr.y * a.y, thr.z * a.z};
+                        }
+                    for (size_t k = 0; k < rr.vtx.size(); ++k) {
+                        const Vtx& v = rr.vtx[k];
+                        if (v.thing != thing || v.type != OPT_REFLECT) continue;
+                        const D3 ds = tangent_to_sky(*wd, rr, k + 1, D3{0, 0, 0}, dd3(v.v), amb, wht);
+                        adj += g[0] * thr.x * ds.x + g[1] * thr.y * ds.y + g[2] * thr.z * ds.z;
+                    }
+                }
+                delta_plus[3 * pix + 0] += (cp.x - c0.x) * inv;
+                delta_plus[3 * pix + 1] += (cp.y - c0.y) * inv;
+                delta_plus[3 * pix + 2] += (cp.z - c0.z) * inv;
+                delta_minus[3 * pix + 0] += (cm.x - c0.x) * inv;
+                delta_minus[3 * pix + 1] += (cm.y - c0.y) * inv;
+                delta_minus[3 * pix + 2] += (cm.z - c0.z) * inv;
+                // would a plain re-render see this path jump?
+                PathRec rp;
+                for (float f : {float(fp), float(fm)}) {
+                    trace_path_fuzz(*wd, c, x, y, w, h, depth, seed, scene, smp, amb, wht, thing, f, &rp);
+                    bool same = rp.miss == r0.miss && rp.vtx.size() == r0.vtx.size();
+                    for (size_t k = 0; same && k < rp.vtx.size(); ++k)
+                        same = rp.vtx[k].prim == r0.vtx[k].prim && rp.vtx[k].branch == r0.vtx[k].branch;
+                    if (!same) { changed += 1; break; }
+                }
+            }
+        }
+    }
+    out[0] = replayed;
+    out[1] = degenerate;
+    out[2] = changed;
+    out[3] = adj;
 }
 
 int orc_world_set_optics(orc_world* w, int thing, int type, const float albedo[3], float fuzz, float index) {

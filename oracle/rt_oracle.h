@@ -127,6 +127,20 @@ void orc_world_get_optics(const orc_world* w, int* types, float* albedos, float*
 void orc_fuzz_path_check(orc_world* wd, const orc_camera* cam, unsigned w, unsigned h, unsigned spp,
                          unsigned depth, uint32_t seed, int thing, float step, const float ambient[3],
                          const float white[3], double* out);  /* out[7] */
+/* Image-level central difference of metal `thing`'s fuzz with visibility
+ * held fixed: every sky-ending path that reflects off `thing` is replayed in
+ * double precision along its recorded primitives and branches with fuzz
+ * f0 and f0 +- step;
+ * delta_plus/minus (w*h*3) receive the change of every pixel's mean.  out[4]
+ * = paths replayed, degenerate replays left out, paths whose plain re-render
+ * changes its hit sequence, and (image and grad_image given, else 0) the
+ * adjoint's fuzz gradient over the replayed paths on their replayed
+ * trajectories. */
+void orc_fuzz_held_delta(const orc_world* wd, const orc_camera* cam, unsigned w, unsigned h, unsigned spp,
+                         unsigned depth, uint32_t seed, uint32_t scene, int thing, double step,
+                         const float ambient[3], const float white[3], const float* image,
+                         const float* grad_image, double* delta_plus, double* delta_minus, double* out,
+                         int nthreads);
 /* FP64 gradients of a scalar loss of the rendered image, given dL/dI
  * (grad_image, w*h*3, with image = the clamped render): per thing
  * grad_albedo[3*n], grad_fuzz[n]; grad_sky[6] = d/d ambient xyz, d/d white xyz.

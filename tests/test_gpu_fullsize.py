@@ -104,6 +104,28 @@ def test_c1_render_subset_bit_exact_and_properties(product, oracle, cuda, c1):
     assert np.array_equal(rpp[pix], ref["rpp"])
 
 
+def test_c1_benchmark_frame_500spp_bit_exact(product, oracle, cuda, c1):
+    """The benchmark frame itself: 1200x800, 500 spp, depth 50 (480 M paths,
+    about 1.3 G rays; the oracle needs about a minute on 16 host cores).
+    Every pixel's colour bits and rays per pixel equal the oracle's, so the
+    converged image's relative RMSE against the CPU render is 0 (the target
+    is at most 1 %)."""
+    R, O = product, oracle
+    sc, wd = c1
+    spp = 500
+    cam = R.rtow_camera(W, H)
+    out = R.render(sc, cam, R.launch_params(W, H, spp, depth=50, seed=4711))
+    ref = wd.render(oracle_camera(O, cam), W, H, spp, 50, 4711, guides=False)
+    g, c = out["rawRGB"], ref["rawRGB"]
+    same = (g.view(np.uint32) == c.view(np.uint32)).all(axis=1)
+    rel_rmse = float(np.sqrt(np.mean((g.astype(np.float64) - c) ** 2)) / np.sqrt(np.mean(c.astype(np.float64) ** 2)))
+    print(f"C1 500 spp: {int(out['stats'].rays)} rays, {int((~same).sum())} pixels differ, rel-RMSE {rel_rmse:.3e}")
+    assert int(out["rpp"].sum(dtype=np.uint64)) == int(out["stats"].rays) == ref["rays"]
+    assert same.all()
+    assert np.array_equal(out["rpp"], ref["rpp"])
+    assert rel_rmse <= 1e-2
+
+
 def test_c1_full_frame_bit_exact(product, oracle, cuda, c1):
     """Every pixel of the benchmark frame (1200x800, 4 spp, depth 50) equals
     the oracle's: colour bits and rays per pixel; sRGB bytes within one step."""
