@@ -11,8 +11,13 @@ closest-hit query, the final miss included).
   e2e       the same metric through the C ABI from host buffers: per step the
             host mesh and things are copied in, the LBVH is built, the frame is
             rendered and post-processed, image and rays-per-pixel are copied out.
-  roofline  traversal kernel (k_extend): algorithmic bytes per launch / mean
-            launch time against the measured HBM copy bandwidth.
+  roofline  traversal kernel (k_extend_p), the bound its counters show:
+            instruction issue.  achieved = thread instructions per ray (ncu
+            summary of the same kernel) x rays per launch / mean launch time
+            (CUDA events, live), against 152 SMs x 4 schedulers x 32 lanes x
+            the SM clock sampled during the run; beside it the L2 bytes/s
+            against an L2 copy bandwidth measured in the run, and the DRAM
+            bytes/s against the measured HBM copy bandwidth.
   cpu_baseline  the CPU oracle (a C++ restatement of the reference's path) on a
             bounded pixel sample of the same workload on all host cores.
 
@@ -63,7 +68,7 @@ def parse():
     p.add_argument("--tune", action="store_true",
                    help="search the launch shape (rt_tuning) of every workload and store it in the tuning cache")
     p.add_argument("--no-tuning", action="store_true", help="built-in launch shape, ignore the tuning cache")
-    p.add_argument("--inverse-iters", type=int, default=10,
+    p.add_argument("--inverse-iters", type=int, default=200,
                    help="Adam iterations of the inverse-rendering leg, batched and serial each")
     return p.parse_args()
 
@@ -99,9 +104,11 @@ LAYOUTS = {"auto": 0, "flat": 1, "instanced": 2, "grouped": 3, "sah": 4}
 
 
 def profile_bytes_per_ray(layout, key="dram_bytes_per_ray"):
-    """DRAM (or, with key "lts_bytes_per_ray", L2) bytes per ray of k_extend
-    from the committed ncu summary of the layout (one capture of full-wave
-    launches), or None."""
+    """A per-ray figure of k_extend_p from the committed ncu summary of the
+    layout (one capture of full-wave launches): DRAM bytes
+    ("dram_bytes_per_ray"), L2 bytes ("lts_bytes_per_ray"), warp
+    instructions ("warp_inst_per_ray") or thread instructions
+    ("thread_inst_per_ray"); None when absent."""
     name = {1: "k_extend_c1.txt", 2: "k_extend_c1_instanced.txt", 3: "k_extend_c1_grouped.txt",
             4: "k_extend_c1_sah.txt"}.get(layout, "")
     path = os.path.join(ROOT, "profiles", name)
@@ -110,6 +117,29 @@ def profile_bytes_per_ray(layout, key="dram_bytes_per_ray"):
     with open(path) as f:
         m = re.search(r"^" + key + r":\s*([0-9.eE+]+)", f.read(), re.M)
     return float(m.group(1)) if m else None
+
+
+def l2_copy_gbs(torch, stream, mib=16, reps=400):
+    """Copy bandwidth of a working set that stays in L2: b.copy_(a) over two
+    `mib` MiB buffers (2 x 16 MiB against the 129 MB L2), bytes read + written
+    per copy, CUDA events around `reps` back-to-back copies (best of 3)."""
+    n = mib * 2**20 // 4
+    a = torch.ones(n, dtype=torch.float32, device="cuda")
+    b = torch.empty_like(a)
+    for _ in range(20):
+        b.copy_(a)
+    best = 0.0
+    for _ in range(3):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            b.copy_(a)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        best = max(best, 2.0 * n * 4 * reps / (e0.elapsed_time(e1) * 1e-3) / 1e9)
+    return best
 
 
 class ClockSampler:
@@ -174,7 +204,10 @@ def cpu_oracle_run(args, target_s, threads=None):
     dt = time.perf_counter() - t0
     return {"value": r["rays"] / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{len(pix)} of {npix} pixels (stride {stride}) x {args.spp} spp, depth {args.depth}, "
-                      f"{r['rays']} rays in {dt:.2f} s; LBVH build excluded"}
+                      f"{r['rays']} rays in {dt:.2f} s; LBVH build excluded",
+            "note": "the unmodified rtow.cxx is not timed here: the reference checkout it is compiled from "
+                    "does not travel to the GPU machine and the build container's binary is x86 (this host "
+                    "is Arm); the port is statistically pinned to it (rel-RMSE 0.26 % at 1280x720x10)"}
 
 
 def run_reference(args, world, rank):
@@ -277,20 +310,30 @@ def batched_leg(R, torch, sptr, stream, nscenes, steps, tuning_mode):
     key_b = tune.workload_key("batch", paths, binfo["n_prims"], 16, scenes=nscenes)
     t_batch = apply_tuning(R, tune, key_b, tune.batch_timer(batch, repeats=1, stream=sptr), tuning_mode)
     batch.launch(stream=sptr)   # warm-up
-    b_ms, b_rays = [], 0
+    b_ms, b_rays, b_wall = [], 0, []
     for _ in range(steps):
+        t0 = time.perf_counter()
         ms, st = time_it(lambda: batch.launch(stream=sptr))
+        b_wall.append((time.perf_counter() - t0) * 1e3)
         b_ms.append(ms)
         b_rays = int(st.rays)
-    keep = [(raw.clone(), rpp.clone()) for raw, rpp in bufs[:8]]
+    keep = [(raw.clone(), rpp.clone()) for raw, rpp in bufs]   # every scene's image and rays per pixel
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in scenes]
 
-    def serial():
+    def serial(per_scene=None):
         rays = 0
-        for sc, cam, pa, fr in zip(scenes, cams, params, frames):
+        for k, (sc, cam, pa, fr) in enumerate(zip(scenes, cams, params, frames)):
             st = R.LaunchStats()
+            if per_scene is not None:
+                ev[k][0].record(stream)
             R.check(lib.rt_launch_ex(sc.h, ctypes.byref(cam), ctypes.byref(pa), ctypes.byref(fr), sptr,
                                      ctypes.byref(st)))
+            if per_scene is not None:
+                ev[k][1].record(stream)
             rays += int(st.rays)
+        if per_scene is not None:
+            torch.cuda.synchronize()
+            per_scene.append(sum(a.elapsed_time(b) for a, b in ev))
         return rays
 
     def serial_probe(t, first=32):   # the tuning search times the first scenes only
@@ -309,17 +352,36 @@ def batched_leg(R, torch, sptr, stream, nscenes, steps, tuning_mode):
     key_s = tune.workload_key("serial", paths, binfo["n_prims"], 16, scenes=nscenes)
     t_serial = apply_tuning(R, tune, key_s, serial_probe, tuning_mode)
     serial()   # warm-up
-    s_ms, s_rays = [], 0
+    s_ms, s_rays, s_dev, s_wall = [], 0, [], []
     for _ in range(steps):
-        ms, s_rays = time_it(serial)
+        t0 = time.perf_counter()
+        ms, s_rays = time_it(lambda: serial(s_dev))
+        s_wall.append((time.perf_counter() - t0) * 1e3)
         s_ms.append(ms)
-    equal = all(torch.equal(a, raw) and torch.equal(b, rpp) for (a, b), (raw, rpp) in zip(keep, bufs[:8]))
+    equal = all(torch.equal(a, raw) and torch.equal(b, rpp) for (a, b), (raw, rpp) in zip(keep, bufs))
     bm, sm = float(np.median(b_ms)), float(np.median(s_ms))
+    sdev = float(np.median(s_dev))
+    # kernel time alone: one more serial pass with CUDA events around every traversal and
+    # shading launch (host-driven wave loop), summed over the scenes
+    s_kernel = 0.0
+    for sc, cam, pa, fr in zip(scenes, cams, params, frames):
+        pt = R.launch_params(pa.image_w, pa.image_h, pa.spp, pa.depth, pa.seed, R.RT_FLAG_STAGE_TIMING)
+        st = R.LaunchStats()
+        R.check(lib.rt_launch_ex(sc.h, ctypes.byref(cam), ctypes.byref(pt), ctypes.byref(fr), sptr,
+                                 ctypes.byref(st)))
+        s_kernel += st.extend_ms + st.shade_ms
     return {"scenes": nscenes, "triangles": binfo["n_prims"],
             "paths": int(sum(sp["w"] * sp["h"] * sp["spp"] for sp in specs)),
             "rays": b_rays, "batched_ms": bm, "serial_ms": sm, "speedup": sm / bm,
             "batched_mrays_s": b_rays / (bm * 1e-3) / 1e6, "serial_mrays_s": s_rays / (sm * 1e-3) / 1e6,
-            "images_equal_first8": bool(equal and b_rays == s_rays),
+            # device time: the batch's one launch between two events, and the sum over the
+            # scenes of the time between events recorded right before and after each scene's
+            # launch (its device work; the host work between launches falls outside)
+            "batched_device_ms": bm, "serial_device_ms": sdev, "serial_kernel_ms": s_kernel,
+            "batched_wall_ms": float(np.median(b_wall)), "serial_wall_ms": float(np.median(s_wall)),
+            "serial_ceiling": float(np.median(s_wall)) / sdev,
+            "device_speedup": sdev / bm,
+            "images_equal_all": bool(equal and b_rays == s_rays),
             "build_batched_s": batch_build_s, "build_serial_s": serial_build_s,
             # the same comparison with the hierarchy builds included (one segmented build
             # of all scenes against one build per scene)
@@ -572,33 +634,58 @@ def main():
         cpu = cpu_oracle_run(args, args.cpu_seconds)
 
     peak, peak_src = load_peaks()
+    l2_peak = l2_copy_gbs(torch, stream)
     ext_launches = max(1, rst.extend_launches)
     per_launch_ms = rst.extend_ms / ext_launches
     rays_per_launch = rst.rays / ext_launches
-    achieved = bytes_per_ray * rays_per_launch / (per_launch_ms * 1e-3) / 1e9 if per_launch_ms > 0 else None
+    frame_ms = elapsed_ms / args.steps
+    sm_mhz = (clk or {}).get("sm_mhz") or 2070.0
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+
+    def rate(per_ray, scale=1e9):   # per-ray figure x rays per launch / mean launch time
+        if per_ray is None or per_launch_ms <= 0:
+            return None
+        return per_ray * rays_per_launch / (per_launch_ms * 1e-3) / scale
+
     dram_per_ray = profile_bytes_per_ray(info.layout)
     l2_per_ray = profile_bytes_per_ray(info.layout, "lts_bytes_per_ray")
-    traffic = dram_per_ray * rays_per_launch if dram_per_ray else None
-    frame_ms = elapsed_ms / args.steps
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": (achieved / peak) if achieved else None,
-                "traffic": traffic,
-                "l2_traffic": l2_per_ray * rays_per_launch if l2_per_ray else None,
-                "traffic_note": "ncu dram__bytes (l2_traffic: lts__t_sectors x 32 B) of full-wave launches "
-                                "(profiles/k_extend_c1_<layout>.txt), per ray, times the rays of a mean launch",
-                "kernel": "k_extend (hierarchy traversal + ray/triangle tests)",
-                "timing": "CUDA events around every k_extend launch of one frame of the same workload "
+    tinst_per_ray = profile_bytes_per_ray(info.layout, "thread_inst_per_ray")
+    winst_per_ray = profile_bytes_per_ray(info.layout, "warp_inst_per_ray")
+    issue_peak = sms * 4 * 32 * sm_mhz * 1e6 / 1e12           # thread instructions, T/s
+    achieved = rate(tinst_per_ray, 1e12)
+    dram_gbs, l2_gbs = rate(dram_per_ray), rate(l2_per_ray)
+    alg_gbs = rate(bytes_per_ray)
+    roofline = {"bound": "issue", "achieved": achieved, "peak": issue_peak, "unit": "Tinst/s",
+                "frac": (achieved / issue_peak) if achieved else None,
+                "traffic": dram_per_ray * rays_per_launch if dram_per_ray else None,
+                "kernel": "k_extend_p (persistent hierarchy traversal + ray/triangle tests)",
+                "what": "thread instructions per second: ncu's instructions per ray x lanes per instruction "
+                        "(profiles/k_extend_c1_<layout>.txt) x rays per launch / mean launch time measured "
+                        "here; peak = SMs x 4 schedulers x 32 lanes x the median SM clock sampled during "
+                        "the run (one warp instruction per scheduler per cycle)",
+                "peak_source": f"computed: {sms} SMs x 4 x 32 x {sm_mhz:.0f} MHz",
+                "issue_frac": (rate(winst_per_ray, 1e12) / (issue_peak / 32)) if winst_per_ray else None,
+                "lanes_per_inst": (tinst_per_ray / winst_per_ray) if tinst_per_ray and winst_per_ray else None,
+                "l2": {"achieved_gbs": l2_gbs, "peak_gbs": l2_peak, "frac": (l2_gbs / l2_peak) if l2_gbs else None,
+                       "peak_source": "measured in this run: copy of 2 x 16 MiB (inside L2), CUDA events",
+                       "bytes_per_ray": l2_per_ray},
+                "hbm": {"achieved_gbs": dram_gbs, "peak_gbs": peak, "frac": (dram_gbs / peak) if dram_gbs else None,
+                        "peak_source": f"{peak_src} hbm_gbs (MEASURED_PEAKS.json)", "bytes_per_ray": dram_per_ray},
+                "algorithmic": {"bytes_per_ray": bytes_per_ray, "nodes_per_ray": nodes_per_ray,
+                                "prims_per_ray": prims_per_ray, "gbs_per_launch": alg_gbs,
+                                "gbs_per_step": bytes_per_ray * total_rays / args.steps / world / (frame_ms * 1e-3) / 1e9,
+                                "note": "node, primitive and ray bytes the traversal touches, L1 hits included; "
+                                        "against the L2 copy peak they are an upper bound of the L2 demand"},
+                "traffic_note": "traffic: ncu dram__bytes of full-wave launches per ray x rays of a mean launch",
+                "timing": "CUDA events around every k_extend_p launch of one frame of the same workload "
                           "rendered right after the timed steps",
-                "peak_source": f"{peak_src} hbm_gbs",
-                "bytes_per_ray": bytes_per_ray, "nodes_per_ray": nodes_per_ray, "prims_per_ray": prims_per_ray,
                 "extend_ms_per_launch": per_launch_ms, "extend_launches": int(rst.extend_launches),
                 "shade_ms_per_frame": rst.shade_ms, "extend_ms_per_frame": rst.extend_ms,
-                "extend_share": rst.extend_ms / max(frame_ms, 1e-9), "rays_per_launch": rays_per_launch,
-                # what actually reaches DRAM and L2 per second at the measured launch time
-                # (profiled bytes per ray x rays per launch / mean launch duration)
-                "dram_gbs": (traffic / (per_launch_ms * 1e-3) / 1e9) if traffic and per_launch_ms > 0 else None,
-                "l2_gbs": (l2_per_ray * rays_per_launch / (per_launch_ms * 1e-3) / 1e9)
-                if l2_per_ray and per_launch_ms > 0 else None}
+                "extend_share": rst.extend_ms / max(frame_ms, 1e-9), "rays_per_launch": rays_per_launch}
+    roofline["algorithmic"]["of_l2_peak_per_step"] = roofline["algorithmic"]["gbs_per_step"] / l2_peak
+    for k in ("frac",):
+        if roofline[k] is not None and roofline[k] > 1.2:
+            roofline["check"] = f"{k} {roofline[k]:.3f} > 1.2: the per-ray profile does not fit this build"
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": frame_ms, "higher_is_better": True,
