@@ -267,7 +267,7 @@ rt_status rt_scene_get_lbvh(rt_scene scene, unsigned long long* codes, unsigned 
 /* Progressive rendering with checkpoint and resume (no reference counterpart:
  * every Launcher::ignite renders all spp afresh, optx/camera_i.cu:58).  An
  * accumulator keeps the exact fixed-point pixel sums (colour and rays) of the
- * samples rendered so far and their count.  Sample k of a pixel draws from
+ * samples rendered so far, their count and the index of the first.  Sample k of a pixel draws from
  * its own counter-RNG stream, so rendering samples [0, a), then [a, b), ...
  * with one seed gives the sums, and so the image and rays per pixel, of one
  * launch of b samples bit for bit. */
@@ -292,6 +292,26 @@ rt_status rt_launch_accum(rt_scene scene, const rt_camera* cam, const rt_launch_
 rt_status rt_accum_state_size(rt_accum acc, size_t* bytes);
 rt_status rt_accum_save(rt_accum acc, void* host, size_t bytes, void* stream);
 rt_status rt_accum_load(rt_accum acc, const void* host, size_t bytes, void* stream);
+
+/* Sample ranges split across processes or GPUs (the one collective of the
+ * multi-GPU form of the single optixLaunch at optx/launcher.cxx:60-69: a sum
+ * of the accumulation buffers).  Each rank sets its accumulator's first
+ * sample index before rendering (rt_accum_set_first_sample, on an empty
+ * accumulator: rt_accum_reset clears it to 0) and renders its range;
+ * rt_accum_device_sums gives the device arrays of the exact sums (three
+ * int64 colour channels in units of 2^-32, and the uint32 rays per pixel,
+ * w*h each) for a sum-reduction across the ranks; rt_accum_set_range then
+ * declares the samples the reduced sums hold, [first, first + samples), and
+ * their total rays, and rt_accum_resolve writes frame->rawRGB (the clamped
+ * mean) and frame->rpp from the sums, stream-ordered.  Ranks that tile
+ * [0, n) this way give the image and rays per pixel of one n-sample launch
+ * bit for bit. */
+rt_status rt_accum_set_first_sample(rt_accum acc, unsigned long long first);
+rt_status rt_accum_device_sums(rt_accum acc, unsigned long long** red, unsigned long long** green,
+                               unsigned long long** blue, unsigned int** rays);
+rt_status rt_accum_set_range(rt_accum acc, unsigned long long first, unsigned long long samples,
+                             unsigned long long rays);
+rt_status rt_accum_resolve(rt_accum acc, const rt_frame* frame, void* stream);
 
 /* -------------------------------------------------------------- tuning */
 /* Launch shape of the wavefront (no reference counterpart; OptiX chooses its
@@ -443,6 +463,14 @@ rt_status rt_launcher_download(rt_launcher l, rt_float3* rawRGB, unsigned int* r
  * sort).  key_bits <= 32 sorts 32-bit keys, otherwise 64-bit keys. */
 rt_status rt_radix_sort_pairs(void* keys, unsigned int* vals, unsigned int n,
                               unsigned int key_bits, void* stream);
+
+/* Measurement helper (no reference counterpart): the copy bandwidth, in GB/s
+ * of bytes read plus written, of two device buffers of `bytes` each, copied
+ * `reps` times inside one launch with loads and stores that bypass L1; with
+ * 2 x bytes well inside L2 (e.g. 2 x 16 MiB) this is the L2 bandwidth the
+ * traversal's L2 traffic is reported against.  Allocates its buffers;
+ * synchronous. */
+rt_status rt_measure_copy_bandwidth(size_t bytes, unsigned int reps, double* gbs, void* stream);
 
 /* No counterpart in the reference.  The same stable pair sort for callers
  * that may not allocate device memory while they run (an engine that hands

@@ -161,6 +161,12 @@ SIGNATURES = {
     "rt_accum_state_size": [_P, ctypes.POINTER(ctypes.c_size_t)],
     "rt_accum_save": [_P, _P, ctypes.c_size_t, _P],
     "rt_accum_load": [_P, _P, ctypes.c_size_t, _P],
+    "rt_measure_copy_bandwidth": [ctypes.c_size_t, _U, ctypes.POINTER(ctypes.c_double), _P],
+    "rt_accum_set_first_sample": [_P, ctypes.c_ulonglong],
+    "rt_accum_device_sums": [_P, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p),
+                             ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p)],
+    "rt_accum_set_range": [_P, ctypes.c_ulonglong, ctypes.c_ulonglong, ctypes.c_ulonglong],
+    "rt_accum_resolve": [_P, _P, _P],
     "rt_tuning_set": [ctypes.POINTER(Tuning)],
     "rt_debug_fail_alloc": [_U],
     "rt_tuning_get": [ctypes.POINTER(Tuning)],
@@ -521,6 +527,21 @@ class Accum:
 
     def reset(self, stream=None):
         check(lib().rt_accum_reset(self.h, stream))
+
+    def set_first_sample(self, first):
+        check(lib().rt_accum_set_first_sample(self.h, first))
+
+    def device_sums(self):
+        """Device addresses of the red, green, blue (int64) and rays (uint32) sums, w*h each."""
+        ptrs = [ctypes.c_void_p() for _ in range(4)]
+        check(lib().rt_accum_device_sums(self.h, *[ctypes.byref(p) for p in ptrs]))
+        return [p.value for p in ptrs]
+
+    def set_range(self, first, samples, rays):
+        check(lib().rt_accum_set_range(self.h, first, samples, rays))
+
+    def resolve(self, frame, stream=None):
+        check(lib().rt_accum_resolve(self.h, ctypes.byref(frame), stream))
 
     def launch(self, scene, cam, params, frame, stream=None):
         """rt_launch_accum into a Frame of device pointers; returns LaunchStats."""

@@ -568,6 +568,17 @@ __global__ void __launch_bounds__(kThreads) k_finalize(const JobDev* __restrict_
     if (lane_id() == 0 && r) atomicAdd(&st->rays, r);
 }
 
+// An accumulator's sums as an image: the mean over `spp` samples clamped to
+// [0, 1] and the rays per pixel (k_finalize for sums merged elsewhere).
+__global__ void __launch_bounds__(kThreads) k_resolve(Acc acc, uint32_t npix, uint32_t spp, rt_float3* rawRGB,
+                                                      uint32_t* rpp) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npix) return;
+    rawRGB[p] = rt_float3{clamp01(fx_mean(acc.col[0][p], spp)), clamp01(fx_mean(acc.col[1][p], spp)),
+                          clamp01(fx_mean(acc.col[2][p], spp))};
+    if (rpp) rpp[p] = acc.rays[p];
+}
+
 // FP64 distance from the (binary32) ray to the selected primitive: the
 // binary32 Moller-Trumbore t loses digits on grazing hits (its error grows
 // like 1/sin of the grazing angle), so the reported distance re-evaluates the
@@ -859,6 +870,7 @@ void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s
         RT_REQUIRE(!(p.flags & RT_FLAG_GUIDES), "RT_FLAG_GUIDES is not supported with an accumulator");
         // the per-pixel ray count is u32 and the RNG's sample index u32
         RT_REQUIRE((accum->samples + p.spp) * p.depth < (1ull << 32), "accumulator full (samples x depth >= 2^32)");
+        RT_REQUIRE(accum->first + accum->samples + p.spp < (1ull << 32), "sample index beyond 2^32");
     }
     uint32_t flags_union = 0;
     for (const Job& j : jobs) {
@@ -895,7 +907,7 @@ void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s
         d.depth = jb.params.depth;
         d.seed = jb.params.seed;
         d.key1 = 0;
-        d.first_sample = accum ? uint32_t(accum->samples) : 0u;
+        d.first_sample = accum ? uint32_t(accum->first + accum->samples) : 0u;
         d.mean_spp = accum ? uint32_t(accum->samples + d.spp) : d.spp;
         d.root = g.root(jb.seg);
         d.pix_offset = uint32_t(total_pix);
@@ -1125,9 +1137,9 @@ void render_scene(Scene& sc, const rt_camera& cam, const rt_launch_params& p, co
 
 // Checkpoint bytes of an accumulator: a header, then the sums as on the device.
 struct AccumHeader {
-    char magic[8];   // "rtaccum1"
+    char magic[8];   // "rtaccum2"
     uint32_t W, H;
-    unsigned long long samples, rays;
+    unsigned long long first, samples, rays;
     unsigned long long sum_bytes;
 };
 
@@ -1218,6 +1230,7 @@ rt_status rt_accum_reset(rt_accum acc, void* stream) {
         cudaStream_t s = as_stream(stream);
         RT_CUDA(cudaMemsetAsync(a->sums.p, 0, accum_sum_bytes(*a), s));
         RT_CUDA(cudaStreamSynchronize(s));
+        a->first = 0;
         a->samples = 0;
         a->rays = 0;
     });
@@ -1252,9 +1265,10 @@ rt_status rt_accum_save(rt_accum acc, void* host, size_t bytes, void* stream) {
         RT_REQUIRE(host != nullptr, "host is NULL");
         RT_REQUIRE(bytes == sizeof(AccumHeader) + accum_sum_bytes(*a), "state size differs (rt_accum_state_size)");
         AccumHeader h{};
-        std::memcpy(h.magic, "rtaccum1", 8);
+        std::memcpy(h.magic, "rtaccum2", 8);
         h.W = a->W;
         h.H = a->H;
+        h.first = a->first;
         h.samples = a->samples;
         h.rays = a->rays;
         h.sum_bytes = accum_sum_bytes(*a);
@@ -1272,7 +1286,7 @@ rt_status rt_accum_load(rt_accum acc, const void* host, size_t bytes, void* stre
         RT_REQUIRE(bytes >= sizeof(AccumHeader), "not an accumulator state (too short)");
         AccumHeader h;
         std::memcpy(&h, host, sizeof h);
-        RT_REQUIRE(std::memcmp(h.magic, "rtaccum1", 8) == 0, "not an accumulator state");
+        RT_REQUIRE(std::memcmp(h.magic, "rtaccum2", 8) == 0, "not an accumulator state");
         RT_REQUIRE(h.W == a->W && h.H == a->H,
                    "accumulator state of another image size (" + std::to_string(h.W) + "x" + std::to_string(h.H) +
                        ", not " + std::to_string(a->W) + "x" + std::to_string(a->H) + ")");
@@ -1282,8 +1296,58 @@ rt_status rt_accum_load(rt_accum acc, const void* host, size_t bytes, void* stre
         RT_CUDA(cudaMemcpyAsync(a->sums.p, static_cast<const char*>(host) + sizeof h, h.sum_bytes,
                                 cudaMemcpyHostToDevice, s));
         RT_CUDA(cudaStreamSynchronize(s));
+        a->first = h.first;
         a->samples = h.samples;
         a->rays = h.rays;
+    });
+}
+
+rt_status rt_accum_set_first_sample(rt_accum acc, unsigned long long first) {
+    return guarded([&] {
+        AccumState* a = accum_from(acc);
+        RT_REQUIRE(a->samples == 0, "the accumulator holds samples (rt_accum_reset first)");
+        RT_REQUIRE(first < (1ull << 32), "first sample beyond 2^32");
+        a->first = first;
+    });
+}
+
+rt_status rt_accum_device_sums(rt_accum acc, unsigned long long** red, unsigned long long** green,
+                               unsigned long long** blue, unsigned int** rays) {
+    return guarded([&] {
+        AccumState* a = accum_from(acc);
+        const size_t n = size_t(a->W) * a->H;
+        unsigned long long* c = a->sums.as<unsigned long long>();
+        if (red) *red = c;
+        if (green) *green = c + n;
+        if (blue) *blue = c + 2 * n;
+        if (rays) *rays = reinterpret_cast<unsigned int*>(c + 3 * n);
+    });
+}
+
+rt_status rt_accum_set_range(rt_accum acc, unsigned long long first, unsigned long long samples,
+                             unsigned long long rays) {
+    return guarded([&] {
+        AccumState* a = accum_from(acc);
+        RT_REQUIRE(first + samples < (1ull << 32), "sample range beyond 2^32");
+        a->first = first;
+        a->samples = samples;
+        a->rays = rays;
+    });
+}
+
+rt_status rt_accum_resolve(rt_accum acc, const rt_frame* frame, void* stream) {
+    return guarded([&] {
+        AccumState* a = accum_from(acc);
+        RT_REQUIRE(frame != nullptr && frame->rawRGB != nullptr, "frame/rawRGB is NULL");
+        RT_REQUIRE(a->samples > 0, "the accumulator holds no samples");
+        const uint32_t n = a->W * a->H;
+        unsigned long long* c = a->sums.as<unsigned long long>();
+        Acc acc_v{};
+        for (int k = 0; k < 3; ++k) acc_v.col[k] = c + size_t(k) * n;
+        acc_v.rays = reinterpret_cast<uint32_t*>(c + 3 * size_t(n));
+        k_resolve<<<grid_for(n), kThreads, 0, as_stream(stream)>>>(acc_v, n, uint32_t(a->samples), frame->rawRGB,
+                                                                  frame->rpp);
+        RT_CHECK_LAUNCH();
     });
 }
 

@@ -144,8 +144,9 @@ struct Job {
 // pixel, and the samples per pixel they hold.
 struct AccumState {
     uint32_t W = 0, H = 0;
-    unsigned long long samples = 0;
-    unsigned long long rays = 0;   // sum of the per-pixel ray counts
+    unsigned long long first = 0;     // sample index of the first sample the sums hold
+    unsigned long long samples = 0;   // the sums hold samples [first, first + samples)
+    unsigned long long rays = 0;      // sum of the per-pixel ray counts
     DevBuf sums;
 };
 

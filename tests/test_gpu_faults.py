@@ -86,3 +86,13 @@ def test_failed_rebuild_leaves_no_stale_scene(product, cuda):
     sc.build(60, layout=R.RT_LAYOUT_INSTANCED)
     _same(R.render(sc, cam, params), ref)   # layouts give identical images
     sc.close()
+
+
+def test_copy_bandwidth_probe(product, cuda):
+    """The L2 copy probe returns a positive rate and refuses bad sizes."""
+    import ctypes
+    R = product
+    g = ctypes.c_double()
+    R.check(R.lib().rt_measure_copy_bandwidth(1 << 20, 4, ctypes.byref(g), None))
+    assert g.value > 0
+    assert R.lib().rt_measure_copy_bandwidth(100, 4, ctypes.byref(g), None) == R.RT_ERR_INVALID_ARG
