@@ -464,7 +464,7 @@ def inverse_leg(torch, nscenes, iters):
     scene-by-scene launches, same number of iterations."""
     from rtxplay_gb300 import inverse
     specs = inverse.inverse_specs(nscenes, seed=7, level=4, size=256, spp=16, depth=8)
-    e0, eb, lb, tb = inverse.run(torch, specs, iters, batched=True)
+    e0, eb, lb, tb = inverse.run(torch, specs, iters, batched=True, graph=True)
     _, es, ls, ts = inverse.run(torch, specs, iters, batched=False)
     return {"workload": f"{nscenes} final-scene variants, half-extent U{{3..8}}, level 4, 256x256, 16 spp, depth 8; "
                         "albedos from 0.5 towards the recipe's, Adam lr 1e-2, L2 loss of the clamped image",
@@ -472,6 +472,11 @@ def inverse_leg(torch, nscenes, iters):
             "batched_ms_per_iter": tb / iters * 1e3, "serial_ms_per_iter": ts / iters * 1e3,
             "albedo_error_start": e0, "albedo_error_batched": eb, "albedo_error_serial": es,
             "loss_batched": lb, "loss_serial": ls,
+            "batched_iteration": "one CUDA graph launch per iteration (set albedos -> batched render with the "
+                                 "wave loop as a conditional node -> L2 loss -> batched adjoint -> Adam with a "
+                                 "device step counter); the first iteration runs as calls and is captured, its "
+                                 "capture inside the timed region; captured launches' errors checked once at "
+                                 "the end (rt_batch_status)",
             "timing": "host wall clock around the iterations (device synchronised on both ends)"}
 
 

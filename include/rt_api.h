@@ -390,6 +390,22 @@ rt_status rt_batch_set_adjoint(rt_batch b, unsigned int index, const rt_float3* 
                                double* grad_albedo, double* grad_fuzz, double* grad_sky);
 rt_status rt_batch_adjoint(rt_batch b, void* stream);
 
+/* One optimisation iteration as one CUDA graph (no reference counterpart):
+ * rt_batch_set_albedos, rt_batch_launch, rt_batch_adjoint, rt_l2_loss_grad
+ * and rt_adam_step_device may be called on a stream that is being captured
+ * (cudaStreamBeginCapture, or a framework's graph capture), after the same
+ * calls ran once outside the capture (which sizes the batch's buffers and
+ * uploads its job tables and optics).  Inside a capture they enqueue
+ * stream-ordered work only: the wave loop becomes a conditional WHILE node
+ * of the captured graph, no stats are returned (stats must be NULL), and an
+ * error of a captured launch (stack overflow, wave bound) is not returned by
+ * the call but kept in the batch's error word.  rt_batch_status synchronises
+ * `stream`, returns that error (RT_ERR_LIMIT / RT_ERR_INTERNAL) or RT_OK, and
+ * clears the word.  The graph stays valid while the batch and the buffers
+ * it was captured with live and the batch is not rebuilt; host-side optics
+ * changes (rt_scene_set_optics) need a launch outside the capture. */
+rt_status rt_batch_status(rt_batch b, void* stream);
+
 /* Device-side albedos (no reference counterpart): every thing's albedo from
  * a device array of 3 floats per thing (a batch: all scenes' things in the
  * order they were added), on `stream`, without a refit and without touching
@@ -410,6 +426,12 @@ rt_status rt_l2_loss_grad(const rt_float3* image, const rt_float3* target, rt_fl
 rt_status rt_adam_step(float* theta, const double* grad, float* m, float* v, unsigned int n, float lr,
                        float beta1, float beta2, float eps, unsigned int step, float lo, float hi,
                        void* stream);
+/* The same step with its counter on the device: the step taken is
+ * t = *step + 1 (bias corrections from it), after which *step = t.  An
+ * iteration captured into a CUDA graph advances with every replay. */
+rt_status rt_adam_step_device(float* theta, const double* grad, float* m, float* v, unsigned int n, float lr,
+                              float beta1, float beta2, float eps, unsigned int* step, float lo, float hi,
+                              void* stream);
 
 /* ------------------------------------------------------------- adjoint */
 /* Gradients of an image loss (no counterpart in the reference): given the

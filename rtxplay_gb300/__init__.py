@@ -152,6 +152,7 @@ SIGNATURES = {
     "rt_batch_set_albedos": [_P, _P, _P],
     "rt_l2_loss_grad": [_P, _P, _P, _U, _P, _P],
     "rt_adam_step": [_P, _P, _P, _P, _U, _F, _F, _F, _F, _U, _F, _F, _P],
+    "rt_adam_step_device": [_P, _P, _P, _P, _U, _F, _F, _F, _F, _P, _F, _F, _P],
     "rt_accum_create": [ctypes.POINTER(_P), _U, _U],
     "rt_accum_destroy": [_P],
     "rt_accum_reset": [_P, _P],
@@ -163,6 +164,7 @@ SIGNATURES = {
     "rt_accum_load": [_P, _P, ctypes.c_size_t, _P],
     "rt_measure_copy_bandwidth": [ctypes.c_size_t, _U, ctypes.POINTER(ctypes.c_double), _P],
     "rt_accum_set_first_sample": [_P, ctypes.c_ulonglong],
+    "rt_batch_status": [_P, _P],
     "rt_accum_device_sums": [_P, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p),
                              ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p)],
     "rt_accum_set_range": [_P, ctypes.c_ulonglong, ctypes.c_ulonglong, ctypes.c_ulonglong],
@@ -466,7 +468,11 @@ class Batch:
             check(lib().rt_batch_set_layout(self.h, layout))
         check(lib().rt_batch_build(self.h, morton_bits, stream))
 
-    def launch(self, stream=None):
+    def launch(self, stream=None, stats=True):
+        """rt_batch_launch; stats=False passes no stats (required inside a stream capture)."""
+        if not stats:
+            check(lib().rt_batch_launch(self.h, stream, None))
+            return None
         st = LaunchStats()
         check(lib().rt_batch_launch(self.h, stream, ctypes.byref(st)))
         return st
@@ -477,6 +483,10 @@ class Batch:
 
     def adjoint(self, stream=None):
         check(lib().rt_batch_adjoint(self.h, stream))
+
+    def status(self, stream=None):
+        """rt_batch_status: raises the error of a launch captured into a graph, if any."""
+        check(lib().rt_batch_status(self.h, stream))
 
     def set_albedos(self, albedo, stream=None):
         """rt_batch_set_albedos from a device pointer (3 floats per thing, scenes in order)."""
@@ -498,6 +508,12 @@ def l2_loss_grad(image, target, grad_image, n, loss=None, stream=None):
 def adam_step(theta, grad, m, v, n, step, lr=1e-2, beta1=0.9, beta2=0.999, eps=1e-8, lo=0.0, hi=1.0, stream=None):
     """rt_adam_step on device pointers."""
     check(lib().rt_adam_step(theta, grad, m, v, n, lr, beta1, beta2, eps, step, lo, hi, stream))
+
+
+def adam_step_device(theta, grad, m, v, n, step_ptr, lr=1e-2, beta1=0.9, beta2=0.999, eps=1e-8, lo=0.0, hi=1.0,
+                     stream=None):
+    """rt_adam_step_device: the step counter is a device uint32 (advanced by the call)."""
+    check(lib().rt_adam_step_device(theta, grad, m, v, n, lr, beta1, beta2, eps, step_ptr, lo, hi, stream))
 
 
 class Accum:

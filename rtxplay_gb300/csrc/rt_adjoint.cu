@@ -366,24 +366,48 @@ __global__ void k_adjoint_out(const double* __restrict__ G, uint32_t nthings_tot
         o.sky[threadIdx.x] = G[4 * size_t(nthings_total) + 6 * size_t(jx) + threadIdx.x];
 }
 
-struct AdjWorkspace {
-    DevBuf jobs, outs, G, err, gpix;
-    std::vector<AdjJob> jobs_host;
-    std::vector<AdjOut> outs_host;
-};
-
-AdjWorkspace& adj_workspace() {
-    static thread_local AdjWorkspace ws;
-    return ws;
+// ORs the launch's error word into a caller's word (launches inside a stream
+// capture, which read nothing back).
+__global__ void k_or_error(const uint32_t* __restrict__ err, uint32_t* sticky) {
+    if (*err) atomicOr(sticky, *err);
 }
 
 }  // namespace
 
-void adjoint_jobs(const Geometry& g, const std::vector<AdjointJob>& jobs, cudaStream_t s) {
+struct AdjointWorkspace {
+    DevBuf jobs, outs, G, err, gpix;
+    std::vector<AdjJob> jobs_host, jobs_uploaded;
+    std::vector<AdjOut> outs_host, outs_uploaded;
+};
+
+AdjointWorkspace* adjoint_workspace_new() { return new AdjointWorkspace(); }
+void adjoint_workspace_free(AdjointWorkspace* ws) { delete ws; }
+
+namespace {
+AdjointWorkspace& adj_workspace() {
+    static thread_local AdjointWorkspace ws;
+    return ws;
+}
+
+template <class T>
+bool same_table(const std::vector<T>& a, const std::vector<T>& b) {
+    return a.size() == b.size() && std::memcmp(a.data(), b.data(), a.size() * sizeof(T)) == 0;
+}
+}  // namespace
+
+// Inside a stream capture the adjoint enqueues its work without reading back:
+// the job and output tables must be the ones the workspace already holds and
+// no buffer may grow (both hold after the same call ran once outside the
+// capture), and the error word is ORed into `sticky` for a later check.
+void adjoint_jobs(const Geometry& g, const std::vector<AdjointJob>& jobs, cudaStream_t s, AdjointWorkspace* own,
+                  uint32_t* sticky) {
     NvtxRange nvtx("rt adjoint");
     RT_REQUIRE(!jobs.empty(), "no adjoint jobs");
     RT_REQUIRE(jobs.size() < (1u << 24), "too many jobs (>= 2^24)");
-    AdjWorkspace& ws = adj_workspace();
+    const bool capturing = stream_capturing(s);
+    RT_REQUIRE(!capturing || sticky, "this adjoint cannot run inside a stream capture");
+    CaptureNoAlloc no_alloc(capturing);
+    AdjointWorkspace& ws = own ? *own : adj_workspace();
     const uint32_t nj = uint32_t(jobs.size());
     ws.jobs_host.resize(nj);
     ws.outs_host.resize(nj);
@@ -428,8 +452,15 @@ void adjoint_jobs(const Geometry& g, const std::vector<AdjointJob>& jobs, cudaSt
     ws.outs.reserve(nj * sizeof(AdjOut));
     ws.G.reserve(gsize);
     ws.err.reserve(4);
-    RT_CUDA(cudaMemcpyAsync(ws.jobs.p, ws.jobs_host.data(), nj * sizeof(AdjJob), cudaMemcpyHostToDevice, s));
-    RT_CUDA(cudaMemcpyAsync(ws.outs.p, ws.outs_host.data(), nj * sizeof(AdjOut), cudaMemcpyHostToDevice, s));
+    if (capturing) {
+        RT_REQUIRE(same_table(ws.jobs_host, ws.jobs_uploaded) && same_table(ws.outs_host, ws.outs_uploaded),
+                   "the adjoint's job table differs from the workspace's: make the same call once before capturing");
+    } else {
+        RT_CUDA(cudaMemcpyAsync(ws.jobs.p, ws.jobs_host.data(), nj * sizeof(AdjJob), cudaMemcpyHostToDevice, s));
+        RT_CUDA(cudaMemcpyAsync(ws.outs.p, ws.outs_host.data(), nj * sizeof(AdjOut), cudaMemcpyHostToDevice, s));
+        ws.jobs_uploaded = ws.jobs_host;
+        ws.outs_uploaded = ws.outs_host;
+    }
     RT_CUDA(cudaMemsetAsync(ws.G.p, 0, gsize, s));
     RT_CUDA(cudaMemsetAsync(ws.err.p, 0, 4, s));
     const uint32_t sh_things = std::min(max_things, kAdjShThings);
@@ -449,6 +480,11 @@ void adjoint_jobs(const Geometry& g, const std::vector<AdjointJob>& jobs, cudaSt
     const unsigned gx = std::max(1u, std::min(64u, (max_things + 255) / 256));
     k_adjoint_out<<<dim3(gx, nj), 256, 0, s>>>(ws.G.as<double>(), g.nthings, ws.outs.as<AdjOut>(), nj);
     RT_CHECK_LAUNCH();
+    if (capturing) {
+        k_or_error<<<1, 1, 0, s>>>(ws.err.as<uint32_t>(), sticky);
+        RT_CHECK_LAUNCH();
+        return;
+    }
     uint32_t herr = 0;
     RT_CUDA(cudaMemcpyAsync(&herr, ws.err.p, 4, cudaMemcpyDeviceToHost, s));
     RT_CUDA(cudaStreamSynchronize(s));

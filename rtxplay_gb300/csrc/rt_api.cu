@@ -21,6 +21,18 @@ bool injected_alloc_failure() {
     return false;
 }
 
+bool stream_capturing(cudaStream_t s) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    RT_CUDA(cudaStreamIsCapturing(s, &cs));
+    RT_REQUIRE(cs != cudaStreamCaptureStatusInvalidated, "the stream's capture has been invalidated");
+    return cs == cudaStreamCaptureStatusActive;
+}
+
+int& capture_no_alloc() {
+    static thread_local int depth = 0;
+    return depth;
+}
+
 void set_last_error(const std::string& msg) { g_last_error = msg; }
 void clear_last_error() { g_last_error.clear(); }
 

@@ -38,6 +38,20 @@ struct NvtxRange {
 // the one chosen to fail.
 bool injected_alloc_failure();
 
+// Stream capture: true while `s` is being captured into a CUDA graph.  Calls
+// that support capture enqueue only stream-ordered work then (no host reads,
+// no synchronisation) and may not grow a device buffer: inside a
+// CaptureNoAlloc scope a DevBuf that would have to allocate throws instead.
+bool stream_capturing(cudaStream_t s);
+int& capture_no_alloc();
+struct CaptureNoAlloc {
+    bool on;
+    explicit CaptureNoAlloc(bool enable) : on(enable) { if (on) ++capture_no_alloc(); }
+    ~CaptureNoAlloc() { if (on) --capture_no_alloc(); }
+    CaptureNoAlloc(const CaptureNoAlloc&) = delete;
+    CaptureNoAlloc& operator=(const CaptureNoAlloc&) = delete;
+};
+
 #define RT_CUDA(call)                                                        \
     do {                                                                     \
         cudaError_t rt_e_ = (call);                                          \
@@ -90,6 +104,9 @@ struct DevBuf {
     }
     void reserve(size_t n) {
         if (n <= bytes) return;
+        if (capture_no_alloc())
+            throw Error(RT_ERR_INVALID_ARG, "a device buffer would have to grow inside a stream capture: make the "
+                                            "same call once before capturing");
         release();
         if (n == 0) return;
         if (injected_alloc_failure())

@@ -65,6 +65,30 @@ __global__ void k_adam(float* __restrict__ theta, const double* __restrict__ gra
     theta[i] = fminf(fmaxf(th, lo), hi);
 }
 
+// The same step with the step number on the device (an iteration captured
+// into a CUDA graph replays the same kernel arguments): t = *step + 1, the
+// bias corrections from it; k_step_advance then stores t.
+__global__ void k_adam_dev(float* __restrict__ theta, const double* __restrict__ grad, float* __restrict__ m,
+                           float* __restrict__ v, uint32_t n, float lr, float b1, float b2, float eps,
+                           const uint32_t* __restrict__ step, float lo, float hi) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double t = double(*step) + 1.0;
+    const float bc1 = float(1.0 - pow(double(b1), t));
+    const float bc2 = float(1.0 - pow(double(b2), t));
+    const float g = float(grad[i]);
+    const float mi = b1 * m[i] + (1.f - b1) * g;
+    const float vi = b2 * v[i] + (1.f - b2) * (g * g);
+    m[i] = mi;
+    v[i] = vi;
+    const float mh = mi / bc1;
+    const float vh = vi / bc2;
+    const float th = theta[i] - lr * mh / (sqrtf(vh) + eps);
+    theta[i] = fminf(fmaxf(th, lo), hi);
+}
+
+__global__ void k_step_advance(uint32_t* step) { *step += 1u; }
+
 }  // namespace
 }  // namespace rt
 
@@ -93,6 +117,23 @@ rt_status rt_adam_step(float* theta, const double* grad, float* m, float* v, uns
         const float bc2 = float(1.0 - std::pow(double(beta2), double(step)));
         k_adam<<<(n + kThreads - 1) / kThreads, kThreads, 0, as_stream(stream)>>>(theta, grad, m, v, n, lr, beta1,
                                                                                    beta2, eps, bc1, bc2, lo, hi);
+        RT_CHECK_LAUNCH();
+    });
+}
+
+rt_status rt_adam_step_device(float* theta, const double* grad, float* m, float* v, unsigned int n, float lr,
+                              float beta1, float beta2, float eps, unsigned int* step, float lo, float hi,
+                              void* stream) {
+    return guarded([&] {
+        RT_REQUIRE(theta && grad && m && v && step, "theta/grad/m/v/step is NULL");
+        RT_REQUIRE(beta1 >= 0.f && beta1 < 1.f && beta2 >= 0.f && beta2 < 1.f, "betas must be in [0, 1)");
+        cudaStream_t s = as_stream(stream);
+        if (n) {
+            k_adam_dev<<<(n + kThreads - 1) / kThreads, kThreads, 0, s>>>(theta, grad, m, v, n, lr, beta1, beta2, eps,
+                                                                          step, lo, hi);
+            RT_CHECK_LAUNCH();
+        }
+        k_step_advance<<<1, 1, 0, s>>>(step);
         RT_CHECK_LAUNCH();
     });
 }

@@ -23,6 +23,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <vector>
 
@@ -545,9 +546,12 @@ __device__ __forceinline__ float fx_mean(unsigned long long s, uint32_t spp) {
 }
 
 // optx/camera_i.cu:104-113: mean over spp clamped to [0,1]; rpp; guides.
+// With `sticky` (launches inside a stream capture, which read no state back)
+// the launch's error bits are also ORed into that word for a later check.
 __global__ void __launch_bounds__(kThreads) k_finalize(const JobDev* __restrict__ jobs, uint32_t nj, Acc acc,
-                                                       uint32_t total_pix, WaveState* st) {
+                                                       uint32_t total_pix, WaveState* st, uint32_t* sticky) {
     const uint32_t gp = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sticky && gp == 0 && st->err) atomicOr(sticky, st->err);
     unsigned long long r = 0;
     if (gp < total_pix) {
         const JobDev& j = jobs[job_of_pixel(jobs, nj, gp)];
@@ -750,6 +754,7 @@ struct Workspace {
     DevBuf hits, hthing, acc, acc_gd, jobs, state;
     WaveState* host_state = nullptr;   // pinned
     std::vector<JobDev> jobs_host;
+    std::vector<JobDev> jobs_uploaded;   // the job table in `jobs` (a capture may not upload one)
     std::vector<cudaEvent_t> events;
     WaveGraph graph;
     ~Workspace() {
@@ -812,19 +817,19 @@ unsigned persistent_grid(ExtendFn fn, uint32_t bpsm) {
     return unsigned(per_sm * sm_count());
 }
 
-void build_wave_graph(Workspace& ws, const WaveLaunch& L) {
-    WaveGraph& G = ws.graph;
-    G.reset();
-    RT_CUDA(cudaGraphCreate(&G.graph, 0));
+// Adds the wave loop to `graph` after `deps`: a conditional WHILE node (its
+// condition set to 1 at every launch of the graph) whose body is extend ->
+// shade -> ctrl; k_wave_ctrl clears the condition when the loop is done.
+cudaGraphNode_t add_wave_loop(cudaGraph_t graph, const cudaGraphNode_t* deps, size_t ndeps, const WaveLaunch& L) {
     cudaGraphConditionalHandle handle;
-    RT_CUDA(cudaGraphConditionalHandleCreate(&handle, G.graph, 1u, cudaGraphCondAssignDefault));
+    RT_CUDA(cudaGraphConditionalHandleCreate(&handle, graph, 1u, cudaGraphCondAssignDefault));
     cudaGraphNodeParams cp = {};
     cp.type = cudaGraphNodeTypeConditional;
     cp.conditional.handle = handle;
     cp.conditional.type = cudaGraphCondTypeWhile;
     cp.conditional.size = 1;
     cudaGraphNode_t cnode;
-    RT_CUDA(cudaGraphAddNode(&cnode, G.graph, nullptr, nullptr, 0, &cp));
+    RT_CUDA(cudaGraphAddNode(&cnode, graph, deps, nullptr, ndeps, &cp));
     cudaGraph_t body = cp.conditional.phGraph_out[0];
 
     WaveLaunch l = L;   // kernel arguments must stay addressable while the nodes are added
@@ -854,14 +859,46 @@ void build_wave_graph(Workspace& ws, const WaveLaunch& L) {
     kp.blockDim = dim3(1);
     kp.kernelParams = ctrl_args;
     RT_CUDA(cudaGraphAddKernelNode(&n_ctrl, body, &n_shade, 1, &kp));
+    return cnode;
+}
+
+void build_wave_graph(Workspace& ws, const WaveLaunch& L) {
+    WaveGraph& G = ws.graph;
+    G.reset();
+    RT_CUDA(cudaGraphCreate(&G.graph, 0));
+    add_wave_loop(G.graph, nullptr, 0, L);
     RT_CUDA(cudaGraphInstantiate(&G.exec, G.graph, 0));
+}
+
+// Adds the wave loop to the graph that stream `s` is being captured into, after
+// the work captured so far, and makes later captured work depend on it.
+void capture_wave_loop(cudaStream_t s, const WaveLaunch& L) {
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t graph;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    RT_CUDA(cudaStreamGetCaptureInfo(s, &cs, nullptr, &graph, &deps, nullptr, &ndeps));
+    RT_REQUIRE(cs == cudaStreamCaptureStatusActive, "stream is not capturing");
+    const std::vector<cudaGraphNode_t> d(deps, deps + ndeps);   // valid until the next capture call
+    cudaGraphNode_t loop = add_wave_loop(graph, d.data(), d.size(), L);
+    RT_CUDA(cudaStreamUpdateCaptureDependencies(s, &loop, nullptr, 1, cudaStreamSetCaptureDependencies));
 }
 
 }  // namespace
 
-void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s, rt_launch_stats* stats,
-                 AccumState* accum) {
+namespace {
+
+// The wavefront over all jobs with workspace `ws`.  Inside a stream capture
+// (a caller capturing a whole iteration into one CUDA graph) the launch
+// enqueues its work without reading anything back: the job table must be
+// the one the workspace already holds and no buffer may grow (both hold
+// after the same launch ran once outside the capture), the wave loop becomes
+// a conditional node of the captured graph, no stats are filled in, and the
+// launch's error bits are ORed into `sticky` for a later check.
+void render_jobs_ws(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s, rt_launch_stats* stats,
+                    AccumState* accum, Workspace& ws, uint32_t* sticky) {
     NvtxRange nvtx("rt render");
+    const bool capturing = stream_capturing(s);
     RT_REQUIRE(!jobs.empty(), "no jobs to render");
     if (accum) {
         RT_REQUIRE(jobs.size() == 1, "an accumulator takes one job");
@@ -886,8 +923,14 @@ void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s
     const bool count = (flags_union & RT_FLAG_COUNT_VISITS) != 0;
     const int any_guides = (flags_union & RT_FLAG_GUIDES) ? 1 : 0;
     const bool use_graph = graph_mode() && !stage_timing;
+    if (capturing) {
+        RT_REQUIRE(!stats && !accum && !stage_timing && !count,
+                   "inside a stream capture: no stats, accumulator, stage timing or visit counting");
+        RT_REQUIRE(use_graph, "inside a stream capture the wave loop must be a graph (RTX_GRAPH=0 is set)");
+        RT_REQUIRE(sticky != nullptr, "this launch cannot run inside a stream capture");
+    }
+    CaptureNoAlloc no_alloc(capturing);
 
-    Workspace& ws = workspace();
     const uint32_t nj = uint32_t(jobs.size());
     ws.jobs_host.resize(nj);
     unsigned long long total_paths = 0;
@@ -942,7 +985,10 @@ void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s
     if (any_guides) ws.acc_gd.reserve(size_t(total_pix) * 48);
     ws.jobs.reserve(size_t(nj) * sizeof(JobDev));
     ws.state.reserve(sizeof(WaveState));
-    if (!ws.host_state) RT_CUDA(cudaMallocHost(&ws.host_state, sizeof(WaveState)));
+    if (!ws.host_state) {
+        RT_REQUIRE(!capturing, "make the same launch once before capturing it");
+        RT_CUDA(cudaMallocHost(&ws.host_state, sizeof(WaveState)));
+    }
 
     WaveLaunch L;
     for (int b = 0; b < 2; ++b) {
@@ -979,7 +1025,16 @@ void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s
     }
     L.any_guides = any_guides;
 
-    RT_CUDA(cudaMemcpyAsync(ws.jobs.p, ws.jobs_host.data(), size_t(nj) * sizeof(JobDev), cudaMemcpyHostToDevice, s));
+    const bool same_jobs = ws.jobs_uploaded.size() == ws.jobs_host.size() &&
+                           std::memcmp(ws.jobs_uploaded.data(), ws.jobs_host.data(), size_t(nj) * sizeof(JobDev)) == 0;
+    if (capturing) {
+        RT_REQUIRE(same_jobs, "the job table differs from the workspace's: make the same launch once before "
+                              "capturing it");
+    } else {
+        RT_CUDA(cudaMemcpyAsync(ws.jobs.p, ws.jobs_host.data(), size_t(nj) * sizeof(JobDev), cudaMemcpyHostToDevice,
+                                s));
+        ws.jobs_uploaded = ws.jobs_host;
+    }
     if (!accum) RT_CUDA(cudaMemsetAsync(ws.acc.p, 0, size_t(total_pix) * 28, s));
     if (any_guides) RT_CUDA(cudaMemsetAsync(ws.acc_gd.p, 0, size_t(total_pix) * 48, s));
     const uint32_t n0 = W;
@@ -989,7 +1044,10 @@ void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s
     uint32_t launches = 2;
     std::vector<std::pair<size_t, int>> timed;   // (event index, 0 extend / 1 shade)
 
-    if (use_graph) {
+    if (capturing) {
+        NvtxRange nvtx_loop("wave loop (captured)");
+        capture_wave_loop(s, L);
+    } else if (use_graph) {
         const std::vector<const void*> key = {
             reinterpret_cast<const void*>(L.ext_fn), reinterpret_cast<const void*>(uintptr_t(L.qgrid)),
             reinterpret_cast<const void*>(uintptr_t(L.egrid)), reinterpret_cast<const void*>(L.shade),
@@ -1051,9 +1109,11 @@ void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s
             if (hs.count[hs.cur] == 0 || hs.err) break;
         }
     }
-    k_finalize<<<grid_for(total_pix), kThreads, 0, s>>>(L.jobs, nj, L.acc, uint32_t(total_pix), L.st);
+    k_finalize<<<grid_for(total_pix), kThreads, 0, s>>>(L.jobs, nj, L.acc, uint32_t(total_pix), L.st,
+                                                        capturing ? sticky : nullptr);
     RT_CHECK_LAUNCH();
     launches += 1;
+    if (capturing) return;
     RT_CUDA(cudaMemcpyAsync(ws.host_state, L.st, sizeof(WaveState), cudaMemcpyDeviceToHost, s));
     RT_CUDA(cudaStreamSynchronize(s));
     const WaveState hs = *ws.host_state;
@@ -1085,6 +1145,13 @@ void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s
         }
         if (!timed.empty()) stats->extend_launches = uint32_t(timed.size() / 2);
     }
+}
+
+}  // namespace
+
+void render_jobs(const Geometry& g, const std::vector<Job>& jobs, cudaStream_t s, rt_launch_stats* stats,
+                 AccumState* accum) {
+    render_jobs_ws(g, jobs, s, stats, accum, workspace(), nullptr);
 }
 
 namespace {
@@ -1180,7 +1247,11 @@ Launcher* launcher_from(rt_launcher l) {
     return reinterpret_cast<Launcher*>(l);
 }
 
-// Many scenes rendered by one wavefront over one segmented geometry.
+// Many scenes rendered by one wavefront over one segmented geometry.  A
+// batch owns the workspaces of its launches and adjoints (queues, sums, job
+// tables), so that a launch captured into a CUDA graph keeps pointing at
+// buffers that no other launch reuses or regrows, and a device error word
+// that launches inside a capture report to (rt_batch_status).
 struct Batch {
     std::vector<Scene*> scenes;
     std::vector<Job> jobs;
@@ -1188,6 +1259,10 @@ struct Batch {
     int layout = RT_LAYOUT_AUTO;
     Geometry geo;
     bool built = false;
+    Workspace ws;
+    std::unique_ptr<AdjointWorkspace, void (*)(AdjointWorkspace*)> adj_ws{adjoint_workspace_new(),
+                                                                          adjoint_workspace_free};
+    DevBuf sticky;                 // error bits of captured launches since the last rt_batch_status
 };
 
 Batch* batch_from(rt_batch b) {
@@ -1566,6 +1641,8 @@ rt_status rt_batch_build(rt_batch b, unsigned int morton_bits, void* stream) {
         RT_REQUIRE(!B->scenes.empty(), "batch is empty");
         B->built = false;   // a build that fails half way leaves no launchable batch behind
         build_geometry(B->geo, B->scenes, int(morton_bits), B->layout, as_stream(stream));
+        B->sticky.reserve(4);
+        RT_CUDA(cudaMemset(B->sticky.p, 0, 4));
         B->built = true;
     });
 }
@@ -1575,8 +1652,28 @@ rt_status rt_batch_launch(rt_batch b, void* stream, rt_launch_stats* stats) {
         Batch* B = batch_from(b);
         if (!B->built) throw Error(RT_ERR_NOT_BUILT, "batch not built (call rt_batch_build)");
         rt_launch_stats st{};
-        sync_optics(B->geo, B->scenes, as_stream(stream));
-        render_jobs(B->geo, B->jobs, as_stream(stream), stats ? stats : &st);
+        cudaStream_t s = as_stream(stream);
+        const bool capturing = stream_capturing(s);
+        RT_REQUIRE(!capturing || !stats, "no stats from a launch inside a stream capture");
+        sync_optics(B->geo, B->scenes, s);
+        render_jobs_ws(B->geo, B->jobs, s, capturing ? nullptr : (stats ? stats : &st), nullptr, B->ws,
+                       B->sticky.as<uint32_t>());
+    });
+}
+
+rt_status rt_batch_status(rt_batch b, void* stream) {
+    return guarded([&] {
+        Batch* B = batch_from(b);
+        if (!B->built) throw Error(RT_ERR_NOT_BUILT, "batch not built (call rt_batch_build)");
+        cudaStream_t s = as_stream(stream);
+        uint32_t err = 0;
+        RT_CUDA(cudaMemcpyAsync(&err, B->sticky.p, 4, cudaMemcpyDeviceToHost, s));
+        RT_CUDA(cudaMemsetAsync(B->sticky.p, 0, 4, s));
+        RT_CUDA(cudaStreamSynchronize(s));
+        if (err & kErrBounds) throw Error(RT_ERR_INTERNAL, "a captured launch failed a bounds check (RT_CHECKS build)");
+        if (err & 1u) throw Error(RT_ERR_LIMIT, "a captured launch overflowed its traversal stack");
+        if (err & 2u) throw Error(RT_ERR_LIMIT, "a captured launch exceeded its wave bound");
+        if (err) throw Error(RT_ERR_INTERNAL, "a captured launch reported error bits " + std::to_string(err));
     });
 }
 
@@ -1611,7 +1708,7 @@ rt_status rt_batch_adjoint(rt_batch b, void* stream) {
         RT_REQUIRE(!jobs.empty(), "no scene of the batch has adjoint buffers (rt_batch_set_adjoint)");
         cudaStream_t s = as_stream(stream);
         sync_optics(B->geo, B->scenes, s);
-        adjoint_jobs(B->geo, jobs, s);
+        adjoint_jobs(B->geo, jobs, s, B->adj_ws.get(), B->sticky.as<uint32_t>());
     });
 }
 

@@ -950,6 +950,8 @@ void sync_optics(Geometry& g, const std::vector<Scene*>& scenes, cudaStream_t s)
     bool stale = false;
     for (size_t si = 0; si < scenes.size(); ++si) stale = stale || scenes[si]->optics_version != g.optics_seen[si];
     if (!stale) return;
+    RT_REQUIRE(!stream_capturing(s), "optics changed on the host since the last launch: upload them with a "
+                                     "launch outside the stream capture first");
     g.things_host.clear();
     for (size_t si = 0; si < scenes.size(); ++si) {
         for (const ThingHost& th : scenes[si]->things) g.things_host.push_back(thing_dev(th));

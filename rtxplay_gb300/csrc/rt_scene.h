@@ -173,7 +173,16 @@ struct AdjointJob {
     double* grad_sky;      // [6]: ambient rgb, white rgb
 };
 
-// Replays the paths of all jobs and writes their gradients (rt_adjoint.cu).
-void adjoint_jobs(const Geometry& g, const std::vector<AdjointJob>& jobs, cudaStream_t s);
+// Device buffers and job tables of adjoint launches (a batch keeps its own,
+// so that a launch captured into a CUDA graph owns what it points at).
+struct AdjointWorkspace;
+AdjointWorkspace* adjoint_workspace_new();
+void adjoint_workspace_free(AdjointWorkspace* ws);
+
+// Replays the paths of all jobs and writes their gradients (rt_adjoint.cu),
+// with workspace `ws` (NULL: the calling thread's); inside a stream capture
+// the error word is ORed into `sticky` instead of being read back.
+void adjoint_jobs(const Geometry& g, const std::vector<AdjointJob>& jobs, cudaStream_t s,
+                  AdjointWorkspace* ws = nullptr, uint32_t* sticky = nullptr);
 
 }  // namespace rt

@@ -4,7 +4,11 @@ variants from target images with Adam, every step on the device.
 One iteration, batched: ``rt_batch_set_albedos`` (parameters -> optics),
 ``rt_batch_launch`` (all scenes, one wavefront), ``rt_l2_loss_grad`` over all
 frames (one contiguous image buffer), ``rt_batch_adjoint`` (all scenes, one
-launch), ``rt_adam_step`` over all parameters.  Serial runs the same steps
+launch), ``rt_adam_step`` over all parameters.  In graph mode the first
+iteration runs as these calls and the same sequence (with the Adam step
+counter on the device) is captured into one CUDA graph, which every later
+iteration replays with a single launch; errors of the captured launches are
+checked with ``rt_batch_status`` at the end.  Serial runs the same steps
 scene by scene with the single-scene calls.  The reference has no inverse
 rendering; this is the differentiable extension built on its scene recipe
 (rtow.cxx:51-80 with the counter RNG).
@@ -109,6 +113,41 @@ class InverseProblem:
         R.adam_step(_p(self.theta), _p(self.galb), _p(self.m), _p(self.v), self.theta.numel(), self.step, lr=lr,
                     stream=s)
 
+    def _iteration_device(self, s, lr):
+        """The batched iteration with the Adam step counter on the device (capturable)."""
+        self.batch.set_albedos(_p(self.theta), s)
+        self.batch.launch(s, stats=False)
+        self.loss.zero_()
+        R.l2_loss_grad(_p(self.image), _p(self.target), _p(self.gimg), int(self.poff[-1]), _p(self.loss), s)
+        self.batch.adjoint(s)
+        R.adam_step_device(_p(self.theta), _p(self.galb), _p(self.m), _p(self.v), self.theta.numel(),
+                           _p(self.step_dev), lr=lr, stream=s)
+
+    def make_graph(self, lr=1e-2):
+        """Runs one batched iteration with the calls themselves (it sizes the
+        batch's buffers and uploads its tables), then captures the same
+        iteration into one CUDA graph; iterate_graph replays it."""
+        torch = self.torch
+        if self.batch is None:
+            self.make_batch()
+        self.step_dev = torch.tensor([self.step], dtype=torch.int32, device="cuda")
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            self._iteration_device(ctypes.c_void_p(side.cuda_stream), lr)
+        torch.cuda.current_stream().wait_stream(side)
+        torch.cuda.synchronize()
+        self.step += 1
+        self.batch.status()
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self._iteration_device(ctypes.c_void_p(torch.cuda.current_stream().cuda_stream), lr)
+
+    def iterate_graph(self):
+        """One batched iteration: one replay of the captured graph."""
+        self.graph.replay()
+        self.step += 1
+
     def iterate_serial(self, lr=1e-2):
         """The same iteration scene by scene (single-scene launches)."""
         self.step += 1
@@ -135,16 +174,25 @@ class InverseProblem:
         return float(np.abs(th - tr)[self.mask].mean())
 
 
-def run(torch, specs, iters, batched=True, lr=1e-2, stream=None):
-    """Optimises from albedo 0.5; returns (initial error, final error, final loss, seconds)."""
+def run(torch, specs, iters, batched=True, lr=1e-2, stream=None, graph=False):
+    """Optimises from albedo 0.5; returns (initial error, final error, final loss, seconds).
+    graph=True (batched only): the first iteration runs as calls and is
+    captured, the others replay the captured graph; the capture is timed."""
     prob = InverseProblem(torch, specs, stream=stream)
     if batched:
         prob.make_batch()
     e0 = prob.albedo_error()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(iters):
-        (prob.iterate_batched if batched else prob.iterate_serial)(lr)
+    if batched and graph:
+        prob.make_graph(lr)
+        for _ in range(iters - 1):
+            prob.iterate_graph()
+        torch.cuda.synchronize()
+        prob.batch.status()
+    else:
+        for _ in range(iters):
+            (prob.iterate_batched if batched else prob.iterate_serial)(lr)
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
     return e0, prob.albedo_error(), float(prob.loss.item()), dt

@@ -95,3 +95,54 @@ def test_batched_inverse_rendering_recovers_albedos(product, cuda):
     print("inverse: loss after 10 / 60 iterations", l10, pb.loss.item(), "albedo error", e0, pb.albedo_error())
     assert pb.loss.item() < 0.7 * l10
     assert pb.albedo_error() < e0 - 0.02
+
+
+def test_adam_step_device_counter(product, cuda):
+    """rt_adam_step_device takes step *step + 1 and advances the counter; the
+    same update as rt_adam_step within an ulp of the bias corrections."""
+    R, torch = product, cuda
+    rng = np.random.default_rng(2)
+    n = 777
+    theta = rng.uniform(0, 1, n).astype(np.float32)
+    g = rng.normal(0, 1, n)
+    a = [torch.from_numpy(x.copy()).cuda() for x in (theta, np.zeros(n, np.float32), np.zeros(n, np.float32))]
+    b = [torch.from_numpy(x.copy()).cuda() for x in (theta, np.zeros(n, np.float32), np.zeros(n, np.float32))]
+    dg = torch.from_numpy(g).cuda()
+    step = torch.zeros(1, dtype=torch.int32, device="cuda")
+    for k in range(1, 4):
+        R.adam_step(dptr(a[0]), dptr(dg), dptr(a[1]), dptr(a[2]), n, k)
+        R.adam_step_device(dptr(b[0]), dptr(dg), dptr(b[1]), dptr(b[2]), n, dptr(step))
+    torch.cuda.synchronize()
+    assert int(step.item()) == 3
+    assert torch.allclose(a[0], b[0], rtol=1e-6, atol=1e-7)
+
+
+def test_inverse_iteration_as_one_captured_graph(product, cuda):
+    """The batched iteration captured into one CUDA graph (wave loop as a
+    conditional node, Adam's step counter on the device) follows the
+    call-by-call iteration; the batch reports no error of the captured
+    launches; a call that cannot be captured is refused cleanly."""
+    R, torch = product, cuda
+    from rtxplay_gb300 import inverse
+    specs = inverse.inverse_specs(3, seed=5, level=2, size=48, spp=4, depth=8)
+    pc = inverse.InverseProblem(torch, specs)
+    pg = inverse.InverseProblem(torch, specs)
+    for _ in range(6):
+        pc.iterate_batched()
+    pg.make_graph()          # iteration 1 as calls, then the capture
+    for _ in range(5):
+        pg.iterate_graph()   # iterations 2..6, one graph launch each
+    torch.cuda.synchronize()
+    pg.batch.status()
+    assert pg.step == pc.step == 6 and int(pg.step_dev.item()) == 6
+    # the same renders and adjoints; Adam's bias corrections come from pow on the
+    # device against the host's, which may differ in the last bit
+    assert torch.allclose(pg.theta, pc.theta, rtol=1e-5, atol=1e-6)
+    assert abs(pg.loss.item() - pc.loss.item()) <= 1e-5 * pc.loss.item()
+    # stats cannot come out of a capture: refused before anything is enqueued
+    g = torch.cuda.CUDAGraph()
+    with pytest.raises(R.RTError) as e:
+        with torch.cuda.graph(g):
+            pg.batch.launch(ctypes.c_void_p(torch.cuda.current_stream().cuda_stream), stats=True)
+    assert e.value.status == R.RT_ERR_INVALID_ARG
+    pg.batch.status()
