@@ -8,17 +8,18 @@
 //
 // Design: a render is a list of jobs (a scene segment of a geometry, its
 // camera, parameters and output frame); a single-scene launch is a list of
-// one.  Paths are numbered globally (job after job, sample-major inside a
+// one.  Paths are numbered globally (job after job, pixel-major inside a
 // job).  A wave queue of W rays (SoA float4 arrays) is traversed by `extend`
 // (closest hit over the job's LBVH) and resolved by `shade` (miss/sky, depth
 // limit, Lambertian / metal / dielectric scatter).  A path that ends adds its
 // colour and ray count to its pixel in 64-bit fixed point (integer atomics,
-// so the sums do not depend on the order in which paths finish) and its
-// thread starts the next camera path (one atomic per warp); continuing and new
-// rays are appended to the next queue with a warp ballot and one atomic per
-// warp.  A one-thread `ctrl` kernel flips the queues and decides whether
-// another wave runs; the wave loop runs either from the host (a status read
-// every 8 waves) or inside a CUDA graph as a conditional WHILE node.
+// so the sums do not depend on the order in which paths finish); continuing
+// rays are appended to the front of the next queue (a warp ballot, one atomic
+// per block), and `fill` starts the next paths in path order in the free slots
+// behind them.  A one-thread `ctrl` kernel advances the path counter, flips
+// the queues and decides whether another wave runs; the wave loop runs either
+// from the host (a status read every 8 waves) or inside a CUDA graph as a
+// conditional WHILE node.
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
@@ -194,6 +195,47 @@ __global__ void __launch_bounds__(kThreads) k_generate(const JobDev* __restrict_
     }
 }
 
+// Fresh paths of the next wave: the queue's free slots behind the continuing
+// rays (slots [front, cap)) take the next paths in path order, as many as
+// remain.  Path order is pixel-major, so consecutive claims of the next
+// traversal are samples of one pixel.  A fixed grid (a graph node needs a
+// fixed shape) of a few blocks per SM strides over the fresh paths, so a wave
+// that needs few pays for few; k_wave_ctrl then advances next_path by the
+// same count.  Moving the start of new paths here from the shading kernel
+// took the path counter's block-wide aggregation, the camera-ray work and most
+// of its register spills out of it (shading 100.4 -> 78.3 ms per C1 frame).
+__device__ __forceinline__ uint32_t fresh_count(const WaveState* st, uint32_t nxt) {
+    const unsigned long long rem = st->total_paths - st->next_path;
+    const uint32_t room = st->cap - st->front[nxt];
+    return rem < room ? uint32_t(rem) : room;
+}
+
+__global__ void __launch_bounds__(kThreads) k_fill(const JobDev* __restrict__ jobs, uint32_t nj, Queues qs,
+                                                   const WaveState* st, int any_guides) {
+    const uint32_t nxt = (*((volatile const uint32_t*)&st->cur)) ^ 1u;
+    const uint32_t n = fresh_count(st, nxt);
+    const unsigned long long base = st->next_path;
+    const uint32_t cap = st->cap;
+    const Queue Q = nxt ? qs.q[1] : qs.q[0];
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const unsigned long long g = base + t;
+        const uint32_t jx = job_of_path(jobs, nj, g);
+        const JobDev& j = jobs[jx];
+        const uint32_t pid = uint32_t(g - j.path_offset);
+        const uint32_t pixel = pid / j.spp, sample = j.first_sample + pid % j.spp;
+        float3 o, d;
+        make_camera_ray(j, pixel, sample, o, d);
+        const uint32_t slot = cap - n + t;
+        Q.ori[slot] = make_float4(o.x, o.y, o.z, __uint_as_float(pixel));
+        Q.dir[slot] = make_float4(d.x, d.y, d.z, __uint_as_float(jx << 8));
+        Q.thr[slot] = make_float4(1.f, 1.f, 1.f, __uint_as_float(sample));
+        if (any_guides) {
+            Q.gn[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
+            Q.ga[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    }
+}
+
 // Refill rule of the persistent traversal (rt_tuning: refill_below,
 // steps_per_check); the counting pass takes it too, unused, so both kernels
 // share one signature.
@@ -328,15 +370,17 @@ __device__ __forceinline__ unsigned long long fx_q(float x) {
     return (unsigned long long)__float2ll_rn(x * 4294967296.0f);
 }
 
-// Four resident blocks per SM (64 registers): more warps in flight for the
-// latency-bound gathers.  Measured without gain on C1 (64 spp, within 0.3 %):
-// one block-wide aggregation round for the three counters instead of two
-// (2 barriers instead of 5), and the hit's thing id written by k_extend so its
-// optics load beside the primitive record (k_extend then needs 51 registers,
-// 4 % slower overall unless held to 48).
-// kB threads per block (rt_tuning: shade_block), held to 64 registers.  (Three
-// 512-thread blocks per SM at 40 registers, with 408 B of spills, measured
-// slower on the full C1 frame: 103.3 against 100.5 ms of shading per frame.)
+// kB threads per block (rt_tuning: shade_block), held to 64 registers, so two
+// 512-thread blocks per SM.  One block-wide aggregation round (two barriers)
+// for the continuing rays' queue offsets.  Measured without gain on C1 (64
+// spp, within 0.3 %) when the kernel also started the fresh paths: one
+// aggregation round for its three counters instead of two, and the hit's
+// thing id written by k_extend so its optics load beside the primitive record
+// (k_extend then needs 51 registers, 4 % slower overall unless held to 48);
+// three 512-thread blocks per SM at 40 registers, with 408 B of spills, were
+// slower on the full C1 frame (103.3 against 100.5 ms of shading per frame);
+// without the fresh paths (40 registers, 256 B of spills) the same as two
+// blocks (78.2 against 78.8 ms), 256-thread blocks 80.3 ms.
 template <int kB>
 __global__ void __launch_bounds__(kB, 1024 / kB)
     k_shade(Queues qs, const float4* __restrict__ hits, const uint32_t* __restrict__ hthing, WaveState* st,
@@ -345,8 +389,8 @@ __global__ void __launch_bounds__(kB, 1024 / kB)
             uint2 lim) {
     // per-warp counts, turned into block-exclusive offsets by thread 0, and the
     // block's bases from one global atomic per block (not one per warp)
-    __shared__ uint32_t s_warp[kB / 32], s_warp2[kB / 32];
-    __shared__ unsigned long long s_base, s_base2;
+    __shared__ uint32_t s_warp[kB / 32];
+    __shared__ unsigned long long s_base;
     const uint32_t cur = *((volatile uint32_t*)&st->cur);
     const uint32_t n = *((volatile uint32_t*)&st->count[cur]);
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -450,74 +494,30 @@ __global__ void __launch_bounds__(kB, 1024 / kB)
             }
         }
     }
-    // regenerate: every ended path is replaced by the next camera path
-    const uint32_t want = __ballot_sync(0xFFFFFFFFu, ended);
-    if (lane == 0) s_warp[warp] = __popc(want);
+    // continuing rays fill the next queue from the front (one atomic per
+    // block); the fresh paths follow behind them (k_fill)
+    if (cont) bounce += 1;
+    const uint32_t pc = __ballot_sync(0xFFFFFFFFu, cont);
+    if (lane == 0) s_warp[warp] = __popc(pc);
     __syncthreads();
     if (threadIdx.x == 0) {
-        uint32_t tot = 0;
+        uint32_t tc = 0;
         for (uint32_t w = 0; w < kB / 32; ++w) {
             const uint32_t c = s_warp[w];
-            s_warp[w] = tot;
-            tot += c;
-        }
-        s_base = tot ? atomicAdd(&st->next_path, (unsigned long long)tot) : 0ull;
-    }
-    __syncthreads();
-    bool fresh = false;
-    if (want) {
-        if (ended) {
-            const unsigned long long g = s_base + s_warp[warp] + __popc(want & ((1u << lane) - 1u));
-            if (g < st->total_paths) {
-                jx = job_of_path(jobs, nj, g);
-                const JobDev& j = jobs[jx];
-                const uint32_t pid = uint32_t(g - j.path_offset);
-                pixel = pid / j.spp;
-                sample = j.first_sample + pid % j.spp;
-                make_camera_ray(j, pixel, sample, no, nd);
-                nthr = mk(1.f, 1.f, 1.f);
-                gN = mk(0.f, 0.f, 0.f);
-                gA = mk(0.f, 0.f, 0.f);
-                bounce = 0;
-                fresh = true;
-            }
-        }
-    }
-    if (cont) bounce += 1;
-    const bool push = cont || fresh;
-    // continuing rays fill the next queue from the front, fresh rays from the back
-    const uint32_t pc = __ballot_sync(0xFFFFFFFFu, cont), pf = __ballot_sync(0xFFFFFFFFu, fresh);
-    __syncthreads();   // every warp has read its regeneration offset
-    if (lane == 0) {
-        s_warp[warp] = __popc(pc);
-        s_warp2[warp] = __popc(pf);
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t tc = 0, tf = 0;
-        for (uint32_t w = 0; w < kB / 32; ++w) {
-            const uint32_t c = s_warp[w], f = s_warp2[w];
             s_warp[w] = tc;
-            s_warp2[w] = tf;
             tc += c;
-            tf += f;
         }
         s_base = tc ? (unsigned long long)atomicAdd(&st->front[cur ^ 1], tc) : 0ull;
-        s_base2 = tf ? (unsigned long long)atomicAdd(&st->back[cur ^ 1], tf) : 0ull;
     }
     __syncthreads();
-    if (pc | pf) {
-        if (push) {
-            const uint32_t lt = (1u << lane) - 1u;
-            const uint32_t slot = cont ? uint32_t(s_base) + s_warp[warp] + __popc(pc & lt)
-                                       : st->cap - 1u - (uint32_t(s_base2) + s_warp2[warp] + __popc(pf & lt));
-            N.ori[slot] = make_float4(no.x, no.y, no.z, __uint_as_float(pixel));
-            N.dir[slot] = make_float4(nd.x, nd.y, nd.z, __uint_as_float((jx << 8) | bounce));
-            N.thr[slot] = make_float4(nthr.x, nthr.y, nthr.z, __uint_as_float(sample));
-            if (any_guides) {
-                N.gn[slot] = make_float4(gN.x, gN.y, gN.z, 0.f);
-                N.ga[slot] = make_float4(gA.x, gA.y, gA.z, 0.f);
-            }
+    if (cont) {
+        const uint32_t slot = uint32_t(s_base) + s_warp[warp] + __popc(pc & ((1u << lane) - 1u));
+        N.ori[slot] = make_float4(no.x, no.y, no.z, __uint_as_float(pixel));
+        N.dir[slot] = make_float4(nd.x, nd.y, nd.z, __uint_as_float((jx << 8) | bounce));
+        N.thr[slot] = make_float4(nthr.x, nthr.y, nthr.z, __uint_as_float(sample));
+        if (any_guides) {
+            N.gn[slot] = make_float4(gN.x, gN.y, gN.z, 0.f);
+            N.ga[slot] = make_float4(gA.x, gA.y, gA.z, 0.f);
         }
     }
 }
@@ -529,6 +529,9 @@ __global__ void k_wave_ctrl(WaveState* st, cudaGraphConditionalHandle handle, in
     const uint32_t cur = st->cur;
     if (st->count[cur] != 0) st->iter += 1;   // a wave ran (the host loop may run empty ones)
     const uint32_t next = cur ^ 1u;
+    const uint32_t nf = fresh_count(st, next);   // the paths k_fill started behind the continuing rays
+    st->next_path += nf;
+    st->back[next] = nf;
     st->cur = next;
     st->count[next] = st->front[next] + st->back[next];
     st->ext_next[next] = 0;
@@ -788,6 +791,7 @@ struct WaveLaunch {
     ExtendFn ext_fn;
     unsigned egrid;    // extend grid (persistent: fills the GPU once)
     unsigned qgrid;    // one thread per wave slot, kThreads per block
+    unsigned fgrid;    // k_fill: a few blocks per SM striding over the fresh paths
     ShadeFn shade;
     unsigned sgrid;    // shading grid, sblock threads per block
     int sblock;
@@ -852,13 +856,21 @@ cudaGraphNode_t add_wave_loop(cudaGraph_t graph, const cudaGraphNode_t* deps, si
     kp.blockDim = dim3(unsigned(l.sblock));
     kp.kernelParams = shade_args;
     RT_CUDA(cudaGraphAddKernelNode(&n_shade, body, &n_ext, 1, &kp));
+    cudaGraphNode_t n_fill;
+    const WaveState* st_c = l.st;
+    void* fill_args[] = {&l.jobs, &l.nj, &l.qs, &st_c, &l.any_guides};
+    kp.func = reinterpret_cast<void*>(k_fill);
+    kp.gridDim = dim3(l.fgrid);
+    kp.blockDim = dim3(kThreads);
+    kp.kernelParams = fill_args;
+    RT_CUDA(cudaGraphAddKernelNode(&n_fill, body, &n_shade, 1, &kp));
     int in_graph = 1;
     void* ctrl_args[] = {&l.st, &handle, &in_graph};
     kp.func = reinterpret_cast<void*>(k_wave_ctrl);
     kp.gridDim = dim3(1);
     kp.blockDim = dim3(1);
     kp.kernelParams = ctrl_args;
-    RT_CUDA(cudaGraphAddKernelNode(&n_ctrl, body, &n_shade, 1, &kp));
+    RT_CUDA(cudaGraphAddKernelNode(&n_ctrl, body, &n_fill, 1, &kp));
     return cnode;
 }
 
@@ -1002,6 +1014,7 @@ void render_jobs_ws(const Geometry& g, const std::vector<Job>& jobs, cudaStream_
     L.ext_fn = g.ninstances ? (count ? k_extend<true, true> : k_extend_p<true>)
                             : (count ? k_extend<true, false> : k_extend_p<false>);
     L.qgrid = grid_for(W);
+    L.fgrid = std::min(L.qgrid, unsigned(8 * sm_count()));
     L.egrid = count ? L.qgrid : persistent_grid(L.ext_fn, shape.ext_bpsm);
     L.sblock = shape.shade_block;
     L.shade = shade_fn(L.sblock);
@@ -1099,9 +1112,11 @@ void render_jobs_ws(const Geometry& g, const std::vector<Job>& jobs, cudaStream_
                                              dim3(unsigned(L.sblock)), shade_args, 0, s));
                 }
                 if (stage_timing) RT_CUDA(cudaEventRecord(ws.event(ev - 1), s));
+                k_fill<<<L.fgrid, kThreads, 0, s>>>(L.jobs, nj, L.qs, L.st, L.any_guides);
+                RT_CHECK_LAUNCH();
                 k_wave_ctrl<<<1, 1, 0, s>>>(L.st, no_handle, 0);
                 RT_CHECK_LAUNCH();
-                launches += 3;
+                launches += 4;
             }
             RT_CUDA(cudaMemcpyAsync(ws.host_state, L.st, sizeof(WaveState), cudaMemcpyDeviceToHost, s));
             RT_CUDA(cudaStreamSynchronize(s));
@@ -1127,7 +1142,7 @@ void render_jobs_ws(const Geometry& g, const std::vector<Job>& jobs, cudaStream_
         accum->rays = hs.rays;
         accum->samples += jobs[0].params.spp;
     }
-    if (use_graph) launches += 3 * hs.iter;
+    if (use_graph) launches += 4 * hs.iter;
     if (stats) {
         std::memset(stats, 0, sizeof(*stats));
         stats->rays = launch_rays;
