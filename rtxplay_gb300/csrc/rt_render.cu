@@ -371,7 +371,9 @@ __device__ __forceinline__ unsigned long long fx_q(float x) {
 }
 
 // kB threads per block (rt_tuning: shade_block), held to 64 registers, so two
-// 512-thread blocks per SM.  One block-wide aggregation round (two barriers)
+// 512-thread blocks per SM; the grid is the resident blocks, each walking the
+// wave in tiles of kB rays (one block per tile measured slower: 78.2 against
+// 69.5 ms of shading per C1 frame, the empty blocks of short waves included).  One block-wide aggregation round (two barriers)
 // for the continuing rays' queue offsets.  Measured without gain on C1 (64
 // spp, within 0.3 %) when the kernel also started the fresh paths: one
 // aggregation round for its three counters instead of two, and the hit's
@@ -388,136 +390,145 @@ __global__ void __launch_bounds__(kB, 1024 / kB)
             const FlatDesc* __restrict__ desc, const ThingDev* __restrict__ things, Acc acc, int any_guides,
             uint2 lim) {
     // per-warp counts, turned into block-exclusive offsets by thread 0, and the
-    // block's bases from one global atomic per block (not one per warp)
-    __shared__ uint32_t s_warp[kB / 32];
-    __shared__ unsigned long long s_base;
+    // block's base from one global atomic per block (not one per warp); two
+    // buffers by tile parity, so that a tile's counts are written while slower
+    // warps may still read the previous tile's offsets
+    __shared__ uint32_t s_warp_buf[2][kB / 32];
+    __shared__ unsigned long long s_base_buf[2];
     const uint32_t cur = *((volatile uint32_t*)&st->cur);
     const uint32_t n = *((volatile uint32_t*)&st->count[cur]);
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
-    if (blockIdx.x * blockDim.x >= n) return;   // whole block past the queue end
-    const bool active = i < n;
     const Queue Q = pick(qs, cur), N = pick(qs, cur ^ 1);
+    // a grid of resident blocks walks the wave in tiles of kB rays (the loop
+    // condition is the same for the whole block, so every thread of the block
+    // meets the barriers inside)
+    uint32_t parity = 0;
+    for (uint32_t tile = blockIdx.x; tile * kB < n; tile += gridDim.x, parity ^= 1u) {
+        uint32_t* s_warp = s_warp_buf[parity];
+        unsigned long long& s_base = s_base_buf[parity];
+        const uint32_t i = tile * kB + threadIdx.x;
+        const bool active = i < n;
 
-    bool cont = false, ended = false;
-    unsigned long long a_px = ~0ull, a_r = 0, a_g = 0, a_b = 0, a_n = 0;
-    float3 no{}, nd{}, nthr{};
-    float3 gN{}, gA{};
-    uint32_t pixel = 0, sample = 0, bounce = 0, jx = 0;
-    if (active) {
-        const uint32_t q = wave_slot(st, cur, i);
-        const float4 o4 = Q.ori[q], d4 = Q.dir[q], t4 = Q.thr[q], h4 = hits[i];
-        pixel = __float_as_uint(o4.w);
-        sample = __float_as_uint(t4.w);
-        const uint32_t tag = __float_as_uint(d4.w);
-        jx = tag >> 8;
-        bounce = tag & 0xFFu;
-        const JobDev& j = jobs[jx];
-        const float3 o = xyz(o4), d = xyz(d4);
-        float3 thr = xyz(t4);
-        if (any_guides) {
-            gN = xyz(Q.gn[q]);
-            gA = xyz(Q.ga[q]);
-        }
-        const int ref = __float_as_int(h4.w);
-        float3 color = mk(0.f, 0.f, 0.f);
-        if (ref == -1) {
-            color = mulv(thr, sky(d, j.ambient, j.white));
-            ended = true;
-        } else if (bounce + 1 >= j.depth) {
-            ended = true;   // black at the depth limit (optx/optics_r.cu:34-42)
-        } else {
-            Stream s(j.seed, j.key1, pixel, sample, bounce + 1);
-            float4 pa, pb, pc;
-            bool ok = ref >= 0 ? rt_in_bounds(uint32_t(ref) < lim.x, &st->err)
-                               : rt_in_bounds(hthing[i] < lim.y, &st->err);
-            if (ok) {
-                if (ref >= 0) {   // the world-space record itself
-                    pa = __ldg(tprims + 3 * ref);
-                    pb = __ldg(tprims + 3 * ref + 1);
-                    pc = __ldg(tprims + 3 * ref + 2);
-                } else {          // an instanced triangle, rebuilt exactly as the flat layout stores it
-                    world_prim(desc, hthing[i], uint32_t(-2 - ref), pa, pb, pc);
-                }
-                ok = rt_in_bounds(__float_as_uint(pa.w) < lim.y, &st->err);
+        bool cont = false, ended = false;
+        unsigned long long a_px = ~0ull, a_r = 0, a_g = 0, a_b = 0, a_n = 0;
+        float3 no{}, nd{}, nthr{};
+        float3 gN{}, gA{};
+        uint32_t pixel = 0, sample = 0, bounce = 0, jx = 0;
+        if (active) {
+            const uint32_t q = wave_slot(st, cur, i);
+            const float4 o4 = Q.ori[q], d4 = Q.dir[q], t4 = Q.thr[q], h4 = hits[i];
+            pixel = __float_as_uint(o4.w);
+            sample = __float_as_uint(t4.w);
+            const uint32_t tag = __float_as_uint(d4.w);
+            jx = tag >> 8;
+            bounce = tag & 0xFFu;
+            const JobDev& j = jobs[jx];
+            const float3 o = xyz(o4), d = xyz(d4);
+            float3 thr = xyz(t4);
+            if (any_guides) {
+                gN = xyz(Q.gn[q]);
+                gA = xyz(Q.ga[q]);
             }
-            const ScatterOut so = ok ? scatter(pa, pb, pc, things, o, d, h4, s) : ScatterOut{};
-            if (so.guide) {
-                if (isnull(gN)) gN = so.N;
-                if (isnull(gA)) gA = so.albedo;
-            }
-            if (so.cont) {
-                thr = mulv(thr, so.albedo);   // glass: albedo (1,1,1), an exact no-op
-                no = so.p; nd = so.dir; nthr = thr; cont = true;
+            const int ref = __float_as_int(h4.w);
+            float3 color = mk(0.f, 0.f, 0.f);
+            if (ref == -1) {
+                color = mulv(thr, sky(d, j.ambient, j.white));
+                ended = true;
+            } else if (bounce + 1 >= j.depth) {
+                ended = true;   // black at the depth limit (optx/optics_r.cu:34-42)
             } else {
-                ended = true;   // absorbed: black
+                Stream s(j.seed, j.key1, pixel, sample, bounce + 1);
+                float4 pa, pb, pc;
+                bool ok = ref >= 0 ? rt_in_bounds(uint32_t(ref) < lim.x, &st->err)
+                                   : rt_in_bounds(hthing[i] < lim.y, &st->err);
+                if (ok) {
+                    if (ref >= 0) {   // the world-space record itself
+                        pa = __ldg(tprims + 3 * ref);
+                        pb = __ldg(tprims + 3 * ref + 1);
+                        pc = __ldg(tprims + 3 * ref + 2);
+                    } else {          // an instanced triangle, rebuilt exactly as the flat layout stores it
+                        world_prim(desc, hthing[i], uint32_t(-2 - ref), pa, pb, pc);
+                    }
+                    ok = rt_in_bounds(__float_as_uint(pa.w) < lim.y, &st->err);
+                }
+                const ScatterOut so = ok ? scatter(pa, pb, pc, things, o, d, h4, s) : ScatterOut{};
+                if (so.guide) {
+                    if (isnull(gN)) gN = so.N;
+                    if (isnull(gA)) gA = so.albedo;
+                }
+                if (so.cont) {
+                    thr = mulv(thr, so.albedo);   // glass: albedo (1,1,1), an exact no-op
+                    no = so.p; nd = so.dir; nthr = thr; cont = true;
+                } else {
+                    ended = true;   // absorbed: black
+                }
             }
-        }
-        if (ended) {
-            const size_t px = size_t(j.pix_offset) + pixel;
-            a_px = px;
-            a_r = fx_q(color.x);
-            a_g = fx_q(color.y);
-            a_b = fx_q(color.z);
-            a_n = bounce + 1;
-            if (j.guides) {
-                const float gv[6] = {gN.x, gN.y, gN.z, gA.x, gA.y, gA.z};
-#pragma unroll
-                for (int k = 0; k < 6; ++k) {
-                    const unsigned long long q = fx_q(gv[k]);
-                    if (q) atomicAdd(acc.gd[k] + px, q);
+            if (ended) {
+                const size_t px = size_t(j.pix_offset) + pixel;
+                a_px = px;
+                a_r = fx_q(color.x);
+                a_g = fx_q(color.y);
+                a_b = fx_q(color.z);
+                a_n = bounce + 1;
+                if (j.guides) {
+                    const float gv[6] = {gN.x, gN.y, gN.z, gA.x, gA.y, gA.z};
+    #pragma unroll
+                    for (int k = 0; k < 6; ++k) {
+                        const unsigned long long q = fx_q(gv[k]);
+                        if (q) atomicAdd(acc.gd[k] + px, q);
+                    }
                 }
             }
         }
-    }
 
-    {   // pixel sums: one atomic per sum when every ended lane of the warp shares the pixel
-        // (common with pixel-major path numbers), else one per lane
-        const uint32_t em = __ballot_sync(0xFFFFFFFFu, ended);
-        if (em) {
-            const uint32_t grp = __match_any_sync(0xFFFFFFFFu, a_px);
-            const uint32_t leader = __ffs(em) - 1;
-            const bool uni = __shfl_sync(0xFFFFFFFFu, (grp & em) == em ? 1 : 0, leader) != 0;
-            if (uni) {
-                for (int o = 16; o > 0; o >>= 1) {
-                    a_r += __shfl_xor_sync(0xFFFFFFFFu, a_r, o);
-                    a_g += __shfl_xor_sync(0xFFFFFFFFu, a_g, o);
-                    a_b += __shfl_xor_sync(0xFFFFFFFFu, a_b, o);
-                    a_n += __shfl_xor_sync(0xFFFFFFFFu, a_n, o);
+        {   // pixel sums: one atomic per sum when every ended lane of the warp shares the pixel
+            // (common with pixel-major path numbers), else one per lane
+            const uint32_t em = __ballot_sync(0xFFFFFFFFu, ended);
+            if (em) {
+                const uint32_t grp = __match_any_sync(0xFFFFFFFFu, a_px);
+                const uint32_t leader = __ffs(em) - 1;
+                const bool uni = __shfl_sync(0xFFFFFFFFu, (grp & em) == em ? 1 : 0, leader) != 0;
+                if (uni) {
+                    for (int o = 16; o > 0; o >>= 1) {
+                        a_r += __shfl_xor_sync(0xFFFFFFFFu, a_r, o);
+                        a_g += __shfl_xor_sync(0xFFFFFFFFu, a_g, o);
+                        a_b += __shfl_xor_sync(0xFFFFFFFFu, a_b, o);
+                        a_n += __shfl_xor_sync(0xFFFFFFFFu, a_n, o);
+                    }
+                }
+                if (ended && (!uni || lane == leader)) {
+                    if (a_r) atomicAdd(acc.col[0] + a_px, a_r);
+                    if (a_g) atomicAdd(acc.col[1] + a_px, a_g);
+                    if (a_b) atomicAdd(acc.col[2] + a_px, a_b);
+                    atomicAdd(acc.rays + a_px, uint32_t(a_n));
                 }
             }
-            if (ended && (!uni || lane == leader)) {
-                if (a_r) atomicAdd(acc.col[0] + a_px, a_r);
-                if (a_g) atomicAdd(acc.col[1] + a_px, a_g);
-                if (a_b) atomicAdd(acc.col[2] + a_px, a_b);
-                atomicAdd(acc.rays + a_px, uint32_t(a_n));
+        }
+        // continuing rays fill the next queue from the front (one atomic per
+        // block); the fresh paths follow behind them (k_fill)
+        if (cont) bounce += 1;
+        const uint32_t pc = __ballot_sync(0xFFFFFFFFu, cont);
+        if (lane == 0) s_warp[warp] = __popc(pc);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t tc = 0;
+            for (uint32_t w = 0; w < kB / 32; ++w) {
+                const uint32_t c = s_warp[w];
+                s_warp[w] = tc;
+                tc += c;
             }
+            s_base = tc ? (unsigned long long)atomicAdd(&st->front[cur ^ 1], tc) : 0ull;
         }
-    }
-    // continuing rays fill the next queue from the front (one atomic per
-    // block); the fresh paths follow behind them (k_fill)
-    if (cont) bounce += 1;
-    const uint32_t pc = __ballot_sync(0xFFFFFFFFu, cont);
-    if (lane == 0) s_warp[warp] = __popc(pc);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t tc = 0;
-        for (uint32_t w = 0; w < kB / 32; ++w) {
-            const uint32_t c = s_warp[w];
-            s_warp[w] = tc;
-            tc += c;
-        }
-        s_base = tc ? (unsigned long long)atomicAdd(&st->front[cur ^ 1], tc) : 0ull;
-    }
-    __syncthreads();
-    if (cont) {
-        const uint32_t slot = uint32_t(s_base) + s_warp[warp] + __popc(pc & ((1u << lane) - 1u));
-        N.ori[slot] = make_float4(no.x, no.y, no.z, __uint_as_float(pixel));
-        N.dir[slot] = make_float4(nd.x, nd.y, nd.z, __uint_as_float((jx << 8) | bounce));
-        N.thr[slot] = make_float4(nthr.x, nthr.y, nthr.z, __uint_as_float(sample));
-        if (any_guides) {
-            N.gn[slot] = make_float4(gN.x, gN.y, gN.z, 0.f);
-            N.ga[slot] = make_float4(gA.x, gA.y, gA.z, 0.f);
+        __syncthreads();
+        if (cont) {
+            const uint32_t slot = uint32_t(s_base) + s_warp[warp] + __popc(pc & ((1u << lane) - 1u));
+            N.ori[slot] = make_float4(no.x, no.y, no.z, __uint_as_float(pixel));
+            N.dir[slot] = make_float4(nd.x, nd.y, nd.z, __uint_as_float((jx << 8) | bounce));
+            N.thr[slot] = make_float4(nthr.x, nthr.y, nthr.z, __uint_as_float(sample));
+            if (any_guides) {
+                N.gn[slot] = make_float4(gN.x, gN.y, gN.z, 0.f);
+                N.ga[slot] = make_float4(gA.x, gA.y, gA.z, 0.f);
+            }
         }
     }
 }
@@ -1018,7 +1029,12 @@ void render_jobs_ws(const Geometry& g, const std::vector<Job>& jobs, cudaStream_
     L.egrid = count ? L.qgrid : persistent_grid(L.ext_fn, shape.ext_bpsm);
     L.sblock = shape.shade_block;
     L.shade = shade_fn(L.sblock);
-    L.sgrid = grid_for(W, L.sblock);
+    {   // shading: the resident blocks, walking the wave in tiles
+        int per_sm = 0;
+        RT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, reinterpret_cast<const void*>(L.shade),
+                                                              L.sblock, 0));
+        L.sgrid = std::min(grid_for(W, L.sblock), unsigned(std::max(1, per_sm) * sm_count()));
+    }
     L.tn = shape.ext;
     L.hits = ws.hits.as<float4>();
     L.hthing = ws.hthing.as<uint32_t>();
