@@ -82,3 +82,63 @@ def test_checkpoint_and_resume(product, cuda):
     assert b.samples == 11   # refused calls change nothing
     c.close()
     b.close()
+
+
+def test_sample_range_split_in_one_process(product, cuda):
+    """Samples [0, 4) in one accumulator and [4, 10) in another (first sample
+    set to 4), their exact sums added on the device and resolved: the image
+    and rays per pixel of one 10-sample launch bit for bit."""
+    R, torch = product, cuda
+    sc = R.rtow_scene(2, half_extent=4)
+    w, h, seed = 72, 40, 13
+    cam = R.rtow_camera(w, h)
+    a, b = R.Accum(w, h), R.Accum(w, h)
+    raw, rpp, fr = _frame(R, torch, w, h)
+    sa = a.launch(sc, cam, R.launch_params(w, h, 4, depth=50, seed=seed), fr)
+    b.set_first_sample(4)
+    sb = b.launch(sc, cam, R.launch_params(w, h, 6, depth=50, seed=seed), fr)
+    assert b.samples == 6
+    n = w * h
+
+    class _Dev:
+        def __init__(self, ptr, typestr):
+            self.__cuda_array_interface__ = {"shape": (n,), "typestr": typestr, "data": (ptr, False), "version": 3}
+
+    for pa, pb, ts in zip(a.device_sums(), b.device_sums(), ("<i8", "<i8", "<i8", "<i4")):
+        ta = torch.as_tensor(_Dev(pa, ts), device="cuda")
+        ta += torch.as_tensor(_Dev(pb, ts), device="cuda")
+    a.set_range(0, 10, int(sa.rays) + int(sb.rays))
+    a.resolve(fr)
+    _check(raw, rpp, R.render(sc, cam, R.launch_params(w, h, 10, depth=50, seed=seed)), torch)
+    # the state keeps the range; a resumed accumulator continues at sample 10
+    c = R.Accum(w, h)
+    c.load(a.save())
+    assert c.samples == 10
+    c.launch(sc, cam, R.launch_params(w, h, 2, depth=50, seed=seed), fr)
+    _check(raw, rpp, R.render(sc, cam, R.launch_params(w, h, 12, depth=50, seed=seed)), torch)
+    for x in (a, b, c):
+        x.close()
+
+
+def test_sample_range_api_errors(product, cuda):
+    R, torch = product, cuda
+    sc = R.rtow_scene(1, half_extent=2)
+    w, h = 16, 12
+    cam = R.rtow_camera(w, h)
+    acc = R.Accum(w, h)
+    raw, rpp, fr = _frame(R, torch, w, h)
+    with pytest.raises(R.RTError) as e:   # nothing to resolve yet
+        acc.resolve(fr)
+    assert e.value.status == R.RT_ERR_INVALID_ARG
+    acc.launch(sc, cam, R.launch_params(w, h, 2, depth=8, seed=1), fr)
+    with pytest.raises(R.RTError) as e:   # the first sample of a filled accumulator is fixed
+        acc.set_first_sample(5)
+    assert e.value.status == R.RT_ERR_INVALID_ARG
+    with pytest.raises(R.RTError):
+        acc.set_range(0, 1 << 32, 0)
+    acc.reset()   # clears the first sample too: the next launch renders samples [0, 3)
+    acc.set_first_sample(7)
+    acc.reset()
+    acc.launch(sc, cam, R.launch_params(w, h, 3, depth=8, seed=1), fr)
+    _check(raw, rpp, R.render(sc, cam, R.launch_params(w, h, 3, depth=8, seed=1)), torch)
+    acc.close()

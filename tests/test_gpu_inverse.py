@@ -146,3 +146,37 @@ def test_inverse_iteration_as_one_captured_graph(product, cuda):
             pg.batch.launch(ctypes.c_void_p(torch.cuda.current_stream().cuda_stream), stats=True)
     assert e.value.status == R.RT_ERR_INVALID_ARG
     pg.batch.status()
+
+
+def test_capture_refuses_what_it_cannot_record(product, cuda):
+    """A batch launch inside a capture is refused, before it enqueues anything,
+    when host-side optics changed since the last launch (their upload is a host
+    copy) and when the batch never ran outside a capture; the batch launches
+    normally afterwards and reports no captured error."""
+    R, torch = product, cuda
+    from rtxplay_gb300 import inverse
+    specs = inverse.inverse_specs(2, seed=9, level=1, size=32, spp=2, depth=4)
+    p = inverse.InverseProblem(torch, specs)
+    p.make_batch()
+    side = torch.cuda.Stream()
+
+    def capture_launch():
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=side):
+            p.batch.launch(ctypes.c_void_p(side.cuda_stream), stats=False)
+
+    with pytest.raises(R.RTError) as e:   # no launch outside a capture yet
+        capture_launch()
+    assert e.value.status == R.RT_ERR_INVALID_ARG
+    with torch.cuda.stream(side):
+        p.batch.launch(ctypes.c_void_p(side.cuda_stream))
+    torch.cuda.synchronize()
+    sp = p.true[0]
+    p.scenes[0].set_optics(0, R.optics(int(sp["types"][0]), (0.3, 0.3, 0.3), float(sp["fuzz"][0]),
+                                       float(sp["index"][0])))
+    with pytest.raises(R.RTError) as e:   # host optics changed since the last launch
+        capture_launch()
+    assert e.value.status == R.RT_ERR_INVALID_ARG and b"optics" in R.lib().rt_last_error_string()
+    p.batch.launch()
+    torch.cuda.synchronize()
+    p.batch.status()
