@@ -353,9 +353,12 @@ inline Box unite(const Box& a, const Box& b) {
                mk(fmaxf(a.hi.x, b.hi.x), fmaxf(a.hi.y, b.hi.y), fmaxf(a.hi.z, b.hi.z))};
 }
 
-// Conservative slab test: relative slack 2^-12 so a box that holds the closest
-// primitive is never culled by rounding; the hit set and hence the closest-hit
-// result are those of brute force.
+// Conservative slab test: relative slack 2^-12 so a box is never culled by
+// rounding while a hit inside it is in range.  Ancestor boxes hold a record's
+// own box, so the closest hit is the closest over the records whose own box
+// passes the test, for any hierarchy: brute force for triangles; a binary32
+// sphere root outside the sphere's box (a ray leaving the r = 1000 ground
+// sphere from just inside it) is dropped, as the product drops it.
 constexpr float kSlack = 1.f + 1.f / 4096.f;
 inline bool slab(const Box& b, F3 o, F3 inv, float tmin, float tmax, float& tnear) {
     const float tx0 = (b.lo.x - o.x) * inv.x, tx1 = (b.hi.x - o.x) * inv.x;
