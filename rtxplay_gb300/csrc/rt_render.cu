@@ -346,7 +346,7 @@ __global__ void __launch_bounds__(kThreads, kInst ? 4 : 5)
             continue;
         }
         if (busy) {
-#pragma unroll 1
+#pragma unroll 1   // unrolled twice: 2.6 % slower (C1, 500 spp)
             for (int k = 0; k < tn.steps; ++k) {
                 if (!trav_step<false, kInst>(s, stack, g, nvis, ntest)) {
                     const HitRec& h = s.h;
@@ -1083,7 +1083,8 @@ void render_jobs_ws(const Geometry& g, const std::vector<Job>& jobs, cudaStream_
             reinterpret_cast<const void*>(uintptr_t(L.sgrid)), reinterpret_cast<const void*>(uintptr_t(L.tn.refill_below)),
             reinterpret_cast<const void*>(uintptr_t(L.tn.steps)),
             L.qs.q[0].ori, L.qs.q[0].gn, L.qs.q[1].ori, L.qs.q[1].gn, L.hits, L.hthing, L.st, L.jobs,
-            reinterpret_cast<const void*>(uintptr_t(nj)), L.geo.tnodes, L.geo.tprims, L.geo.bnodes, L.geo.bprims,
+            reinterpret_cast<const void*>(uintptr_t(nj)), L.geo.tnodes, L.geo.tprims, L.geo.tedges, L.geo.bnodes,
+            L.geo.bprims,
             L.geo.inst, L.geo.desc, L.things, L.acc.col[0], L.acc.gd[0], reinterpret_cast<const void*>(uintptr_t(total_pix)),
             reinterpret_cast<const void*>(uintptr_t(any_guides))};
         if (!ws.graph.exec || ws.graph.key != key) {

@@ -402,15 +402,28 @@ __global__ void k_permute(const K* __restrict__ codes_in, const uint32_t* __rest
     ids_out[i] = ids_in[perm[i]];
 }
 
+// Records in leaf order, and their traversal form: a triangle as (A, B - A,
+// C - A), the edges rounded as the triangle test rounds them, other records
+// as they are.
 __global__ void k_gather_prims(const float4* __restrict__ flat, const uint32_t* __restrict__ ids, uint32_t n,
-                               float4* __restrict__ out) {
+                               float4* __restrict__ out, float4* __restrict__ out_e) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float4* s = flat + 3 * size_t(ids[i]);
+    const float4 a = s[0], b = s[1], c = s[2];
     float4* o = out + 3 * size_t(i);
-    o[0] = s[0];
-    o[1] = s[1];
-    o[2] = s[2];
+    o[0] = a;
+    o[1] = b;
+    o[2] = c;
+    float4* e = out_e + 3 * size_t(i);
+    e[0] = a;
+    if (__float_as_uint(c.w) == kPrimTriangle) {
+        e[1] = make_float4(b.x - a.x, b.y - a.y, b.z - a.z, b.w);
+        e[2] = make_float4(c.x - a.x, c.y - a.y, c.z - a.z, c.w);
+    } else {
+        e[1] = b;
+        e[2] = c;
+    }
 }
 
 __device__ __forceinline__ void write_child_box(float4* node, int slot, const Box3& b) {
@@ -670,7 +683,7 @@ void refit(Lbvh& L, cudaStream_t s) {
     const uint32_t n = L.nprims;
     if (n == 0) return;
     k_gather_prims<<<grid_for(n), kThreads, 0, s>>>(L.prims_flat.as<float4>(), L.ids.as<uint32_t>(), n,
-                                                     L.prims.as<float4>());
+                                                     L.prims.as<float4>(), L.prims_e.as<float4>());
     RT_CHECK_LAUNCH();
     int* parents = L.parents.as<int>();
     RT_CUDA(cudaMemsetAsync(L.flags.p, 0, size_t(n) * sizeof(uint32_t), s));
@@ -781,6 +794,7 @@ void build_lbvh(Lbvh& L, int morton_bits, cudaStream_t s, const FlatDesc* desc =
     }
     const uint32_t n = L.nprims;
     L.prims.reserve(std::max<size_t>(1, n) * 48);
+    L.prims_e.reserve(std::max<size_t>(1, n) * 48);
     L.nodes.reserve(std::max<size_t>(1, n) * 64);
     L.parents.reserve((size_t(n) * 2 + 1) * sizeof(int));
     L.flags.reserve(std::max<size_t>(1, n) * sizeof(uint32_t));
@@ -965,7 +979,7 @@ void sync_optics(Geometry& g, const std::vector<Scene*>& scenes, cudaStream_t s)
 }
 
 size_t Lbvh::device_bytes() const {
-    return segs.bytes + prim_seg.bytes + prims_flat.bytes + prims.bytes + nodes.bytes + codes.bytes + ids.bytes +
+    return segs.bytes + prim_seg.bytes + prims_flat.bytes + prims.bytes + prims_e.bytes + nodes.bytes + codes.bytes + ids.bytes +
            parents.bytes + flags.bytes + bounds.bytes + sort_tmp.bytes + seg_tmp.bytes + tbounds.bytes + tcodes.bytes +
            tids.bytes + tsegs.bytes + scene_things.bytes + tseg.bytes + ttmp.bytes;
 }
@@ -978,6 +992,7 @@ GeoView Geometry::view() const {
     GeoView v;
     v.tnodes = top.nodes.as<float4>();
     v.tprims = top.prims.as<float4>();
+    v.tedges = top.prims_e.as<float4>();
     v.bnodes = blas.nodes.as<float4>();
     v.bprims = blas.prims.as<float4>();
     v.inst = inst.as<InstDev>();

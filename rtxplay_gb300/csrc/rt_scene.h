@@ -37,6 +37,7 @@ struct Lbvh {
     DevBuf prim_seg;        // segment of each record (record-id order), n_segs > 1 only
     DevBuf prims_flat;      // 3 float4 per record, record-id order
     DevBuf prims;           // 3 float4 per record, leaf order
+    DevBuf prims_e;         // the same for traversal: triangles as (A, B - A, C - A)
     DevBuf nodes;           // 4 float4 per node slot (one slot per record)
     DevBuf codes;           // sorted Morton codes (u32 or u64)
     DevBuf ids;             // sorted record ids
