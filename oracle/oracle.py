@@ -84,6 +84,8 @@ def lib():
         L.orc_world_nprims.restype = ctypes.c_uint
         L.orc_world_lbvh.argtypes = [ctypes.c_void_p] + [ctypes.c_void_p] * 7
         L.orc_world_triangles.argtypes = [ctypes.c_void_p, _f32p]
+        L.orc_closest.argtypes = [ctypes.c_void_p, ctypes.c_uint, _f32p, _f32p, ctypes.c_int, _i32p, _f32p,
+                                  ctypes.c_int]
         L.orc_first_hit.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Camera), ctypes.c_uint,
                                     ctypes.c_uint, ctypes.c_uint32, ctypes.c_uint32,
                                     ctypes.c_uint32, ctypes.c_int, _i32p, _i32p, _f32p, _f32p,
@@ -267,6 +269,19 @@ class World:
         t = np.zeros((self.nprims, 9), np.float32)
         lib().orc_world_triangles(self._w, t)
         return t
+
+    def closest(self, o, d, mode, nthreads=0):
+        """Closest hits of rays o + t d (n x 3 arrays): mode "brute" (all
+        primitives), "bvh" (the hierarchy) or "boxed" (brute force over the
+        primitives whose own box passes the slab test).  Returns (prim, t),
+        prim -1 on a miss."""
+        o = np.ascontiguousarray(o, np.float32)
+        d = np.ascontiguousarray(d, np.float32)
+        n = len(o)
+        prim = np.zeros(n, np.int32)
+        t = np.zeros(n, np.float32)
+        lib().orc_closest(self._w, n, o, d, {"brute": 0, "bvh": 1, "boxed": 2}[mode], prim, t, nthreads)
+        return prim, t
 
     def first_hit(self, cam, w, h, seed, scene=0, sample=0, use_bvh=True, fp64=False,
                   nthreads=0):

@@ -818,6 +818,25 @@ Hit closest_bvh(const orc_world& w, F3 o, F3 d) {
     return h;
 }
 
+// Brute force over the records whose own box passes the slab test (with the
+// far limit at kTmax): the hit set the hierarchy's rule implies, since every
+// ancestor box holds a record's box.
+Hit closest_brute_boxed(const orc_world& w, F3 o, F3 d) {
+    Hit h;
+    bool have = false;
+    const F3 inv = mk(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
+    for (size_t i = 0; i < w.prims.size(); ++i) {
+        float tn;
+        if (!slab(prim_box(w.prims[i]), o, inv, kTmin, kTmax, tn)) continue;
+        float t, u, v;
+        if (!prim_hit(w.prims[i], o, d, t, u, v) || t > kTmax) continue;
+        if (better(t, w.prims[i].id, h.t, have ? w.prims[h.prim].id : 0, have)) {
+            h.t = t; h.u = u; h.v = v; h.prim = int(i); have = true;
+        }
+    }
+    return h;
+}
+
 inline Hit closest(const orc_world& w, F3 o, F3 d, int use_bvh) {
     return use_bvh ? closest_bvh(w, o, d) : closest_brute(w, o, d);
 }
@@ -1477,6 +1496,23 @@ void orc_first_hit(const orc_world* wd, const orc_camera* cam, unsigned w, unsig
             t[p] = hh.t; u[p] = hh.u; v[p] = hh.v;
             if (t64) t64[p] = t64_of(pr, o, d);
         }
+    }
+}
+
+void orc_closest(const orc_world* wd, unsigned n, const float* o, const float* d, int mode, int32_t* prim,
+                 float* t, int nthreads) {
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+#pragma omp parallel for schedule(dynamic, 256)
+    for (long k = 0; k < long(n); ++k) {
+        const F3 oo = mk(o[3 * k], o[3 * k + 1], o[3 * k + 2]), dd = mk(d[3 * k], d[3 * k + 1], d[3 * k + 2]);
+        const Hit hh = mode == 1 ? closest_bvh(*wd, oo, dd) : mode == 2 ? closest_brute_boxed(*wd, oo, dd)
+                                                            : closest_brute(*wd, oo, dd);
+        prim[k] = hh.prim < 0 ? -1 : int32_t(wd->prims[hh.prim].id);
+        t[k] = hh.prim < 0 ? 0.f : hh.t;
     }
 }
 

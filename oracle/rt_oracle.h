@@ -108,6 +108,12 @@ void orc_first_hit(const orc_world* wd, const orc_camera* cam, unsigned w, unsig
                    uint32_t seed, uint32_t scene, uint32_t sample, int use_bvh, int32_t* prim,
                    int32_t* thing, float* t, float* u, float* v, double* t64, int nthreads);
 
+/* Closest hit of n arbitrary rays (o, d: 3 floats each): mode 0 brute force
+ * over all primitives, 1 the hierarchy, 2 brute force over the primitives
+ * whose own box passes the slab test.  prim = -1 (t = 0) on a miss. */
+void orc_closest(const orc_world* wd, unsigned n, const float* o, const float* d, int mode, int32_t* prim,
+                 float* t, int nthreads);
+
 /* Renders the listed pixels (pixels == NULL: all w*h, in index order).
  * Outputs are indexed by list position.  Returns total rays cast. */
 uint64_t orc_render(const orc_world* wd, const orc_camera* cam, unsigned w, unsigned h,

@@ -746,7 +746,7 @@ ShadeFn shade_fn(int block) {
 }
 
 // The wave loop captured once as a graph: a conditional WHILE node whose body
-// is extend -> shade -> ctrl; rebuilt whenever a baked-in pointer or launch
+// is extend -> shade -> fill -> ctrl; rebuilt whenever a baked-in pointer or launch
 // shape changes.
 struct WaveGraph {
     cudaGraph_t graph = nullptr;
@@ -834,7 +834,7 @@ unsigned persistent_grid(ExtendFn fn, uint32_t bpsm) {
 
 // Adds the wave loop to `graph` after `deps`: a conditional WHILE node (its
 // condition set to 1 at every launch of the graph) whose body is extend ->
-// shade -> ctrl; k_wave_ctrl clears the condition when the loop is done.
+// shade -> fill -> ctrl; k_wave_ctrl clears the condition when the loop is done.
 cudaGraphNode_t add_wave_loop(cudaGraph_t graph, const cudaGraphNode_t* deps, size_t ndeps, const WaveLaunch& L) {
     cudaGraphConditionalHandle handle;
     RT_CUDA(cudaGraphConditionalHandleCreate(&handle, graph, 1u, cudaGraphCondAssignDefault));
