@@ -191,7 +191,7 @@ def cpu_oracle_run(args, target_s, threads=None):
     r = world.render(cam, args.width, args.height, args.spp, args.depth, 4711, pixels=pix, guides=False,
                      nthreads=threads)
     dt = time.perf_counter() - t0
-    return {"value": r["rays"] / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+    return {"value": r["rays"] / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port", "nprims": world.nprims,
             "sample": f"{len(pix)} of {npix} pixels (stride {stride}) x {args.spp} spp, depth {args.depth}, "
                       f"{r['rays']} rays in {dt:.2f} s; LBVH build excluded",
             "note": "the unmodified rtow.cxx is not timed here: the reference checkout it is compiled from "
@@ -217,8 +217,9 @@ def run_reference(args, world, rank):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall * 1e3 / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (reference scene recipe, glibc rand seed 1)",
-            "config": {"workload": "rtow final scene, level-6 tessellation (7,979,008 triangles), "
-                                   f"{args.width}x{args.height}, {args.spp} spp, depth {args.depth}",
+            "config": {"workload": f"rtow final scene, level-{args.level} tessellation "
+                                   f"({samples[-1]['nprims']} triangles), {args.width}x{args.height}, "
+                                   f"{args.spp} spp, depth {args.depth}",
                        "implementation": "CPU oracle port of rtow/rtwo on all host cores"},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": samples[-1]["cores"], "kind": "port",
                              "sample": samples[-1]["sample"]},
@@ -626,6 +627,7 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_oracle_run(args, args.cpu_seconds)
+        cpu.pop("nprims")
 
     peak, peak_src = load_peaks()
     l2_peak = l2_copy_gbs(R, sptr)
