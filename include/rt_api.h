@@ -321,7 +321,7 @@ rt_status rt_accum_resolve(rt_accum acc, const rt_frame* frame, void* stream);
  * the built-in default.  rtxplay_gb300/tune.py searches it per workload and
  * keeps the results in a JSON cache. */
 typedef struct {
-    unsigned int wave_log2;            /* rays per wave queue = 2^wave_log2, 16..24 (default 23, or RTX_WAVE) */
+    unsigned int wave_log2;            /* rays per wave queue = 2^wave_log2, 16..26 (default 26, or RTX_WAVE) */
     unsigned int shade_block;          /* threads per shading block: 128, 256, 512 or 1024 (default 512) */
     unsigned int extend_blocks_per_sm; /* persistent traversal blocks per SM, 1..32, capped at what fits
                                           (default: what fits) */

@@ -708,10 +708,11 @@ uint32_t env_u32(const char* name, uint32_t dflt) {
 }
 
 // Launch shape set by rt_tuning_set (process-wide; zero fields: defaults).
-// The defaults are the autotuner's choice for the full C1 frame (1200x800,
-// 500 spp, 7,979,008 triangles): 2^23-ray waves and 512-thread shading
-// blocks, 2840 Mrays/s against 2720 with 2^22 and 256 (the earlier defaults).
-constexpr uint32_t kWaveDefault = 1u << 23;
+// The defaults come from the full C1 frame (1200x800, 500 spp, 7,979,008
+// triangles): 512-thread shading blocks, and waves of 2^26 rays (7.7 GB of
+// queues; fewer waves, so fewer traversal drains and launches per frame):
+// 3019 / 3088 / 3117 / 3132 Mrays/s for 2^23 / 2^24 / 2^25 / 2^26.
+constexpr uint32_t kWaveDefault = 1u << 26;
 constexpr int kShadeBlockDefault = 512;
 std::mutex g_tune_mu;
 rt_tuning g_tune{};
@@ -1462,7 +1463,7 @@ rt_status rt_tuning_set(const rt_tuning* tuning) {
     return guarded([&] {
         rt_tuning t{};
         if (tuning) t = *tuning;
-        RT_REQUIRE(t.wave_log2 == 0 || (t.wave_log2 >= 16 && t.wave_log2 <= 24), "wave_log2 outside 16..24");
+        RT_REQUIRE(t.wave_log2 == 0 || (t.wave_log2 >= 16 && t.wave_log2 <= 26), "wave_log2 outside 16..26");
         RT_REQUIRE(t.shade_block == 0 || t.shade_block == 128 || t.shade_block == 256 || t.shade_block == 512 ||
                        t.shade_block == 1024,
                    "shade_block must be 128, 256, 512 or 1024");

@@ -28,11 +28,11 @@ import time
 
 from . import Launcher, tuning_get, tuning_set
 
-DEFAULT = {"wave_log2": 23, "shade_block": 512, "extend_blocks_per_sm": 0, "refill_below": 12, "steps_per_check": 16}
+DEFAULT = {"wave_log2": 26, "shade_block": 512, "extend_blocks_per_sm": 0, "refill_below": 12, "steps_per_check": 16}
 
 # candidate values per knob (extend_blocks_per_sm 0: as many as fit)
 SPACE = {
-    "wave_log2": (20, 21, 22, 23),
+    "wave_log2": (20, 21, 22, 23, 24, 25, 26),
     "shade_block": (128, 256, 512, 1024),
     "extend_blocks_per_sm": (0, 4, 3, 2),
     "refill_below": (4, 8, 12, 16, 20),

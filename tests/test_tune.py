@@ -98,14 +98,14 @@ def test_tuning_abi_set_get_and_validation(product):
     R = product
     R.tuning_set(None)
     d = R.tuning_get()
-    assert d == {"wave_log2": 23, "shade_block": 512, "extend_blocks_per_sm": 0, "refill_below": 12,
+    assert d == {"wave_log2": 26, "shade_block": 512, "extend_blocks_per_sm": 0, "refill_below": 12,
                  "steps_per_check": 16}
     t = {"wave_log2": 16, "shade_block": 512, "extend_blocks_per_sm": 1, "refill_below": 31, "steps_per_check": 64}
     R.tuning_set(t)
     assert R.tuning_get() == t
     R.tuning_set({"refill_below": 3})   # other fields back to their defaults
     assert R.tuning_get() == {**d, "refill_below": 3}
-    for bad in ({"wave_log2": 15}, {"wave_log2": 25}, {"shade_block": 64}, {"shade_block": 2048},
+    for bad in ({"wave_log2": 15}, {"wave_log2": 27}, {"shade_block": 64}, {"shade_block": 2048},
                 {"extend_blocks_per_sm": 33}, {"refill_below": 32}, {"steps_per_check": 65}):
         with pytest.raises(R.RTError) as e:
             R.tuning_set(bad)
@@ -123,4 +123,4 @@ def test_tuning_reports_the_wave_environment(product, monkeypatch):
     monkeypatch.setenv("RTX_WAVE", str(3 << 20))
     assert R.tuning_get()["wave_log2"] == 21   # rounded down to a power of two
     monkeypatch.delenv("RTX_WAVE")
-    assert R.tuning_get()["wave_log2"] == 23
+    assert R.tuning_get()["wave_log2"] == 26
