@@ -725,6 +725,42 @@ __global__ void k_sah_stitch(const SahSplit* __restrict__ splits, uint32_t nspli
     }
 }
 
+// Side streams of the level loop.  A level's big, block and warp nodes cover
+// disjoint record ranges and share only atomic counters (children and clusters
+// are allocated by atomics; where they land does not reach the tree), so the
+// block-node and warp-node kernels run beside the big nodes' chain of small
+// kernels (C1: 17.7 -> 16.4 ms per build, the same tree).  One set per host
+// thread, made on the thread's current device.
+struct SahStreams {
+    int dev = -1;
+    cudaStream_t side[2] = {nullptr, nullptr};
+    cudaEvent_t fork = nullptr, join[2] = {nullptr, nullptr};
+    void release() noexcept {
+        for (int k = 0; k < 2; ++k) {
+            if (side[k]) cudaStreamDestroy(side[k]);
+            if (join[k]) cudaEventDestroy(join[k]);
+            side[k] = nullptr;
+            join[k] = nullptr;
+        }
+        if (fork) cudaEventDestroy(fork);
+        fork = nullptr;
+        dev = -1;
+    }
+    void ensure() {
+        int d = 0;
+        RT_CUDA(cudaGetDevice(&d));
+        if (d == dev) return;
+        release();
+        for (int k = 0; k < 2; ++k) {
+            RT_CUDA(cudaStreamCreateWithFlags(&side[k], cudaStreamNonBlocking));
+            RT_CUDA(cudaEventCreateWithFlags(&join[k], cudaEventDisableTiming));
+        }
+        RT_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+        dev = d;
+    }
+    ~SahStreams() { release(); }
+};
+
 template <class T>
 T* carve(char*& p, size_t count) {
     T* r = reinterpret_cast<T*>(p);
@@ -814,6 +850,8 @@ void build_sah_topology(Lbvh& L, uint32_t cluster_max, cudaStream_t s) {
     static thread_local DevBuf scratch;
     scratch.reserve(layout(reinterpret_cast<char*>(uintptr_t(256))));
     layout(scratch.as<char>());
+    static thread_local SahStreams ss;
+    ss.ensure();
 
     SahCounters c0{};
     c0.next[0][kBig] = uint32_t(seed_big.size());
@@ -846,6 +884,31 @@ void build_sah_topology(Lbvh& L, uint32_t cluster_max, cudaStream_t s) {
         RT_CUDA(cudaMemsetAsync(ctr->next[nx], 0, sizeof(ctr->next[nx]), s));
         const SahOut out{big[nx], block[nx], warp[nx], clusters, splits, ctr, nx, cluster_max};
         const int median_only = level >= kSahMaxLevels ? 1 : 0;
+        // block and warp nodes on the side streams when another kind shares the level
+        const bool fork = int(nb != 0) + int(nbl != 0) + int(nw != 0) >= 2;
+        cudaStream_t s_block = s, s_warp = s;
+        if (fork) {
+            RT_CUDA(cudaEventRecord(ss.fork, s));   // after the counters are cleared
+            if (nbl) {
+                RT_CUDA(cudaStreamWaitEvent(ss.side[0], ss.fork, 0));
+                s_block = ss.side[0];
+            }
+            if (nw) {
+                RT_CUDA(cudaStreamWaitEvent(ss.side[1], ss.fork, 0));
+                s_warp = ss.side[1];
+            }
+        }
+        if (nbl) {
+            k_sah_node<<<nbl, kSahThreads, 0, s_block>>>(rec[cur], rec[nx], block[cur], out_ids, out, nsplit + nb,
+                                                         median_only);
+            RT_CHECK_LAUNCH();
+        }
+        if (nw) {
+            const uint32_t wpb = kSahThreads / 32;
+            k_sah_warp<<<(nw + wpb - 1) / wpb, kSahThreads, 0, s_warp>>>(rec[cur], rec[nx], warp[cur], nw, out_ids,
+                                                                         out, nsplit + nb + nbl, median_only);
+            RT_CHECK_LAUNCH();
+        }
         if (nb) {
             SahNode* nodes = big[cur];
             k_sah_nchunks<<<(nb + kSahThreads - 1) / kSahThreads, kSahThreads, 0, s>>>(nodes, nb, nch);
@@ -870,16 +933,12 @@ void build_sah_topology(Lbvh& L, uint32_t cluster_max, cudaStream_t s) {
             k_sah_partition<<<bound, kSahThreads, 0, s>>>(rec[cur], rec[nx], nodes, nb, chunk_scan, out_ids, out);
             RT_CHECK_LAUNCH();
         }
-        if (nbl) {
-            k_sah_node<<<nbl, kSahThreads, 0, s>>>(rec[cur], rec[nx], block[cur], out_ids, out, nsplit + nb,
-                                                   median_only);
-            RT_CHECK_LAUNCH();
-        }
-        if (nw) {
-            const uint32_t wpb = kSahThreads / 32;
-            k_sah_warp<<<(nw + wpb - 1) / wpb, kSahThreads, 0, s>>>(rec[cur], rec[nx], warp[cur], nw, out_ids, out,
-                                                                   nsplit + nb + nbl, median_only);
-            RT_CHECK_LAUNCH();
+        if (fork) {   // the level's kernels are done before its counters are read
+            for (int k = 0; k < 2; ++k) {
+                if (k == 0 ? !nbl : !nw) continue;
+                RT_CUDA(cudaEventRecord(ss.join[k], ss.side[k]));
+                RT_CUDA(cudaStreamWaitEvent(s, ss.join[k], 0));
+            }
         }
         RT_CUDA(cudaMemcpyAsync(&hc, ctr, sizeof hc, cudaMemcpyDeviceToHost, s));
         RT_CUDA(cudaStreamSynchronize(s));
