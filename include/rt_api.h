@@ -118,7 +118,11 @@ rt_status rt_camera_set(rt_camera* cam, rt_float3 eye, rt_float3 pat, rt_float3 
 /* ---------------------------------------------------------------- scene */
 typedef struct rt_scene_s* rt_scene;
 
-/* Scene::Scene / ~Scene (optx/scene.cxx:38-45; optx/scene.h:19-63). */
+/* Scene::Scene / ~Scene (optx/scene.cxx:38-45; optx/scene.h:19-63).
+ * rt_scene_destroy waits for the device (as freeing device memory does) and
+ * keeps the scene's hierarchy arrays for the next scene this host thread
+ * builds on the same device, instead of freeing and allocating them again;
+ * rt_scene_destroy(NULL) frees the arrays so kept. */
 rt_status rt_scene_create(rt_scene* out);
 rt_status rt_scene_destroy(rt_scene scene);
 

@@ -263,6 +263,12 @@ def rtow_spheres(rng_kind=RT_RECIPE_GLIBC, seed=1, half_extent=11):
     return dict(centers=c, radii=r, types=types, albedos=alb, fuzz=fuzz, index=index)
 
 
+def free_spare_scene_arrays():
+    """Frees the hierarchy arrays a destroyed scene left for the next scene
+    this thread builds (rt_scene_destroy(NULL))."""
+    check(lib().rt_scene_destroy(None))
+
+
 class Scene:
     """Owns an rt_scene handle (the reference's class Scene, optx/scene.h:19-63)."""
 

@@ -1085,7 +1085,11 @@ void render_jobs_ws(const Geometry& g, const std::vector<Job>& jobs, cudaStream_
             reinterpret_cast<const void*>(uintptr_t(L.tn.steps)),
             L.qs.q[0].ori, L.qs.q[0].gn, L.qs.q[1].ori, L.qs.q[1].gn, L.hits, L.hthing, L.st, L.jobs,
             reinterpret_cast<const void*>(uintptr_t(nj)), L.geo.tnodes, L.geo.tprims, L.geo.tedges, L.geo.bnodes,
-            L.geo.bprims,
+            L.geo.bprims, reinterpret_cast<const void*>(uintptr_t(L.geo.ntnodes)),
+            reinterpret_cast<const void*>(uintptr_t(L.geo.ntprims)), reinterpret_cast<const void*>(uintptr_t(L.geo.nbnodes)),
+            reinterpret_cast<const void*>(uintptr_t(L.geo.nbprims)), reinterpret_cast<const void*>(uintptr_t(L.geo.nthings)),
+            reinterpret_cast<const void*>(uintptr_t(L.geo.instanced)), reinterpret_cast<const void*>(uintptr_t(L.lim.x)),
+            reinterpret_cast<const void*>(uintptr_t(L.lim.y)),
             L.geo.inst, L.geo.desc, L.things, L.acc.col[0], L.acc.gd[0], reinterpret_cast<const void*>(uintptr_t(total_pix)),
             reinterpret_cast<const void*>(uintptr_t(any_guides))};
         if (!ws.graph.exec || ws.graph.key != key) {

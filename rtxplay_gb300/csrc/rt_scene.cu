@@ -11,6 +11,7 @@
 #include <cstring>
 #include <limits>
 #include <numeric>
+#include <memory>
 #include <vector>
 
 #include "rt_scene.h"
@@ -1020,8 +1021,31 @@ Scene* scene_from(rt_scene h) {
 
 namespace {
 
+// The device arrays of the last scene destroyed on this host thread, kept for
+// the next scene the thread builds: a hierarchy's arrays (1.8 GB for the
+// 8 M-triangle C1 scene) are handed on instead of freed and allocated again
+// (a new C1 scene per frame: 1.6 ms of cudaFree per destroy and 0.6 ms of
+// cudaMalloc per build).  rt_scene_destroy(NULL) frees them.
+struct SpareGeometry {
+    int dev = -1;
+    std::unique_ptr<Geometry> geo;
+};
+SpareGeometry& spare_geometry() {
+    static thread_local SpareGeometry sp;
+    return sp;
+}
+
 void scene_build(Scene& sc, int morton_bits, cudaStream_t s) {
     sc.built = false;   // a build that fails half way leaves no renderable scene behind
+    if (!sc.geo.top.nodes.p) {   // a first build: take the spare arrays of this device, if any
+        SpareGeometry& sp = spare_geometry();
+        int dev = 0;
+        RT_CUDA(cudaGetDevice(&dev));
+        if (sp.geo && sp.dev == dev) {
+            sc.geo = std::move(*sp.geo);
+            sp.geo.reset();
+        }
+    }
     build_geometry(sc.geo, {&sc}, morton_bits, sc.layout, s);
     sc.built = true;
     sc.topology_dirty = false;
@@ -1104,7 +1128,20 @@ rt_status rt_scene_create(rt_scene* out) {
 
 rt_status rt_scene_destroy(rt_scene scene) {
     return guarded([&] {
-        if (scene) delete reinterpret_cast<Scene*>(scene);
+        SpareGeometry& sp = spare_geometry();
+        if (!scene) {   // frees the arrays kept from the last destroyed scene
+            sp.geo.reset();
+            sp.dev = -1;
+            return;
+        }
+        std::unique_ptr<Scene> sc(reinterpret_cast<Scene*>(scene));
+        int dev = 0;
+        // as cudaFree would, wait for every launch that may still read the arrays
+        if (sc->geo.top.nodes.p && cudaGetDevice(&dev) == cudaSuccess && cudaDeviceSynchronize() == cudaSuccess) {
+            sp.geo.reset();   // the previous spare's arrays are freed here
+            sp.geo = std::make_unique<Geometry>(std::move(sc->geo));
+            sp.dev = dev;
+        }
     });
 }
 
