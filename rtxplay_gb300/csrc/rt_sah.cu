@@ -692,6 +692,33 @@ __global__ void k_sah_codes(const float4* __restrict__ prims, const uint32_t* __
     ids[i] = id;
 }
 
+// Records of every cluster in (code, position) order: a stable insertion sort
+// per cluster of at most kSahLocalSort records, one thread each.  Cluster
+// ranks rise with position, so this is the order a stable radix sort of the
+// full keys (rank << 30 | code) gives, without its passes over all records
+// (C1: 8 M keys of 49 bits, 7 passes).
+constexpr uint32_t kSahLocalSort = 32;
+__global__ void k_sah_sort_clusters(const SegDev* __restrict__ tsegs, uint32_t ncl, unsigned long long* codes,
+                                    uint32_t* ids) {
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= ncl) return;
+    const SegDev sg = tsegs[r];
+    unsigned long long* c = codes + sg.prim_begin;
+    uint32_t* d = ids + sg.prim_begin;
+    for (uint32_t i = 1; i < sg.prim_count; ++i) {
+        const unsigned long long key = c[i];
+        const uint32_t val = d[i];
+        uint32_t j = i;
+        while (j > 0 && c[j - 1] > key) {
+            c[j] = c[j - 1];
+            d[j] = d[j - 1];
+            --j;
+        }
+        c[j] = key;
+        d[j] = val;
+    }
+}
+
 // One thread per split node: it moves to slot split - 1 (the spare slot of
 // the cluster ending at its split); its children become references (split
 // child: its slot; cluster of two or more records: the cluster's root slot,
@@ -972,9 +999,14 @@ void build_sah_topology(Lbvh& L, uint32_t cluster_max, cudaStream_t s) {
     k_sah_codes<<<(n + kSahThreads - 1) / kSahThreads, kSahThreads, 0, s>>>(L.prims_flat.as<float4>(), out_ids, n,
                                                                              tsegs, ncl, tcb, codes, ids);
     RT_CHECK_LAUNCH();
-    int cl_bits = 1;
-    while ((uint64_t(1) << cl_bits) < ncl) ++cl_bits;
-    radix_sort_pairs_u64(codes, ids, n, 30 + cl_bits, L.sort_tmp, s);
+    if (cluster_max <= kSahLocalSort) {
+        k_sah_sort_clusters<<<(ncl + kSahThreads - 1) / kSahThreads, kSahThreads, 0, s>>>(tsegs, ncl, codes, ids);
+        RT_CHECK_LAUNCH();
+    } else {
+        int cl_bits = 1;
+        while ((uint64_t(1) << cl_bits) < ncl) ++cl_bits;
+        radix_sort_pairs_u64(codes, ids, n, 30 + cl_bits, L.sort_tmp, s);
+    }
     int* parents = L.parents.as<int>();
     k_karras<unsigned long long><<<(n + kSahThreads - 1) / kSahThreads, kSahThreads, 0, s>>>(
         codes, tsegs, ncl, n, L.nodes.as<float4>(), parents, parents + n);
