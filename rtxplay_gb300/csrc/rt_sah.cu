@@ -879,6 +879,9 @@ void build_sah_topology(Lbvh& L, uint32_t cluster_max, cudaStream_t s) {
     layout(scratch.as<char>());
     static thread_local SahStreams ss;
     ss.ensure();
+    // a build that stopped with an error between a fork and its join may have
+    // left kernels on the side streams; they finish before the scratch is reused
+    for (int k = 0; k < 2; ++k) RT_CUDA(cudaStreamSynchronize(ss.side[k]));
 
     SahCounters c0{};
     c0.next[0][kBig] = uint32_t(seed_big.size());
