@@ -444,7 +444,9 @@ __device__ __forceinline__ void xbox(float lo, float hi, float sc, float tr, flo
 // Measured on C1 at 64 spp: 2251 -> 2301 Mrays/s.  (Keeping the stack's top
 // entry in a register, so that a pop's node fetch need not wait for a
 // local-memory load, measured 1.5 % slower: 2291 against 2327, more spills
-// at 48 registers.)
+// at 48 registers.  With the wave queues evict-first, an L1 evict-last
+// priority on node loads made no difference and an L2 evict-last cache
+// policy cost 3 %.)
 __device__ __forceinline__ void ld_node(const float4* p, float4& n0, float4& n1, float4& n2, float4& n3) {
     asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
         : "=f"(n0.x), "=f"(n0.y), "=f"(n0.z), "=f"(n0.w), "=f"(n1.x), "=f"(n1.y), "=f"(n1.z), "=f"(n1.w)
