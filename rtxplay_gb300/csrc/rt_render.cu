@@ -311,8 +311,12 @@ __global__ void __launch_bounds__(kThreads)
 constexpr uint32_t kRefillBelow = 12;
 constexpr int kStepsPerCheck = 16;
 
+// Flat layouts: 48 registers (five 256-thread blocks per SM) set as a register
+// cap rather than as a minimum of resident blocks: the compiled kernel differs
+// and measured 0.9 % faster (C1: traversal 335.8 -> 332.4 ms per frame); 192- or
+// 224-thread blocks (42 warps per SM instead of 40) were 3-4 % slower.
 template <bool kInst>
-__global__ void __launch_bounds__(kThreads, kInst ? 4 : 5)
+__global__ void __launch_bounds__(kThreads, kInst ? 4 : 1) __maxnreg__(kInst ? 64 : 48)
     k_extend_p(Queues qs, float4* __restrict__ hits, uint32_t* __restrict__ hthing, WaveState* st,
                const JobDev* __restrict__ jobs, GeoView g, ExtTune tn) {
     const uint32_t cur = *((volatile uint32_t*)&st->cur);
