@@ -121,8 +121,9 @@ typedef struct rt_scene_s* rt_scene;
 /* Scene::Scene / ~Scene (optx/scene.cxx:38-45; optx/scene.h:19-63).
  * rt_scene_destroy waits for the device (as freeing device memory does) and
  * keeps the scene's hierarchy arrays for the next scene this host thread
- * builds on the same device, instead of freeing and allocating them again;
- * rt_scene_destroy(NULL) frees the arrays so kept. */
+ * builds on the same device, instead of freeing and allocating them again
+ * (that scene takes them if they hold at most about twice its records, else
+ * they are freed); rt_scene_destroy(NULL) frees the arrays so kept. */
 rt_status rt_scene_create(rt_scene* out);
 rt_status rt_scene_destroy(rt_scene scene);
 

@@ -1042,7 +1042,13 @@ void scene_build(Scene& sc, int morton_bits, cudaStream_t s) {
         int dev = 0;
         RT_CUDA(cudaGetDevice(&dev));
         if (sp.geo && sp.dev == dev) {
-            sc.geo = std::move(*sp.geo);
+            // records this scene will have (a sphere or instance is one, a
+            // flattened mesh thing its triangles): arrays sized for more than
+            // twice as many are freed rather than held by a smaller scene
+            uint64_t recs = 0;
+            for (const ThingHost& th : sc.things)
+                recs += th.mesh >= 0 && size_t(th.mesh) < sc.meshes.size() ? sc.meshes[size_t(th.mesh)].ni : 1u;
+            if (uint64_t(sp.geo->top.nprims) <= 2 * recs + 65536) sc.geo = std::move(*sp.geo);
             sp.geo.reset();
         }
     }
