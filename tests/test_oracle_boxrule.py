@@ -99,3 +99,26 @@ def test_hierarchy_returns_closest_over_records_whose_box_passes(worlds):
     assert 0 < differ.sum() < len(o) // 100
     # every difference is the ground sphere's root above its box
     assert np.all(pb[differ] == 0) and np.all(o[differ, 1] + tb[differ] * d[differ, 1] > 0.0)
+
+
+def test_triangles_hierarchy_equals_brute_force(oracle):
+    """The final scene tessellated (level 2): rays leaving random points of the
+    triangles, some with a zero direction component -- the flat LBVH and the
+    binned-SAH hierarchy return brute force's closest hit, bit for bit."""
+    rng = np.random.default_rng(3)
+    for cluster in (0, 16):
+        wd, _ = oracle.rtow_world(2, 0, 1, 11, sah_cluster=cluster)
+        tri = wd.triangles().reshape(-1, 3, 3).astype(np.float64)
+        n = 30000
+        k = rng.integers(0, len(tri), n)
+        u, v = rng.random(n), rng.random(n)
+        flip = u + v > 1
+        u[flip], v[flip] = 1 - u[flip], 1 - v[flip]
+        o = (tri[k, 0] + u[:, None] * (tri[k, 1] - tri[k, 0]) + v[:, None] * (tri[k, 2] - tri[k, 0])).astype(np.float32)
+        d = rng.normal(size=(n, 3)).astype(np.float32)
+        z = rng.random(n) < 0.1
+        d[z, rng.integers(0, 3, z.sum())] = 0.0
+        pb, tb = wd.closest(o, d, "brute")
+        ph, th = wd.closest(o, d, "bvh")
+        assert np.array_equal(ph, pb)
+        assert np.array_equal(th.view(np.uint32), tb.view(np.uint32))
