@@ -95,7 +95,10 @@ private:
 class Scene {
 public:
     Scene() { check(rt_scene_create(&h_), "rt_scene_create"); }
+    // ~Scene keeps the hierarchy arrays for the next scene this thread builds
+    // (rt_scene_destroy); free_spare_arrays() frees them
     virtual ~Scene() { rt_scene_destroy(h_); }
+    static void free_spare_arrays() { check(rt_scene_destroy(nullptr), "rt_scene_destroy"); }
     Scene(const Scene&) = delete;
     Scene& operator=(const Scene&) = delete;
 
